@@ -1,0 +1,250 @@
+/*
+ * frehg_gb300.h -- C ABI of the GB300 (sm_103a) groundwater hot path.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes, no exceptions and no
+ * library types across the boundary.  Every entry point names the reference interface it
+ * replaces (paths relative to the zLi90/frehg source tree).
+ *
+ * Two handle families:
+ *   frehg_re_*      -- the Richards-equation step (replaces class ReSolver,
+ *                      src/re/ReSolver.hpp:48-156).  State lives in device memory; the step
+ *                      runs entirely on the GPU.
+ *   frehg_cg_*,     -- the linear-solver seam (replaces LinearSolver / SparseSystem,
+ *   frehg_system_*     include/frehg2/linear/LinearSolver.hpp:18-33, SparseSystem.hpp:15-40)
+ *                      for callers that assemble a 7-point system row by row.
+ *
+ * Layout conventions
+ *   interior arrays : i fastest, then j, then k (k = 0 is the top layer); index i + j*nx + k*nx*ny.
+ *                     This is the order ReSolver::setInitialHead takes (ReSolver.cpp:155-173).
+ *   halo arrays     : (nx+2)*(ny+2)*(nz+2), index (i+1) + (j+1)(nx+2) + (k+1)(nx+2)(ny+2)
+ *                     (Grid::getIndex, src/core/Grid.hpp:186-188).
+ *   owned order     : the linear-solver row order of Decomp3D on one rank, k fastest:
+ *                     row = (j*nx + i)*nz + k (src/linear/DomainDecomposition.cpp:235-245).
+ *
+ * Threading: one CUDA stream per handle; a handle is not thread-safe; handles are independent.
+ */
+#ifndef FREHG_GB300_H
+#define FREHG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------------ */
+/* Status codes.  The reference throws std::runtime_error (PetscLinearSolver.cpp:21-25,206-211); */
+/* the C++ wrappers in include/frehg2_gpu.hpp turn any non-zero code into that exception.      */
+/* ------------------------------------------------------------------------------------------ */
+enum {
+  FREHG_OK = 0,
+  FREHG_ERR_BAD_ARG = 1,        /* invalid argument (size, range, null pointer)              */
+  FREHG_ERR_CUDA = 2,           /* a CUDA runtime call failed                                */
+  FREHG_ERR_NOT_CONVERGED = 3,  /* Krylov solve diverged or hit max_it (KSP reason < 0)      */
+  FREHG_ERR_NONFINITE = 4,      /* NaN/Inf met in a reduction                                */
+  FREHG_ERR_STATE = 5,          /* call out of order (e.g. advance before initial state)     */
+  FREHG_ERR_UNSUPPORTED = 6,    /* configuration the build does not realise                  */
+  FREHG_ERR_NO_DEVICE = 7       /* no CUDA device / extension not loadable                   */
+};
+
+/* Text of the last error raised on the calling thread ("" when none). */
+const char* frehg_last_error(void);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Parameter blocks                                                                            */
+/* ------------------------------------------------------------------------------------------ */
+
+/* struct SoilParams (include/frehg2/re/SoilParams.hpp:13-25), same fields and defaults. */
+typedef struct frehg_soil_params {
+  double alpha;     /* VG alpha [1/m]                                 default 1.43    */
+  double n;         /* VG n                                           default 1.56    */
+  double theta_s;   /* saturated water content                        default 0.33    */
+  double theta_r;   /* residual water content                         default 0.0     */
+  double Ks_x;      /* saturated conductivity [m/s]                   default 0.0     */
+  double Ks_y;      /*                                                default 0.0     */
+  double Ks_z;      /*                                                default 2.89e-6 */
+  double Ss;        /* specific storage [1/m]                         default 1e-5    */
+  int32_t use_vg;   /* van Genuchten (1) or exponential (0)           default 1       */
+  int32_t use_mvg;  /* modified VG with air entry                     default 0       */
+  double air_entry; /* air-entry head [m]                             default -0.02   */
+} frehg_soil_params;
+
+/* struct ReParams (src/re/ReSolver.hpp:24-46) plus the extensions marked "not in reference". */
+typedef struct frehg_re_params {
+  frehg_soil_params soil; /* uniform soil / class 0                                          */
+  double dx, dy, dz;      /* cell sizes [m]                 defaults 1, 1, 0.01              */
+  double botz;            /* domain bottom elevation        default -1                       */
+  double dt;              /* time step [s]                  default 1e-4                     */
+  double dt_min, dt_max;  /* adaptive bounds                defaults 1e-4, 2                 */
+  double co_max;          /* Courant limit                  default 2                        */
+  int32_t adaptive_dt;    /* default 1 */
+  int32_t use_corrector;  /* default 1 */
+  int32_t use_full3d;     /* default 0 */
+  int32_t follow_terrain; /* default 0 (1 is rejected: not realised by the reference step)    */
+  int32_t sim_shallowwater; /* default 0 (coupled top face)                                   */
+  int32_t baroclinic;     /* default 0 (1 is rejected, as Orchestrator.cpp:136-137 does)      */
+  int32_t bc_type[6];     /* x-, x+, y-, y+, z+ (bottom), z- (top); 0 no-flux, 1 Dirichlet,
+                             2 fixed flux; 3 unit-gradient free drainage (bottom, not in
+                             reference).  default {0,0,0,0,0,1}                              */
+  double htop, hbot;      /* Dirichlet heads [m]                                             */
+  double qtop, qbot;      /* fixed fluxes [m/s]; qtop<0 = infiltration, qbot>0 = inflow      */
+  /* ---- not in reference (spec extensions) ---- */
+  int32_t scheme;         /* 0 = PCA predictor-corrector (ReSolver::advanceStep),
+                             1 = mixed-form modified Picard (Celia et al. 1990)               */
+  int32_t face_mean;      /* 0 = arithmetic 0.5(Kp+Km) (reference), 1 = harmonic              */
+  int32_t picard_max_it;  /* default 50                                                      */
+  double picard_tol;      /* |dh|_inf stopping test [m], default 1e-6                        */
+  double rain_rate;       /* time-varying top flux: qtop = rain_rate while t < rain_until    */
+  double rain_until;      /* [s]; rain_rate = 0 disables (default)                           */
+  int32_t picard_dt_adapt;/* Picard-count driven dt (1) or fixed (0)                         */
+  int32_t pad_;
+} frehg_re_params;
+
+/* struct SolverConfig (include/frehg2/linear/SolverConfig.hpp:14-20) plus precision keys. */
+typedef struct frehg_solver_config {
+  char ksp_type[16];      /* "cg" (default) or "fcg"                                         */
+  char pc_type[16];       /* "jacobi" (default here), "none", "unet"                         */
+  double rtol;            /* default 1e-8                                                    */
+  double atol;            /* default 1e-50                                                   */
+  int32_t max_it;         /* default 10000                                                   */
+  int32_t precision;      /* 0 = fp64 throughout, 1 = fp32 Krylov under fp64 refinement      */
+  double ir_rtol;         /* refinement stop: true relative residual, default 1e-10          */
+  double inner_rtol;      /* fp32 inner solve relative tolerance, default 1e-4               */
+} frehg_solver_config;
+
+void frehg_soil_params_default(frehg_soil_params* s);
+void frehg_re_params_default(frehg_re_params* p);
+void frehg_solver_config_default(frehg_solver_config* c);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Richards-equation step: replaces ReSolver (src/re/ReSolver.hpp:48-156).                      */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct frehg_re frehg_re;
+
+/* ReSolver(const Grid&, const MpiComm*) + setParams (ReSolver.hpp:50,53).  Allocates the device
+ * state for an nx*ny*nz grid on the current CUDA device. */
+int frehg_re_create(int nx, int ny, int nz, const frehg_re_params* p, frehg_re** out);
+int frehg_re_destroy(frehg_re* re);
+/* ReSolver::setParams (ReSolver.hpp:53).  Grid sizes stay fixed. */
+int frehg_re_set_params(frehg_re* re, const frehg_re_params* p);
+int frehg_re_get_params(const frehg_re* re, frehg_re_params* p);
+
+/* ReSolver::setSoilMap (ReSolver.hpp:59) with SoilMap::setClasses + setClassIndex/3D
+ * (src/soil/SoilMap.hpp:33-43).  class_index has nx*ny (is3d = 0) or nx*ny*nz (is3d = 1)
+ * entries in interior order; every id must lie in [0, nclass). */
+int frehg_re_set_soil_map(frehg_re* re, const frehg_soil_params* classes, int nclass,
+                          const int32_t* class_index, int is3d);
+/* Not in reference: per-cell overrides of Ks (all three directions) and of alpha, as needed by
+ * continuous random soil fields.  Either pointer may be NULL.  Interior order, nx*ny*nz each. */
+int frehg_re_set_cell_fields(frehg_re* re, const double* Ks, const double* alpha);
+
+/* ReSolver::attachSolver (ReSolver.hpp:67): the RE step uses cfg for its head solve. */
+int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg);
+
+/* ReSolver::initializeGeometry / setInitialWaterContent / setInitialHead /
+ * finalizeInitialState / initializeUniformColumn (ReSolver.hpp:73-79, ReSolver.cpp:104-188).
+ * Host arrays, interior order. */
+int frehg_re_initialize_geometry(frehg_re* re);
+int frehg_re_set_initial_head(frehg_re* re, const double* h);
+int frehg_re_set_initial_water_content(frehg_re* re, const double* wc);
+int frehg_re_finalize_initial_state(frehg_re* re);
+int frehg_re_initialize_uniform_column(frehg_re* re, double init_wc);
+
+/* ReSolver::setTopFluxField (ReSolver.hpp:105): nx*ny values, index i + j*nx. */
+int frehg_re_set_top_flux_field(frehg_re* re, const double* q);
+
+/* ReSolver::advanceStep (ReSolver.cpp:931-969). */
+int frehg_re_advance_step(frehg_re* re);
+/* Convenience: nsteps calls of advanceStep on the handle's stream without host round trips
+ * other than the Krylov convergence checks. */
+int frehg_re_advance_steps(frehg_re* re, int nsteps);
+
+/* ReSolver::dt / dtUsed / setDt / primeAdaptiveDt (ReSolver.hpp:87-98). */
+int frehg_re_dt(const frehg_re* re, double* dt);
+int frehg_re_dt_used(const frehg_re* re, double* dt);
+int frehg_re_set_dt(frehg_re* re, double dt);
+int frehg_re_prime_adaptive_dt(frehg_re* re, double dt);
+/* Simulated time accumulated by advance_step [s] (not in reference; the driver keeps it). */
+int frehg_re_time(const frehg_re* re, double* t);
+
+/* ReSolver::fields() (ReSolver.hpp:84): copy one named GwFields array (src/re/GwFields.hpp:52-59)
+ * to host memory in the halo layout ((nx+2)(ny+2)(nz+2) doubles).  Supported names:
+ * h hn wc wcn wch hwc ch Kx Ky Kz qx qy qz room dz3d actv bot3d. */
+int frehg_re_get_field(frehg_re* re, const char* name, double* out_halo);
+/* Interior copy (nx*ny*nz, interior order) of h, wc, hn or wcn; device_out != 0 means out is a
+ * device pointer (device-to-device copy). */
+int frehg_re_get_interior(frehg_re* re, const char* name, double* out, int device_out);
+
+/* Perf counters (src/perf: cells_touched = cells*steps ReSolver.cpp:933, ksp_iterations :621). */
+typedef struct frehg_re_counters {
+  int64_t steps;
+  int64_t cells_touched;
+  int64_t ksp_iterations;
+  int64_t picard_iterations;
+  int64_t realloc_sweeps;
+  int32_t last_ksp_iterations;
+  int32_t last_picard_iterations;
+  double last_residual_norm;
+} frehg_re_counters;
+int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c);
+
+/* Total water volume sum(theta*V) in FP64 (Orchestrator.cpp:924-930 "water_vol_subs"), and the
+ * cumulative top / bottom boundary inflow volumes (not in reference). */
+int frehg_re_water_volume(frehg_re* re, double* vol);
+int frehg_re_boundary_volumes(frehg_re* re, double* top_in, double* bottom_in);
+
+/* Stream control: all work of the handle is issued on this stream (cudaStream_t passed as
+ * void*; NULL = the handle's own stream).  frehg_re_sync waits for it. */
+int frehg_re_set_stream(frehg_re* re, void* cuda_stream);
+int frehg_re_sync(frehg_re* re);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Linear-solver seam: replaces LinearSolver + SparseSystem + makeLinearSolver                  */
+/* (include/frehg2/linear/LinearSolver.hpp:18-33, SparseSystem.hpp:15-40,                       */
+/*  src/linear/backends/LinearSolverFactory.cpp:9-16).                                         */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct frehg_cg frehg_cg;
+typedef struct frehg_system frehg_system;
+
+/* makeLinearSolver("gb300", cfg).  Unknown ksp/pc types give FREHG_ERR_UNSUPPORTED, as the
+ * reference factory throws for an unknown backend (LinearSolverFactory.cpp:14-15). */
+int frehg_cg_create(const frehg_solver_config* cfg, frehg_cg** out);
+int frehg_cg_destroy(frehg_cg* cg);
+
+/* LinearSolver::createSystem(const DecompBase&) + SparseSystem::preallocate for the 7-point
+ * Decomp3D of one rank (nz = 1 gives the 5-point Decomp2D, row = j*nx + i). */
+int frehg_system_create(frehg_cg* cg, int nx, int ny, int nz, frehg_system** out);
+int frehg_system_destroy(frehg_system* sys);
+int frehg_system_zero_entries(frehg_system* sys);     /* SparseSystem::zeroEntries   */
+int frehg_system_begin_assembly(frehg_system* sys);   /* SparseSystem::beginAssembly */
+int frehg_system_end_assembly(frehg_system* sys);     /* SparseSystem::endAssembly   */
+/* SparseSystem::addRow: ADD_VALUES semantics; every column must be the row itself or one of its
+ * 7-point neighbours, else FREHG_ERR_BAD_ARG. */
+int frehg_system_add_row(frehg_system* sys, int global_row, int ncols, const int* cols,
+                         const double* vals);
+/* SparseSystem::addCOO: n triplets, duplicates summed (KokkosPetscBridgeDevice.cpp:55-61).
+ * on_device != 0: the three arrays are device pointers. */
+int frehg_system_add_coo(frehg_system* sys, const int* rows, const int* cols, const double* vals,
+                         int64_t n, int on_device);
+/* SparseSystem::setRhs / getSolution (owned order). */
+int frehg_system_set_rhs(frehg_system* sys, const double* b, int on_device);
+int frehg_system_get_solution(frehg_system* sys, double* x, int on_device);
+
+/* LinearSolver::setup / solve (PetscLinearSolver.cpp:186-220): zero initial guess, stop when
+ * the preconditioned residual norm <= max(rtol*||B b||, atol).  b and x are owned-order host
+ * arrays (or device arrays when on_device != 0). */
+int frehg_cg_setup(frehg_cg* cg, frehg_system* sys);
+int frehg_cg_solve(frehg_cg* cg, frehg_system* sys, const double* b, double* x, int on_device);
+int frehg_cg_iteration_count(const frehg_cg* cg, int* its);   /* getIterationCount */
+int frehg_cg_residual_norm(const frehg_cg* cg, double* rnorm); /* getResidualNorm   */
+int frehg_cg_converged_reason(const frehg_cg* cg, int* reason); /* KSPConvergedReason */
+
+/* Build information: returns the sm architecture the library was compiled for (e.g. 103). */
+int frehg_build_arch(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FREHG_GB300_H */
