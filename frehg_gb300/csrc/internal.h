@@ -1,0 +1,150 @@
+// Shared internals of libfrehg_gb300: error plumbing, the device Krylov solver, soil tables.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/frehg_gb300.h"
+
+namespace fg {
+
+// ------------------------------------------------------------------------------------------
+// errors: every C entry point returns an int status and records text for frehg_last_error().
+void set_error(const char* fmt, ...);
+void clear_error();
+
+#define FG_CUDA(call)                                                                    \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      ::fg::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+      return FREHG_ERR_CUDA;                                                             \
+    }                                                                                    \
+  } while (0)
+
+#define FG_TRY(expr)            \
+  do {                          \
+    int rc_ = (expr);           \
+    if (rc_ != FREHG_OK) return rc_; \
+  } while (0)
+
+#define FG_ARG(cond, ...)                  \
+  do {                                     \
+    if (!(cond)) {                         \
+      ::fg::set_error(__VA_ARGS__);        \
+      return FREHG_ERR_BAD_ARG;            \
+    }                                      \
+  } while (0)
+
+// Upper bound of the blocks any reduction kernel launches (partials buffers are sized to it).
+constexpr int kMaxRedBlocks = 4096;
+constexpr int kNumSMs = 152;
+
+// ------------------------------------------------------------------------------------------
+// 7-point symmetric stencil operator on an n0 x n1 x n2 box (axis 0 fastest).
+// Before scaling: d = diagonal, a0/a1/a2 = coupling of cell c with its +1 neighbour along each
+// axis (0 where that neighbour does not exist).  After scale(): a* hold D^-1/2 A D^-1/2
+// couplings and s = D^-1/2, so the operator has a unit diagonal (Jacobi PCG == CG on it).
+struct Stencil64 {
+  int n0 = 0, n1 = 0, n2 = 0;
+  size_t n = 0;
+  double* a0 = nullptr;
+  double* a1 = nullptr;
+  double* a2 = nullptr;
+  double* s = nullptr;  // holds d before scale(), D^-1/2 after
+  double* b = nullptr;  // right-hand side (unscaled)
+  bool scaled = false;
+  int alloc(int n0, int n1, int n2);
+  void release();
+};
+
+// Single-precision copy of a scaled operator (the inner solve of the mixed-precision path).
+struct Stencil32 {
+  size_t n = 0;
+  float* a0 = nullptr;
+  float* a1 = nullptr;
+  float* a2 = nullptr;
+  int alloc(size_t n);
+  void release();
+};
+
+// Device-resident Krylov state (PETSc KSPSolve_CG + KSPConvergedDefault scalars).
+struct CgDevState {
+  double beta, betaold, bcoef, a, dpi, dpiold, dp, rnorm0, ttol;
+  double rtol, atol, divtol;
+  int its, max_it, status, iter;
+  unsigned int arrive[8];
+  double ir_bnorm, ir_rnorm;  // refinement loop norms (mixed precision)
+  int ir_its, pad_;
+};
+
+// KSPConvergedReason values
+enum {
+  kConvergedRtol = 2,
+  kConvergedAtol = 3,
+  kDivergedIts = -3,
+  kDivergedDtol = -4,
+  kDivergedIndefinitePc = -8,
+  kDivergedNanOrInf = -9,
+  kDivergedIndefiniteMat = -10,
+};
+
+struct CgResult {
+  int its = 0;
+  int reason = 0;
+  double rnorm = 0.0;
+  int inner_its = 0;  // mixed precision: total fp32 iterations
+  int ir_its = 0;     // mixed precision: refinement sweeps
+};
+
+// Jacobi-preconditioned CG in FP64 (3 kernels per iteration, CUDA-graph chunks), with an
+// optional FP32 inner solve under FP64 iterative refinement.
+class KrylovSolver {
+ public:
+  ~KrylovSolver();
+  int ensure(size_t n);  // work vectors for up to n unknowns
+  // Scale the operator in place (s = D^-1/2, a* -> D^-1/2 A D^-1/2).  Idempotent.
+  int scale(Stencil64& A, cudaStream_t st);
+  // Solve A x = b (A scaled, b unscaled in A.b).  x_out receives the unscaled solution.
+  int solve(Stencil64& A, double* x_out, const frehg_solver_config& cfg, cudaStream_t st,
+            CgResult* res);
+
+  size_t cap = 0;
+  double *x = nullptr, *r = nullptr, *p = nullptr, *w = nullptr;
+  double* partials = nullptr;
+  CgDevState* dst = nullptr;
+  CgDevState* hst = nullptr;  // pinned mirror
+  // mixed precision buffers
+  float *xf = nullptr, *rf = nullptr, *pf = nullptr, *wf = nullptr;
+  double* rres = nullptr;  // fp64 true residual
+  Stencil32 op32;
+  // graphs
+  cudaGraphExec_t g64 = nullptr;
+  cudaGraphExec_t g32 = nullptr;
+  const void* g64_key = nullptr;
+  const void* g32_key = nullptr;
+  cudaStream_t g_stream = nullptr;
+  size_t g_n = 0;
+
+ private:
+  int solve64(Stencil64& A, double* x_out, const frehg_solver_config& cfg, cudaStream_t st,
+              CgResult* res);
+  int solve_mixed(Stencil64& A, double* x_out, const frehg_solver_config& cfg, cudaStream_t st,
+                  CgResult* res);
+  int run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk);
+};
+
+// Launch helpers shared by the stencil kernels: a (32 x 8) thread tile over axes 0/1 marching
+// along axis 2 in slabs.
+struct StencilLaunch {
+  dim3 grid, block;
+  int planes;  // axis-2 planes per block
+};
+StencilLaunch stencil_launch(int n0, int n1, int n2);
+
+int reduction_blocks(size_t n, int threads, int per_thread);
+
+}  // namespace fg

@@ -1,0 +1,464 @@
+// Krylov solver on the GPU: Jacobi-preconditioned CG for a 7-point SPD stencil.
+//
+// Replaces the PETSc KSP solve behind PetscLinearSolver::solve
+// (src/linear/backends/PetscLinearSolver.cpp:200-220): KSPSolve_CG with the preconditioned
+// residual norm, zero initial guess and KSPConvergedDefault (converged when
+// ||B r|| <= max(rtol*||B b||, atol); divergence when ||B r|| >= 1e4*||B b||, NaN/Inf,
+// indefinite matrix or preconditioner, or max_it).
+//
+// GB300 design:
+//  * The operator is scaled once per solve to unit diagonal: A~ = D^-1/2 A D^-1/2.  CG on A~
+//    is Jacobi-PCG on A (x~ = D^1/2 x, r~ = D^-1/2 r, beta = r.z = r~.r~, p'Ap = p~'A~p~,
+//    ||B r|| = ||s r~|| with s = D^-1/2), so the diagonal is never stored or multiplied and
+//    no divisions remain in the loop.
+//  * Three kernels per iteration (p-update, stencil SpMV + p.w, update + two norms); every
+//    reduction ends in the last-arriving block, which also runs the scalar part of the
+//    algorithm (alpha, beta, stopping test) on the device.  Kernels of a converged solve
+//    return at once, so iterations are captured in a CUDA graph of `chunk` iterations and
+//    the host only reads the status between chunks.  Reductions are deterministic (fixed
+//    block partition, fixed summation tree).
+//  * FP64 is 1/64 of the FP32 rate on GB300, so the kernels are arranged to keep the FP64
+//    instruction count per cell low (13 FMA-class ops per iteration) as well as the bytes.
+#include "internal.h"
+#include "reduce.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace fg {
+
+// KSPConvergedDefault
+__device__ __forceinline__ int converged_test(CgDevState* s, double rnorm) {
+  if (isnan(rnorm) || isinf(rnorm)) return kDivergedNanOrInf;
+  if (rnorm <= s->ttol) return rnorm < s->atol ? kConvergedAtol : kConvergedRtol;
+  if (s->divtol > 0.0 && rnorm >= s->divtol * s->rnorm0) return kDivergedDtol;
+  return 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// geometry helpers
+
+StencilLaunch stencil_launch(int n0, int n1, int n2) {
+  StencilLaunch L;
+  L.block = dim3(32, 8, 1);
+  const int t0 = (n0 + 31) / 32, t1 = (n1 + 7) / 8;
+  const long tiles = (long)t0 * t1;
+  const long target = (long)kNumSMs * 8;
+  long z = target / (tiles > 0 ? tiles : 1);
+  if (z < 1) z = 1;
+  if (z > n2) z = n2;
+  int planes = (int)((n2 + z - 1) / z);
+  z = (n2 + planes - 1) / planes;
+  L.planes = planes;
+  L.grid = dim3((unsigned)tiles, (unsigned)z, 1);
+  return L;
+}
+
+int reduction_blocks(size_t n, int threads, int per_thread) {
+  size_t b = (n + (size_t)threads * per_thread - 1) / ((size_t)threads * per_thread);
+  if (b < 1) b = 1;
+  if (b > (size_t)kNumSMs * 8) b = (size_t)kNumSMs * 8;
+  return (int)b;
+}
+
+// ------------------------------------------------------------------------------------------
+// operator scaling
+
+__global__ void k_diag_rsqrt(double* __restrict__ s, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    double d = s[c];
+    if (d == 0.0) d = 1.0;  // PCJacobi replaces a zero diagonal entry by 1
+    s[c] = 1.0 / sqrt(d);   // NaN for d < 0: the solve then stops with DIVERGED_NANORINF
+  }
+}
+
+__global__ void k_scale_offdiag(double* __restrict__ a0, double* __restrict__ a1,
+                                double* __restrict__ a2, const double* __restrict__ s, int n0,
+                                int n1, int n2, int planes) {
+  const int t0 = (n0 + 31) / 32;
+  const int i0 = (blockIdx.x % t0) * 32 + threadIdx.x;
+  const int i1 = (blockIdx.x / t0) * 8 + threadIdx.y;
+  if (i0 >= n0 || i1 >= n1) return;
+  const size_t s01 = (size_t)n0 * n1;
+  const int kb = blockIdx.y * planes;
+  const int ke = min(n2, kb + planes);
+  for (int k = kb; k < ke; ++k) {
+    const size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * k;
+    const double sc = s[c];
+    if (i0 + 1 < n0) a0[c] *= sc * s[c + 1]; else a0[c] = 0.0;
+    if (i1 + 1 < n1) a1[c] *= sc * s[c + n0]; else a1[c] = 0.0;
+    if (k + 1 < n2) a2[c] *= sc * s[c + s01]; else a2[c] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// FP64 CG kernels
+
+// r~ = s b, x~ = 0; ||B b|| and beta = r~.r~; iteration-0 stopping test.
+__global__ void k_cg_init(const double* __restrict__ s, const double* __restrict__ b,
+                          double* __restrict__ x, double* __restrict__ r, size_t n,
+                          CgDevState* st, double* partials) {
+  double v[2] = {0.0, 0.0};
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const double sc = s[c];
+    const double rc = sc * b[c];
+    r[c] = rc;
+    x[c] = 0.0;
+    v[0] = fma(rc, rc, v[0]);
+    const double z = sc * rc;
+    v[1] = fma(z, z, v[1]);
+  }
+  double tot[2];
+  if (!grid_sum<2>(v, partials, &st->arrive[0], tot)) return;
+  if (flat_tid() == 0) {
+    const double dp = sqrt(tot[1]);
+    st->dp = dp;
+    st->rnorm0 = dp;
+    st->ttol = fmax(st->rtol * dp, st->atol);
+    st->its = 0;
+    st->iter = 0;
+    st->dpi = 0.0;
+    st->beta = tot[0];
+    st->status = converged_test(st, dp);
+    if (!st->status && st->beta == 0.0) {  // loop top of iteration 0
+      st->its = 1;
+      st->status = kConvergedAtol;
+    }
+  }
+}
+
+// p = r~ (first iteration) or p = r~ + bcoef p
+__global__ void k_cg_p(const double* __restrict__ r, double* __restrict__ p, size_t n,
+                       const CgDevState* st) {
+  if (st->status) return;
+  const double bc = st->bcoef;
+  const bool first = st->iter == 0;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    p[c] = first ? r[c] : fma(bc, p[c], r[c]);
+  }
+}
+
+// w = A~ p (unit diagonal) and p.w; the last block forms alpha.
+template <typename T, typename Acc>
+__device__ __forceinline__ Acc spmv_cell(const T* __restrict__ p, const T* __restrict__ a0,
+                                         const T* __restrict__ a1, size_t c, int i0, int i1,
+                                         int n0, int n1, T pc) {
+  Acc v = (Acc)pc;
+  if (i0 > 0) v = fma((Acc)a0[c - 1], (Acc)p[c - 1], v);
+  if (i0 + 1 < n0) v = fma((Acc)a0[c], (Acc)p[c + 1], v);
+  if (i1 > 0) v = fma((Acc)a1[c - n0], (Acc)p[c - n0], v);
+  if (i1 + 1 < n1) v = fma((Acc)a1[c], (Acc)p[c + n0], v);
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_cg_spmv(const double* __restrict__ a0,
+                                                 const double* __restrict__ a1,
+                                                 const double* __restrict__ a2,
+                                                 const double* __restrict__ p,
+                                                 double* __restrict__ w, int n0, int n1, int n2,
+                                                 int planes, CgDevState* st, double* partials) {
+  if (st->status) return;
+  const int t0 = (n0 + 31) / 32;
+  const int i0 = (blockIdx.x % t0) * 32 + threadIdx.x;
+  const int i1 = (blockIdx.x / t0) * 8 + threadIdx.y;
+  double acc[1] = {0.0};
+  if (i0 < n0 && i1 < n1) {
+    const size_t s01 = (size_t)n0 * n1;
+    const int kb = blockIdx.y * planes;
+    const int ke = min(n2, kb + planes);
+    size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
+    double pm = 0.0, am = 0.0;
+    if (kb > 0) {
+      pm = p[c - s01];
+      am = a2[c - s01];
+    }
+    double pc = p[c];
+    for (int k = kb; k < ke; ++k) {
+      const double pp = (k + 1 < n2) ? p[c + s01] : 0.0;
+      const double ac = a2[c];
+      double v = spmv_cell<double, double>(p, a0, a1, c, i0, i1, n0, n1, pc);
+      v = fma(am, pm, v);
+      v = fma(ac, pp, v);
+      w[c] = v;
+      acc[0] = fma(pc, v, acc[0]);
+      pm = pc;
+      pc = pp;
+      am = ac;
+      c += s01;
+    }
+  }
+  double tot[1];
+  if (!grid_sum<1>(acc, partials, &st->arrive[1], tot)) return;
+  if (flat_tid() == 0) {
+    const double dpi = tot[0];
+    st->its = st->iter + 1;
+    if (dpi == 0.0 || (st->iter > 0 && ((dpi > 0.0) != (st->dpi > 0.0))) || isnan(dpi)) {
+      st->status = isnan(dpi) ? kDivergedNanOrInf : kDivergedIndefiniteMat;
+      return;
+    }
+    st->dpiold = st->dpi;
+    st->dpi = dpi;
+    st->a = st->beta / dpi;
+  }
+}
+
+// x~ += a p, r~ -= a w, then ||B r|| and beta = r~.r~; the last block runs the stopping test
+// and prepares the next iteration's beta ratio.
+__global__ void k_cg_update(double* __restrict__ x, double* __restrict__ r,
+                            const double* __restrict__ p, const double* __restrict__ w,
+                            const double* __restrict__ s, size_t n, CgDevState* st,
+                            double* partials) {
+  if (st->status) return;
+  const double a = st->a;
+  double v[2] = {0.0, 0.0};
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    x[c] = fma(a, p[c], x[c]);
+    const double rc = fma(-a, w[c], r[c]);
+    r[c] = rc;
+    v[0] = fma(rc, rc, v[0]);
+    const double z = s[c] * rc;
+    v[1] = fma(z, z, v[1]);
+  }
+  double tot[2];
+  if (!grid_sum<2>(v, partials, &st->arrive[2], tot)) return;
+  if (flat_tid() == 0) {
+    const double dp = sqrt(tot[1]);
+    st->dp = dp;
+    const int reason = converged_test(st, dp);
+    if (reason) {
+      st->status = reason;
+      return;
+    }
+    st->betaold = st->beta;
+    st->beta = tot[0];
+    st->iter += 1;
+    if (st->iter >= st->max_it) {
+      st->status = kDivergedIts;
+      return;
+    }
+    st->its = st->iter + 1;
+    if (st->beta == 0.0) {
+      st->status = kConvergedAtol;
+      return;
+    }
+    st->bcoef = st->beta / st->betaold;
+    if (st->bcoef < 0.0) st->status = kDivergedIndefinitePc;
+  }
+}
+
+__global__ void k_unscale(const double* __restrict__ s, const double* __restrict__ xs,
+                          double* __restrict__ x, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x)
+    x[c] = s[c] * xs[c];
+}
+
+// ------------------------------------------------------------------------------------------
+// host side
+
+int Stencil64::alloc(int n0_, int n1_, int n2_) {
+  release();
+  n0 = n0_;
+  n1 = n1_;
+  n2 = n2_;
+  n = (size_t)n0 * n1 * n2;
+  FG_CUDA(cudaMalloc(&a0, n * sizeof(double)));
+  FG_CUDA(cudaMalloc(&a1, n * sizeof(double)));
+  FG_CUDA(cudaMalloc(&a2, n * sizeof(double)));
+  FG_CUDA(cudaMalloc(&s, n * sizeof(double)));
+  FG_CUDA(cudaMalloc(&b, n * sizeof(double)));
+  scaled = false;
+  return FREHG_OK;
+}
+
+void Stencil64::release() {
+  cudaFree(a0);
+  cudaFree(a1);
+  cudaFree(a2);
+  cudaFree(s);
+  cudaFree(b);
+  a0 = a1 = a2 = s = b = nullptr;
+  n = 0;
+}
+
+int Stencil32::alloc(size_t n_) {
+  release();
+  n = n_;
+  FG_CUDA(cudaMalloc(&a0, n * sizeof(float)));
+  FG_CUDA(cudaMalloc(&a1, n * sizeof(float)));
+  FG_CUDA(cudaMalloc(&a2, n * sizeof(float)));
+  return FREHG_OK;
+}
+
+void Stencil32::release() {
+  cudaFree(a0);
+  cudaFree(a1);
+  cudaFree(a2);
+  a0 = a1 = a2 = nullptr;
+  n = 0;
+}
+
+KrylovSolver::~KrylovSolver() {
+  if (g64) cudaGraphExecDestroy(g64);
+  if (g32) cudaGraphExecDestroy(g32);
+  cudaFree(x);
+  cudaFree(r);
+  cudaFree(p);
+  cudaFree(w);
+  cudaFree(partials);
+  cudaFree(dst);
+  cudaFreeHost(hst);
+  cudaFree(xf);
+  cudaFree(rf);
+  cudaFree(pf);
+  cudaFree(wf);
+  cudaFree(rres);
+  op32.release();
+}
+
+int KrylovSolver::ensure(size_t n) {
+  if (n <= cap && x) return FREHG_OK;
+  cudaFree(x);
+  cudaFree(r);
+  cudaFree(p);
+  cudaFree(w);
+  x = r = p = w = nullptr;
+  if (g64) {
+    cudaGraphExecDestroy(g64);
+    g64 = nullptr;
+  }
+  FG_CUDA(cudaMalloc(&x, n * sizeof(double)));
+  FG_CUDA(cudaMalloc(&r, n * sizeof(double)));
+  FG_CUDA(cudaMalloc(&p, n * sizeof(double)));
+  FG_CUDA(cudaMalloc(&w, n * sizeof(double)));
+  if (!partials) FG_CUDA(cudaMalloc(&partials, 4 * kMaxRedBlocks * sizeof(double)));
+  if (!dst) {
+    FG_CUDA(cudaMalloc(&dst, sizeof(CgDevState)));
+    FG_CUDA(cudaMemset(dst, 0, sizeof(CgDevState)));
+    FG_CUDA(cudaMallocHost(&hst, sizeof(CgDevState)));
+  }
+  cap = n;
+  return FREHG_OK;
+}
+
+int KrylovSolver::scale(Stencil64& A, cudaStream_t st) {
+  if (A.scaled) return FREHG_OK;
+  const int nb = reduction_blocks(A.n, 256, 4);
+  k_diag_rsqrt<<<nb, 256, 0, st>>>(A.s, A.n);
+  FG_CUDA(cudaGetLastError());
+  const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
+  k_scale_offdiag<<<L.grid, L.block, 0, st>>>(A.a0, A.a1, A.a2, A.s, A.n0, A.n1, A.n2, L.planes);
+  FG_CUDA(cudaGetLastError());
+  A.scaled = true;
+  return FREHG_OK;
+}
+
+// Run a captured chunk graph until the device status leaves "running" or max_it is reached.
+int KrylovSolver::run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk) {
+  const int max_launch = max_it / chunk + 2;
+  for (int q = 0; q < max_launch; ++q) {
+    FG_CUDA(cudaGraphLaunch(g, st));
+    FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    if (hst->status != 0) return FREHG_OK;
+  }
+  set_error("Krylov loop: device status still running after %d chunk launches", max_launch);
+  return FREHG_ERR_STATE;
+}
+
+int KrylovSolver::solve(Stencil64& A, double* x_out, const frehg_solver_config& cfg,
+                        cudaStream_t st, CgResult* res) {
+  FG_TRY(ensure(A.n));
+  FG_TRY(scale(A, st));
+  if (cfg.precision == 1) return solve_mixed(A, x_out, cfg, st, res);
+  return solve64(A, x_out, cfg, st, res);
+}
+
+static int chunk_for(size_t n) {
+  if (n >= (size_t)4 << 20) return 16;
+  if (n >= (size_t)1 << 18) return 32;
+  return 64;
+}
+
+int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config& cfg,
+                          cudaStream_t st, CgResult* res) {
+  const size_t n = A.n;
+  // stopping parameters
+  CgDevState init;
+  memset(&init, 0, sizeof(init));
+  init.rtol = cfg.rtol;
+  init.atol = cfg.atol;
+  init.divtol = 1.0e4;
+  init.max_it = cfg.max_it;
+  FG_CUDA(cudaMemcpyAsync(dst, &init, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+  const int nb = reduction_blocks(n, 256, 4);
+  k_cg_init<<<nb, 256, 0, st>>>(A.s, A.b, x, r, n, dst, partials);
+  FG_CUDA(cudaGetLastError());
+
+  const int chunk = chunk_for(n);
+  const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
+  const bool rebuild = !g64 || g64_key != (const void*)&A || g_stream != st || g_n != n;
+  if (rebuild) {
+    if (g64) cudaGraphExecDestroy(g64);
+    g64 = nullptr;
+    cudaStream_t cap_st;
+    FG_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
+    cudaGraph_t graph;
+    FG_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
+    for (int q = 0; q < chunk; ++q) {
+      k_cg_p<<<nb, 256, 0, cap_st>>>(r, p, n, dst);
+      k_cg_spmv<<<L.grid, L.block, 0, cap_st>>>(A.a0, A.a1, A.a2, p, w, A.n0, A.n1, A.n2,
+                                                L.planes, dst, partials);
+      k_cg_update<<<nb, 256, 0, cap_st>>>(x, r, p, w, A.s, n, dst, partials);
+    }
+    cudaError_t e = cudaStreamEndCapture(cap_st, &graph);
+    cudaStreamDestroy(cap_st);
+    if (e != cudaSuccess) {
+      set_error("graph capture failed: %s", cudaGetErrorString(e));
+      return FREHG_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&g64, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      set_error("graph instantiate failed: %s", cudaGetErrorString(e));
+      return FREHG_ERR_CUDA;
+    }
+    g64_key = &A;
+    g_stream = st;
+    g_n = n;
+  }
+  // iteration 0 may already have converged
+  FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+  FG_CUDA(cudaStreamSynchronize(st));
+  if (hst->status == 0) FG_TRY(run_chunks(g64, st, cfg.max_it, chunk));
+  k_unscale<<<nb, 256, 0, st>>>(A.s, x, x_out, n);
+  FG_CUDA(cudaGetLastError());
+  res->its = hst->its;
+  res->reason = hst->status;
+  res->rnorm = hst->dp;
+  res->inner_its = hst->its;
+  res->ir_its = 0;
+  if (hst->status < 0) {
+    set_error("KSP diverged (reason %d) after %d iterations, residual norm %g", hst->status,
+              hst->its, hst->dp);
+    return hst->status == kDivergedNanOrInf ? FREHG_ERR_NONFINITE : FREHG_ERR_NOT_CONVERGED;
+  }
+  return FREHG_OK;
+}
+
+int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_config& cfg,
+                              cudaStream_t st, CgResult* res) {
+  (void)A;
+  (void)x_out;
+  (void)cfg;
+  (void)st;
+  (void)res;
+  set_error("mixed-precision Krylov path is not built in this version");
+  return FREHG_ERR_UNSUPPORTED;
+}
+
+}  // namespace fg

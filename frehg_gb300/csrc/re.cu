@@ -1,0 +1,815 @@
+// frehg_re_*: the Richards-equation step on one GPU (replaces class ReSolver,
+// src/re/ReSolver.hpp:48-156 / src/re/ReSolver.cpp).  The whole step runs on the device; the
+// host only issues launches and reads the Krylov / reallocation status words.
+#include "internal.h"
+#include "re_kernels.cuh"
+#include "picard.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+using namespace fg;
+
+struct frehg_re {
+  int nx = 0, ny = 0, nz = 0;
+  size_t n = 0, ncol = 0;
+  frehg_re_params p;
+  frehg_solver_config cfg;
+  bool attached = false;
+  bool have_geometry = false;
+  bool have_state = false;
+  bool finalized = false;
+  bool ghosts_valid = false;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  int cur = 0;
+  // state
+  double* H[2] = {nullptr, nullptr};
+  double* W[2] = {nullptr, nullptr};
+  double* kr = nullptr;
+  double* wch = nullptr;
+  double* qx = nullptr;
+  double* qy = nullptr;
+  double* qz = nullptr;
+  double* qztop = nullptr;
+  double* qtop_field = nullptr;
+  bool has_qtop = false;
+  uint8_t* flags = nullptr;
+  double* scratch = nullptr;  // n doubles for exports / Picard increments
+  ReScalars* sc = nullptr;
+  ReScalars* sc_host = nullptr;
+  double* partials = nullptr;
+  // soil
+  SoilClass* cls = nullptr;
+  int nclass = 0;
+  uint8_t* cid = nullptr;
+  int cid3d = 0;
+  double* fKs = nullptr;
+  double* falpha = nullptr;
+  // operator + Krylov
+  Stencil64 A;
+  KrylovSolver ksp;
+  // counters
+  frehg_re_counters cnt;
+  ~frehg_re();
+};
+
+frehg_re::~frehg_re() {
+  for (int q = 0; q < 2; ++q) {
+    cudaFree(H[q]);
+    cudaFree(W[q]);
+  }
+  cudaFree(kr);
+  cudaFree(wch);
+  cudaFree(qx);
+  cudaFree(qy);
+  cudaFree(qz);
+  cudaFree(qztop);
+  cudaFree(qtop_field);
+  cudaFree(flags);
+  cudaFree(scratch);
+  cudaFree(sc);
+  cudaFreeHost(sc_host);
+  cudaFree(partials);
+  cudaFree(cls);
+  cudaFree(cid);
+  cudaFree(fKs);
+  cudaFree(falpha);
+  A.release();
+  if (own_stream) cudaStreamDestroy(own_stream);
+}
+
+static SoilClass make_class(const frehg_soil_params& s) {
+  SoilClass k;
+  k.alpha = s.alpha;
+  k.n = s.n;
+  k.ths = s.theta_s;
+  k.thr = s.theta_r;
+  k.Ksx = s.Ks_x;
+  k.Ksy = s.Ks_y;
+  k.Ksz = s.Ks_z;
+  k.Ss = s.Ss;
+  k.aev = s.air_entry;
+  k.m = 1.0 - 1.0 / s.n;
+  k.inv_m = 1.0 / k.m;
+  k.inv_n = 1.0 / s.n;
+  k.use_vg = s.use_vg;
+  k.use_mvg = s.use_mvg;
+  return k;
+}
+
+static int validate_params(const frehg_re_params* p) {
+  FG_ARG(p->dx > 0 && p->dy > 0 && p->dz > 0, "dx, dy, dz must be positive");
+  FG_ARG(p->scheme == 0 || p->scheme == 1, "scheme must be 0 (pca) or 1 (picard)");
+  for (int q = 0; q < 4; ++q)
+    if (p->bc_type[q] != 0) {
+      set_error(
+          "bc_type[%d]: lateral Dirichlet/fixed-flux GW boundaries are not implemented; only "
+          "no-flux (0) is supported on lateral faces",
+          q);
+      return FREHG_ERR_UNSUPPORTED;
+    }
+  const int bmax = p->scheme == 1 ? 3 : 2;
+  FG_ARG(p->bc_type[4] >= 0 && p->bc_type[4] <= bmax, "bc_type[4] (bottom) must be in [0,%d]", bmax);
+  FG_ARG(p->bc_type[5] >= 0 && p->bc_type[5] <= 2, "bc_type[5] (top) must be 0, 1 or 2");
+  if (p->baroclinic) {
+    set_error("baroclinic (density-driven) coupling is not implemented");
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  if (p->sim_shallowwater) {
+    set_error("sim_shallowwater: the coupled top face belongs to the SW-GW coupling, not built");
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  if (p->follow_terrain) {
+    set_error("follow_terrain is not realised by the groundwater step");
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  return FREHG_OK;
+}
+
+static int upload_class0(frehg_re* re) {
+  if (re->nclass > 0 && re->cid) return FREHG_OK;  // a soil map owns the table
+  const SoilClass k = make_class(re->p.soil);
+  if (!re->cls) FG_CUDA(cudaMalloc(&re->cls, sizeof(SoilClass) * 256));
+  FG_CUDA(cudaMemcpy(re->cls, &k, sizeof(SoilClass), cudaMemcpyHostToDevice));
+  re->nclass = 1;
+  return FREHG_OK;
+}
+
+static ReArgs make_args(frehg_re* re) {
+  ReArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nx = re->nx;
+  a.ny = re->ny;
+  a.nz = re->nz;
+  a.n = re->n;
+  a.ncol = re->ncol;
+  a.dx = re->p.dx;
+  a.dy = re->p.dy;
+  a.dz = re->p.dz;
+  a.htop = re->p.htop;
+  a.hbot = re->p.hbot;
+  a.qtop = re->p.qtop;
+  a.qbot = re->p.qbot;
+  a.co_max = re->p.co_max;
+  a.dt_min = re->p.dt_min;
+  a.dt_max = re->p.dt_max;
+  a.bc4 = re->p.bc_type[4];
+  a.bc5 = re->p.bc_type[5];
+  a.full3d = re->p.use_full3d;
+  a.ghosts_valid = re->ghosts_valid;
+  a.adaptive = re->p.adaptive_dt;
+  a.use_corrector = re->p.use_corrector;
+  a.has_qtop = re->has_qtop;
+  a.soil.cls = re->cls;
+  a.soil.cid = re->cid;
+  a.soil.cid3d = re->cid3d;
+  a.soil.Ks = re->fKs;
+  a.soil.alpha = re->falpha;
+  a.h_old = re->H[re->cur];
+  a.w_old = re->W[re->cur];
+  a.h_new = re->H[1 - re->cur];
+  a.w_new = re->W[1 - re->cur];
+  a.kr = re->kr;
+  a.wch = re->wch;
+  a.qx = re->qx;
+  a.qy = re->qy;
+  a.qz = re->qz;
+  a.qztop = re->qztop;
+  a.qtop_field = re->qtop_field;
+  a.flags = re->flags;
+  a.sc = re->sc;
+  a.partials = re->partials;
+  return a;
+}
+
+// ------------------------------------------------------------------------------------------
+// simple device helpers for the C API
+
+namespace {
+__global__ void k_theta_of_h(ReArgs a, const double* __restrict__ h, double* __restrict__ w) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const CellSoil s = soil_of(a.soil, c, c % a.ncol);
+    w[c] = vg_theta(s, h[c]);
+  }
+}
+__global__ void k_h_of_theta(ReArgs a, const double* __restrict__ w, double* __restrict__ h) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const CellSoil s = soil_of(a.soil, c, c % a.ncol);
+    h[c] = vg_head(s, w[c]);
+  }
+}
+__global__ void k_cap_of_h(ReArgs a, const double* __restrict__ h, double* __restrict__ o) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const CellSoil s = soil_of(a.soil, c, c % a.ncol);
+    o[c] = vg_capacity(s, h[c]);
+  }
+}
+// face conductances Kx/Ky/Kz as computeKFace leaves them after the step (post-solve head = the
+// kr array, vertical-only closure by the step's starting water content)
+__global__ void k_faces_export(ReArgs a, const double* __restrict__ wstart, int which,
+                               double* __restrict__ o) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = c % a.ncol;
+    const int k = (int)(c / a.ncol), i = (int)(col % a.nx), j = (int)(col / a.nx);
+    const CellSoil s = soil_of(a.soil, c, col);
+    const double krc = a.kr[c];
+    const bool sat_c = a.full3d ? true : wstart[c] >= s.ths;
+    double v = 0.0;
+    if (which == 0) {
+      double Kn = 0.0;
+      bool sat_n = true;
+      if (i + 1 < a.nx) {
+        const CellSoil sn = soil_of(a.soil, c + 1, col + 1);
+        Kn = sn.Ksx * a.kr[c + 1];
+        if (!a.full3d) sat_n = wstart[c + 1] >= sn.ths;
+      }
+      v = face_x(a, i, s.Ksx * krc, Kn, s.Ksx * krc, sat_c, sat_n);
+    } else if (which == 1) {
+      double Kn = 0.0;
+      bool sat_n = true;
+      if (j + 1 < a.ny) {
+        const CellSoil sn = soil_of(a.soil, c + a.nx, col + a.nx);
+        Kn = sn.Ksy * a.kr[c + a.nx];
+        if (!a.full3d) sat_n = wstart[c + a.nx] >= sn.ths;
+      }
+      v = face_y(a, j, s.Ksy * krc, Kn, s.Ksy * krc, sat_c, sat_n);
+    } else {
+      double Kn = 0.0;
+      if (k + 1 < a.nz) {
+        const CellSoil sn = soil_of(a.soil, c + a.ncol, col);
+        Kn = sn.Ksz * a.kr[c + a.ncol];
+      }
+      v = face_z(a, k, s.Ksz * krc, Kn);
+    }
+    o[c] = v;
+  }
+}
+__global__ void k_volume(ReArgs a, const double* __restrict__ w, double* out) {
+  double v[1] = {0.0};
+  const double V = a.dx * a.dy * a.dz;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x)
+    v[0] += w[c] * V;
+  double tot[1];
+  if (grid_sum<1>(v, a.partials, &a.sc->arrive[3], tot) && flat_tid() == 0) *out = tot[0];
+}
+}  // namespace
+
+static int nblocks(size_t n) { return reduction_blocks(n, 256, 4); }
+
+// ------------------------------------------------------------------------------------------
+// PCA step (ReSolver::advanceStep, ReSolver.cpp:931-969)
+
+static int pca_step(frehg_re* re) {
+  cudaStream_t st = re->stream;
+  ReArgs a = make_args(re);
+  const int nb = nblocks(re->n);
+  k_step_begin<<<1, 1, 0, st>>>(re->sc);
+  // computeKFace inputs at h^n
+  k_kr<<<nb, 256, 0, st>>>(a, a.h_old, re->kr);
+  // groundwaterMatCoeff + groundwaterRhs + assembly
+  const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
+  re->A.scaled = false;
+  k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b);
+  FG_CUDA(cudaGetLastError());
+  // LinearSolver::solve
+  CgResult res;
+  const int rc = re->ksp.solve(re->A, a.h_new, re->cfg, st, &res);
+  re->cnt.last_ksp_iterations = res.its;
+  re->cnt.last_residual_norm = res.rnorm;
+  re->cnt.ksp_iterations += res.its;
+  if (rc != FREHG_OK) return rc;
+  // enforceHeadBc + computeKFace + updateDiagnostics at h^{n+1} (the solve wrote h^{n+1})
+  k_post<<<nb, 256, 0, st>>>(a);
+  FG_CUDA(cudaGetLastError());
+  // groundwaterFlux + updateWaterContent (+ dq of adaptiveTimeStep, boundary budgets)
+  k_correct<<<L.grid, L.block, 0, st>>>(a);
+  FG_CUDA(cudaGetLastError());
+  // reallocateWaterContent: relax to the sequential sweep's fixed point
+  const int top_sat = (re->p.bc_type[5] == 1 && re->p.htop >= 0.0) ? 1 : 0;
+  const int cb = (int)((re->ncol + 127) / 128);
+  const int max_sweeps = (int)re->n + 2;
+  int sweeps = 0;
+  for (;;) {
+    FG_CUDA(cudaMemsetAsync(&re->sc->changed, 0, sizeof(int), st));
+    k_realloc_sweep<<<cb, 128, 0, st>>>(a, top_sat);
+    FG_CUDA(cudaGetLastError());
+    ++sweeps;
+    int changed = 0;
+    FG_CUDA(cudaMemcpyAsync(&re->sc_host->changed, &re->sc->changed, sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    changed = re->sc_host->changed;
+    if (!changed) break;
+    if (sweeps > max_sweeps) {
+      set_error("reallocation relaxation did not settle after %d sweeps", sweeps);
+      return FREHG_ERR_STATE;
+    }
+  }
+  re->cnt.realloc_sweeps += sweeps;
+  // apply reallocation, clampWaterContent, adaptiveTimeStep
+  k_finalize<<<nb, 256, 0, st>>>(a, top_sat);
+  FG_CUDA(cudaGetLastError());
+  re->cur = 1 - re->cur;
+  re->ghosts_valid = true;
+  return FREHG_OK;
+}
+
+static int advance_one(frehg_re* re) {
+  if (!re->finalized) {
+    set_error("advance_step before finalize_initial_state");
+    return FREHG_ERR_STATE;
+  }
+  if (!re->attached) {
+    set_error("advance_step before attach_solver");
+    return FREHG_ERR_STATE;
+  }
+  int rc;
+  if (re->p.scheme == 1)
+    rc = picard_step(re);
+  else
+    rc = pca_step(re);
+  if (rc != FREHG_OK) return rc;
+  re->cnt.steps += 1;
+  re->cnt.cells_touched += (int64_t)re->n;
+  return FREHG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// C API
+
+extern "C" {
+
+int frehg_re_create(int nx, int ny, int nz, const frehg_re_params* p, frehg_re** out) {
+  clear_error();
+  FG_ARG(out != nullptr && p != nullptr, "null argument");
+  FG_ARG(nx > 0 && ny > 0 && nz > 0, "grid sizes must be positive");
+  FG_TRY(validate_params(p));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    set_error("no CUDA device");
+    return FREHG_ERR_NO_DEVICE;
+  }
+  frehg_re* re = new frehg_re();
+  re->nx = nx;
+  re->ny = ny;
+  re->nz = nz;
+  re->ncol = (size_t)nx * ny;
+  re->n = re->ncol * nz;
+  re->p = *p;
+  frehg_solver_config_default(&re->cfg);
+  memset(&re->cnt, 0, sizeof(re->cnt));
+  auto fail = [&](int rc) {
+    delete re;
+    return rc;
+  };
+  const size_t n = re->n;
+#define ALLOC(ptr, bytes)                                      \
+  do {                                                         \
+    if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess) {          \
+      set_error("cudaMalloc of %zu bytes failed", (size_t)(bytes)); \
+      return fail(FREHG_ERR_CUDA);                             \
+    }                                                          \
+  } while (0)
+  for (int q = 0; q < 2; ++q) {
+    ALLOC(re->H[q], n * sizeof(double));
+    ALLOC(re->W[q], n * sizeof(double));
+  }
+  ALLOC(re->kr, n * sizeof(double));
+  ALLOC(re->wch, n * sizeof(double));
+  ALLOC(re->qx, n * sizeof(double));
+  ALLOC(re->qy, n * sizeof(double));
+  ALLOC(re->qz, n * sizeof(double));
+  ALLOC(re->qztop, re->ncol * sizeof(double));
+  ALLOC(re->qtop_field, re->ncol * sizeof(double));
+  ALLOC(re->flags, n);
+  ALLOC(re->scratch, n * sizeof(double));
+  ALLOC(re->sc, sizeof(ReScalars));
+  ALLOC(re->partials, 4 * kMaxRedBlocks * sizeof(double));
+#undef ALLOC
+  if (cudaMallocHost(&re->sc_host, sizeof(ReScalars)) != cudaSuccess) return fail(FREHG_ERR_CUDA);
+  if (re->A.alloc(nx, ny, nz) != FREHG_OK) return fail(FREHG_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&re->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(FREHG_ERR_CUDA);
+  re->stream = re->own_stream;
+  ReScalars s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.dt = p->dt;
+  s0.dtn = 0.0;
+  if (cudaMemcpy(re->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(FREHG_ERR_CUDA);
+  for (int q = 0; q < 2; ++q) {
+    cudaMemset(re->H[q], 0, n * sizeof(double));
+    cudaMemset(re->W[q], 0, n * sizeof(double));
+  }
+  cudaMemset(re->qx, 0, n * sizeof(double));
+  cudaMemset(re->qy, 0, n * sizeof(double));
+  cudaMemset(re->qz, 0, n * sizeof(double));
+  cudaMemset(re->qztop, 0, re->ncol * sizeof(double));
+  if (upload_class0(re) != FREHG_OK) return fail(FREHG_ERR_CUDA);
+  if (re->ksp.ensure(n) != FREHG_OK) return fail(FREHG_ERR_CUDA);
+  *out = re;
+  return FREHG_OK;
+}
+
+int frehg_re_destroy(frehg_re* re) {
+  clear_error();
+  if (re) {
+    cudaStreamSynchronize(re->stream);
+    delete re;
+  }
+  return FREHG_OK;
+}
+
+int frehg_re_set_params(frehg_re* re, const frehg_re_params* p) {
+  clear_error();
+  FG_ARG(re && p, "null argument");
+  FG_TRY(validate_params(p));
+  const double old_dt = re->p.dt;
+  re->p = *p;
+  FG_TRY(upload_class0(re));
+  if (p->dt != old_dt) {
+    FG_CUDA(cudaStreamSynchronize(re->stream));
+    FG_CUDA(cudaMemcpy(&re->sc->dt, &p->dt, sizeof(double), cudaMemcpyHostToDevice));
+  }
+  return FREHG_OK;
+}
+
+int frehg_re_get_params(const frehg_re* re, frehg_re_params* p) {
+  clear_error();
+  FG_ARG(re && p, "null argument");
+  *p = re->p;
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(&p->dt, &re->sc->dt, sizeof(double), cudaMemcpyDeviceToHost));
+  return FREHG_OK;
+}
+
+int frehg_re_set_soil_map(frehg_re* re, const frehg_soil_params* classes, int nclass,
+                          const int32_t* class_index, int is3d) {
+  clear_error();
+  FG_ARG(re && classes && class_index, "null argument");
+  FG_ARG(nclass >= 1 && nclass <= 256, "nclass must be in [1, 256]");
+  const size_t cnt = is3d ? re->n : re->ncol;
+  std::vector<uint8_t> ids(cnt);
+  for (size_t c = 0; c < cnt; ++c) {
+    FG_ARG(class_index[c] >= 0 && class_index[c] < nclass,
+           "soil class id %d at %zu is out of range [0,%d)", class_index[c], c, nclass);
+    ids[c] = (uint8_t)class_index[c];
+  }
+  std::vector<SoilClass> tab(nclass);
+  for (int q = 0; q < nclass; ++q) tab[q] = make_class(classes[q]);
+  if (!re->cls) FG_CUDA(cudaMalloc(&re->cls, sizeof(SoilClass) * 256));
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(re->cls, tab.data(), sizeof(SoilClass) * nclass, cudaMemcpyHostToDevice));
+  cudaFree(re->cid);
+  re->cid = nullptr;
+  FG_CUDA(cudaMalloc(&re->cid, cnt));
+  FG_CUDA(cudaMemcpy(re->cid, ids.data(), cnt, cudaMemcpyHostToDevice));
+  re->cid3d = is3d ? 1 : 0;
+  re->nclass = nclass;
+  return FREHG_OK;
+}
+
+int frehg_re_set_cell_fields(frehg_re* re, const double* Ks, const double* alpha) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  cudaFree(re->fKs);
+  cudaFree(re->falpha);
+  re->fKs = re->falpha = nullptr;
+  if (Ks) {
+    FG_CUDA(cudaMalloc(&re->fKs, re->n * sizeof(double)));
+    FG_CUDA(cudaMemcpy(re->fKs, Ks, re->n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (alpha) {
+    FG_CUDA(cudaMalloc(&re->falpha, re->n * sizeof(double)));
+    FG_CUDA(cudaMemcpy(re->falpha, alpha, re->n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  return FREHG_OK;
+}
+
+int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg) {
+  clear_error();
+  FG_ARG(re && cfg, "null argument");
+  if (strcmp(cfg->ksp_type, "cg") != 0 && strcmp(cfg->ksp_type, "fcg") != 0) {
+    set_error("ksp_type '%s' is not available (cg, fcg)", cfg->ksp_type);
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  if (strcmp(cfg->pc_type, "jacobi") != 0) {
+    set_error("pc_type '%s' is not available on the GPU path (jacobi)", cfg->pc_type);
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  FG_ARG(cfg->rtol > 0 && cfg->max_it > 0, "rtol and max_it must be positive");
+  FG_ARG(cfg->precision == 0 || cfg->precision == 1, "precision must be 0 or 1");
+  re->cfg = *cfg;
+  re->attached = true;
+  return FREHG_OK;
+}
+
+int frehg_re_initialize_geometry(frehg_re* re) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  re->have_geometry = true;  // uniform dz per layer, every cell active (ReSolver.cpp:104-131)
+  return FREHG_OK;
+}
+
+int frehg_re_set_initial_head(frehg_re* re, const double* h) {
+  clear_error();
+  FG_ARG(re && h, "null argument");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(re->H[re->cur], h, re->n * sizeof(double), cudaMemcpyHostToDevice));
+  ReArgs a = make_args(re);
+  k_theta_of_h<<<nblocks(re->n), 256, 0, re->stream>>>(a, re->H[re->cur], re->W[re->cur]);
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  re->have_state = true;
+  return FREHG_OK;
+}
+
+int frehg_re_set_initial_water_content(frehg_re* re, const double* wc) {
+  clear_error();
+  FG_ARG(re && wc, "null argument");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(re->W[re->cur], wc, re->n * sizeof(double), cudaMemcpyHostToDevice));
+  ReArgs a = make_args(re);
+  k_h_of_theta<<<nblocks(re->n), 256, 0, re->stream>>>(a, re->W[re->cur], re->H[re->cur]);
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  re->have_state = true;
+  return FREHG_OK;
+}
+
+int frehg_re_finalize_initial_state(frehg_re* re) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  if (!re->have_state) {
+    set_error("finalize_initial_state before an initial head or water content");
+    return FREHG_ERR_STATE;
+  }
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  // dtn_ = params_.dt (ReSolver.cpp:175-178)
+  FG_CUDA(cudaMemcpy(&re->sc->dtn, &re->sc->dt, sizeof(double), cudaMemcpyDeviceToDevice));
+  re->finalized = true;
+  return FREHG_OK;
+}
+
+int frehg_re_initialize_uniform_column(frehg_re* re, double init_wc) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_TRY(frehg_re_initialize_geometry(re));
+  std::vector<double> w(re->n, init_wc);
+  FG_TRY(frehg_re_set_initial_water_content(re, w.data()));
+  return frehg_re_finalize_initial_state(re);
+}
+
+int frehg_re_set_top_flux_field(frehg_re* re, const double* q) {
+  clear_error();
+  FG_ARG(re && q, "null argument");
+  FG_CUDA(cudaMemcpyAsync(re->qtop_field, q, re->ncol * sizeof(double), cudaMemcpyHostToDevice,
+                          re->stream));
+  re->has_qtop = true;
+  return FREHG_OK;
+}
+
+int frehg_re_advance_step(frehg_re* re) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  return advance_one(re);
+}
+
+int frehg_re_advance_steps(frehg_re* re, int nsteps) {
+  clear_error();
+  FG_ARG(re && nsteps >= 0, "bad argument");
+  for (int q = 0; q < nsteps; ++q) FG_TRY(advance_one(re));
+  return FREHG_OK;
+}
+
+static int read_scalars(const frehg_re* re) {
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
+  return FREHG_OK;
+}
+
+int frehg_re_dt(const frehg_re* re, double* dt) {
+  clear_error();
+  FG_ARG(re && dt, "null argument");
+  FG_TRY(read_scalars(re));
+  *dt = re->sc_host->dt;
+  return FREHG_OK;
+}
+
+int frehg_re_dt_used(const frehg_re* re, double* dt) {
+  clear_error();
+  FG_ARG(re && dt, "null argument");
+  FG_TRY(read_scalars(re));
+  *dt = re->sc_host->dt_used;
+  return FREHG_OK;
+}
+
+int frehg_re_time(const frehg_re* re, double* t) {
+  clear_error();
+  FG_ARG(re && t, "null argument");
+  FG_TRY(read_scalars(re));
+  *t = re->sc_host->time;
+  return FREHG_OK;
+}
+
+int frehg_re_set_dt(frehg_re* re, double dt) {
+  clear_error();
+  FG_ARG(re && dt > 0, "bad argument");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(&re->sc->dt, &dt, sizeof(double), cudaMemcpyHostToDevice));
+  re->p.dt = dt;
+  return FREHG_OK;
+}
+
+int frehg_re_prime_adaptive_dt(frehg_re* re, double dt) {
+  clear_error();
+  FG_ARG(re && dt > 0, "bad argument");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(&re->sc->dt, &dt, sizeof(double), cudaMemcpyHostToDevice));
+  FG_CUDA(cudaMemcpy(&re->sc->dtn, &dt, sizeof(double), cudaMemcpyHostToDevice));
+  re->p.dt = dt;
+  return FREHG_OK;
+}
+
+// fill a halo array ((nx+2)(ny+2)(nz+2)) from an interior array; ghosts by the copy rule
+static void to_halo(const frehg_re* re, const std::vector<double>& in, double* out, bool copy_ghosts,
+                    double top_ghost, bool top_fixed, double bot_ghost, bool bot_fixed) {
+  const int nx = re->nx, ny = re->ny, nz = re->nz;
+  const size_t hx = nx + 2, hy = ny + 2;
+  memset(out, 0, sizeof(double) * hx * hy * (nz + 2));
+  auto H = [&](int i, int j, int k) -> double& {
+    return out[(size_t)(i + 1) + (size_t)(j + 1) * hx + (size_t)(k + 1) * hx * hy];
+  };
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) H(i, j, k) = in[(size_t)i + (size_t)nx * (j + (size_t)ny * k)];
+  if (!copy_ghosts) return;
+  for (int k = 0; k < nz; ++k) {
+    for (int j = 0; j < ny; ++j) {
+      H(-1, j, k) = H(0, j, k);
+      H(nx, j, k) = H(nx - 1, j, k);
+    }
+    for (int i = 0; i < nx; ++i) {
+      H(i, -1, k) = H(i, 0, k);
+      H(i, ny, k) = H(i, ny - 1, k);
+    }
+  }
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      H(i, j, nz) = bot_fixed ? bot_ghost : H(i, j, nz - 1);
+      H(i, j, -1) = top_fixed ? top_ghost : H(i, j, 0);
+    }
+}
+
+int frehg_re_get_interior(frehg_re* re, const char* name, double* out, int device_out) {
+  clear_error();
+  FG_ARG(re && name && out, "null argument");
+  const double* src = nullptr;
+  if (!strcmp(name, "h")) src = re->H[re->cur];
+  else if (!strcmp(name, "wc")) src = re->W[re->cur];
+  else if (!strcmp(name, "hn")) src = re->H[1 - re->cur];
+  else if (!strcmp(name, "wcn")) src = re->W[1 - re->cur];
+  else if (!strcmp(name, "wch")) src = re->wch;
+  else if (!strcmp(name, "kr")) src = re->kr;
+  FG_ARG(src != nullptr, "unknown interior field '%s'", name);
+  FG_CUDA(cudaMemcpyAsync(out, src, re->n * sizeof(double),
+                          device_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          re->stream));
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  return FREHG_OK;
+}
+
+int frehg_re_get_field(frehg_re* re, const char* name, double* out_halo) {
+  clear_error();
+  FG_ARG(re && name && out_halo, "null argument");
+  const size_t n = re->n;
+  std::vector<double> buf(n);
+  ReArgs a = make_args(re);
+  // after a step, H[cur]/W[cur] are the new state and H[1-cur]/W[1-cur] the step's start
+  a.h_old = re->H[1 - re->cur];
+  a.w_old = re->W[1 - re->cur];
+  const double* src = nullptr;
+  bool ghosts = true;
+  const bool gv = re->ghosts_valid;
+  if (!strcmp(name, "h")) {
+    src = re->H[re->cur];
+    FG_CUDA(cudaMemcpy(buf.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost));
+    to_halo(re, buf, out_halo, gv, re->p.htop, re->p.bc_type[5] == 1, re->p.hbot,
+            re->p.bc_type[4] == 1);
+    return FREHG_OK;
+  }
+  if (!strcmp(name, "wc") || !strcmp(name, "wcn") || !strcmp(name, "hn")) {
+    src = !strcmp(name, "wc") ? re->W[re->cur]
+          : !strcmp(name, "wcn") ? re->W[1 - re->cur] : re->H[1 - re->cur];
+    FG_CUDA(cudaMemcpy(buf.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost));
+    const bool hn = !strcmp(name, "hn");
+    to_halo(re, buf, out_halo, gv, re->p.htop, hn && re->p.bc_type[5] == 1, re->p.hbot,
+            hn && re->p.bc_type[4] == 1);
+    return FREHG_OK;
+  }
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  const int nb = nblocks(n);
+  if (!strcmp(name, "wch") || !strcmp(name, "qx") || !strcmp(name, "qy") ||
+      !strcmp(name, "qz")) {
+    src = !strcmp(name, "wch") ? re->wch : !strcmp(name, "qx") ? re->qx
+          : !strcmp(name, "qy") ? re->qy : re->qz;
+    ghosts = false;
+  } else if (!strcmp(name, "ch")) {
+    k_cap_of_h<<<nb, 256, 0, re->stream>>>(a, re->H[re->cur], re->scratch);
+    src = re->scratch;
+    ghosts = false;
+  } else if (!strcmp(name, "hwc")) {
+    k_h_of_theta<<<nb, 256, 0, re->stream>>>(a, re->W[re->cur], re->scratch);
+    src = re->scratch;
+    ghosts = false;
+  } else if (!strcmp(name, "Kx") || !strcmp(name, "Ky") || !strcmp(name, "Kz")) {
+    const int which = name[1] == 'x' ? 0 : name[1] == 'y' ? 1 : 2;
+    k_faces_export<<<nb, 256, 0, re->stream>>>(a, re->W[1 - re->cur], which, re->scratch);
+    src = re->scratch;
+    ghosts = false;
+  } else if (!strcmp(name, "dz3d") || !strcmp(name, "actv") || !strcmp(name, "bot3d") ||
+             !strcmp(name, "room")) {
+    std::vector<double> wcn;
+    if (!strcmp(name, "room")) {
+      wcn.resize(n);
+      FG_CUDA(cudaMemcpy(wcn.data(), re->W[1 - re->cur], n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    for (size_t c = 0; c < n; ++c) {
+      const int k = (int)(c / re->ncol);
+      if (!strcmp(name, "dz3d")) buf[c] = re->p.dz;
+      else if (!strcmp(name, "actv")) buf[c] = 1.0;
+      else if (!strcmp(name, "bot3d")) buf[c] = -re->p.dz * (double)(k + 1);
+      else buf[c] = (re->p.soil.theta_s - wcn[c]) * re->p.dz * re->p.dx * re->p.dy;
+    }
+    to_halo(re, buf, out_halo, false, 0, false, 0, false);
+    return FREHG_OK;
+  } else {
+    set_error("unknown field '%s'", name);
+    return FREHG_ERR_BAD_ARG;
+  }
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaMemcpyAsync(buf.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, re->stream));
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  to_halo(re, buf, out_halo, ghosts, 0, false, 0, false);
+  if (!strcmp(name, "qz")) {
+    std::vector<double> top(re->ncol);
+    FG_CUDA(cudaMemcpy(top.data(), re->qztop, re->ncol * sizeof(double), cudaMemcpyDeviceToHost));
+    const size_t hx = re->nx + 2;
+    for (int j = 0; j < re->ny; ++j)
+      for (int i = 0; i < re->nx; ++i) out_halo[(size_t)(i + 1) + (size_t)(j + 1) * hx] = top[(size_t)i + (size_t)re->nx * j];
+  }
+  return FREHG_OK;
+}
+
+int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c) {
+  clear_error();
+  FG_ARG(re && c, "null argument");
+  *c = re->cnt;
+  return FREHG_OK;
+}
+
+int frehg_re_water_volume(frehg_re* re, double* vol) {
+  clear_error();
+  FG_ARG(re && vol, "null argument");
+  ReArgs a = make_args(re);
+  double* d_out = re->scratch;
+  k_volume<<<nblocks(re->n), 256, 0, re->stream>>>(a, re->W[re->cur], d_out);
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaMemcpyAsync(vol, d_out, sizeof(double), cudaMemcpyDeviceToHost, re->stream));
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  return FREHG_OK;
+}
+
+int frehg_re_boundary_volumes(frehg_re* re, double* top_in, double* bottom_in) {
+  clear_error();
+  FG_ARG(re && top_in && bottom_in, "null argument");
+  FG_TRY(read_scalars(re));
+  *top_in = re->sc_host->vol_top;
+  *bottom_in = re->sc_host->vol_bot;
+  return FREHG_OK;
+}
+
+int frehg_re_set_stream(frehg_re* re, void* s) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  re->stream = s ? (cudaStream_t)s : re->own_stream;
+  return FREHG_OK;
+}
+
+int frehg_re_sync(frehg_re* re) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  return FREHG_OK;
+}
+
+}  // extern "C"

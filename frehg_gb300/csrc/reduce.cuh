@@ -1,0 +1,115 @@
+// Deterministic block / grid reductions shared by the kernels (last-arriving-block pattern:
+// no grid barrier, no spin-wait).
+#pragma once
+
+#include "internal.h"
+
+namespace fg {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int flat_tid() { return threadIdx.x + threadIdx.y * blockDim.x; }
+__device__ __forceinline__ int flat_nthreads() { return blockDim.x * blockDim.y; }
+__device__ __forceinline__ int flat_bid() { return blockIdx.x + blockIdx.y * gridDim.x; }
+__device__ __forceinline__ int flat_nblocks() { return gridDim.x * gridDim.y; }
+
+// Sum NV values over the block; the result is valid in thread 0.  Uses sh[NV*32].
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
+  const int tid = flat_tid(), lane = tid & 31, wid = tid >> 5, nw = flat_nthreads() >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) v[q] = warp_sum(v[q]);
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sh[q * 32 + wid] = v[q];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double t = lane < nw ? sh[q * 32 + lane] : 0.0;
+      v[q] = warp_sum(t);
+    }
+  }
+  __syncthreads();
+}
+
+// Grid-wide sum through per-block partials; returns true in every thread of the last block
+// to arrive, where tot[] (valid in thread 0) holds the deterministic grid total.
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double* partials, unsigned int* arrive,
+                         double (&tot)[NV]) {
+  __shared__ double sh[NV * 32];
+  __shared__ unsigned int ticket;
+  const int tid = flat_tid(), bid = flat_bid(), nb = flat_nblocks();
+  block_sum<NV>(v, sh);
+  if (tid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) partials[q * kMaxRedBlocks + bid] = v[q];
+    __threadfence();
+    ticket = atomicAdd(arrive, 1u);
+  }
+  __syncthreads();
+  if (ticket != (unsigned)(nb - 1)) return false;
+  __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    acc[q] = 0.0;
+    for (int b = tid; b < nb; b += flat_nthreads()) acc[q] += __ldcg(&partials[q * kMaxRedBlocks + b]);
+  }
+  block_sum<NV>(acc, sh);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) tot[q] = acc[q];
+  if (tid == 0) *arrive = 0u;
+  return true;
+}
+
+// Grid-wide max through per-block partials (NaN-ignoring, as std::max/std::min with a NaN
+// second argument keep the first).  Same last-block contract as grid_sum.
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__device__ __forceinline__ bool grid_max(double v, double* partials, unsigned int* arrive, double* tot) {
+  __shared__ double sh[32];
+  __shared__ unsigned int ticket;
+  const int tid = flat_tid(), lane = tid & 31, wid = tid >> 5, nw = flat_nthreads() >> 5;
+  const int bid = flat_bid(), nb = flat_nblocks();
+  v = warp_max(v);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    double t = lane < nw ? sh[lane] : -INFINITY;
+    t = warp_max(t);
+    if (lane == 0) {
+      partials[bid] = t;
+      __threadfence();
+      ticket = atomicAdd(arrive, 1u);
+    }
+  }
+  __syncthreads();
+  if (ticket != (unsigned)(nb - 1)) return false;
+  __threadfence();
+  double acc = -INFINITY;
+  for (int b = tid; b < nb; b += flat_nthreads()) acc = fmax(acc, __ldcg(&partials[b]));
+  acc = warp_max(acc);
+  __syncthreads();
+  if (lane == 0) sh[wid] = acc;
+  __syncthreads();
+  if (tid == 0) {
+    double t = -INFINITY;
+    for (int q = 0; q < nw; ++q) t = fmax(t, sh[q]);
+    *tot = t;
+    *arrive = 0u;
+  }
+  return true;
+}
+
+}  // namespace fg

@@ -1,0 +1,169 @@
+// van Genuchten / Mualem constitutive relations on the device (FP64).
+//
+// Same relations and formula order as VanGenuchten (src/re/VanGenuchten.hpp:18-137); the
+// conductivity is returned relative to Ks (kr = K/Ks, with the reference's cap K <= Ks and
+// K = Ks above zero head (VG) or above the air-entry head (MVG)), so one evaluation per cell
+// serves the three directional conductivities Ks_x/y/z * kr.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace fg {
+
+// One soil class with the constants the relations reuse precomputed (same values the
+// reference recomputes per call: m = 1 - 1/n, 1/m, 1/n).
+struct SoilClass {
+  double alpha, n, ths, thr, Ksx, Ksy, Ksz, Ss, aev;
+  double m, inv_m, inv_n;
+  int32_t use_vg, use_mvg;
+};
+
+// Soil of one cell after the per-cell overrides (not in reference: continuous Ks / alpha).
+struct CellSoil {
+  double alpha, n, ths, thr, Ss, aev, m, inv_m, inv_n;
+  double Ksx, Ksy, Ksz;
+  int32_t use_vg, use_mvg;
+};
+
+// Where the soil of a cell comes from: class table + optional class-id map (per column or per
+// cell, uint8) + optional per-cell Ks and alpha fields.
+struct SoilView {
+  const SoilClass* cls = nullptr;
+  const uint8_t* cid = nullptr;
+  const double* Ks = nullptr;
+  const double* alpha = nullptr;
+  int cid3d = 0;
+};
+
+__device__ __forceinline__ CellSoil soil_of(const SoilView& v, size_t cell, size_t col) {
+  const int id = v.cid ? (int)v.cid[v.cid3d ? cell : col] : 0;
+  const SoilClass& k = v.cls[id];
+  CellSoil s;
+  s.alpha = v.alpha ? v.alpha[cell] : k.alpha;
+  s.n = k.n;
+  s.ths = k.ths;
+  s.thr = k.thr;
+  s.Ss = k.Ss;
+  s.aev = k.aev;
+  s.m = k.m;
+  s.inv_m = k.inv_m;
+  s.inv_n = k.inv_n;
+  if (v.Ks) {
+    const double K = v.Ks[cell];
+    s.Ksx = K;
+    s.Ksy = K;
+    s.Ksz = K;
+  } else {
+    s.Ksx = k.Ksx;
+    s.Ksy = k.Ksy;
+    s.Ksz = k.Ksz;
+  }
+  s.use_vg = k.use_vg;
+  s.use_mvg = k.use_mvg;
+  return s;
+}
+
+// VanGenuchten::wcm (VanGenuchten.hpp:22-29)
+__device__ __forceinline__ double vg_wcm(const CellSoil& s) {
+  if (s.use_mvg) return s.thr + (s.ths - s.thr) * pow(1.0 + pow(fabs(s.aev) * s.alpha, s.n), s.m);
+  return s.ths;
+}
+
+// waterContentFromHead (VanGenuchten.hpp:31-47)
+__device__ __forceinline__ double vg_theta(const CellSoil& s, double h) {
+  double wc;
+  if (s.use_vg) {
+    const double wcm_val = vg_wcm(s);
+    const double se = pow(1.0 + pow(fabs(s.alpha * h), s.n), -s.m);
+    if (h > s.aev)
+      wc = s.ths;
+    else
+      wc = s.thr + (wcm_val - s.thr) * se;
+  } else {
+    wc = s.thr + (s.ths - s.thr) * exp(0.1634 * h);
+  }
+  if (wc > s.ths) wc = s.ths;
+  if (wc < s.thr) wc = s.thr;
+  return wc;
+}
+
+// headFromWaterContent (VanGenuchten.hpp:50-65)
+__device__ __forceinline__ double vg_head(const CellSoil& s, double wc) {
+  const double eps = 1.0e-7;
+  if (s.use_vg) {
+    const double wcm_val = vg_wcm(s);
+    double theta = wc;
+    if (theta - s.thr < eps) theta = s.thr + eps;
+    if (theta < s.ths)
+      return -(1.0 / s.alpha) * pow(pow((wcm_val - s.thr) / (theta - s.thr), s.inv_m) - 1.0, s.inv_n);
+    return 0.0;
+  }
+  return log((wc - s.thr) / (s.ths - s.thr)) / 0.1634;
+}
+
+// specificMoistureCapacity (VanGenuchten.hpp:68-81)
+__device__ __forceinline__ double vg_capacity(const CellSoil& s, double h) {
+  const double mm = s.m;
+  const double wcm_val = vg_wcm(s);
+  const double ah = fabs(s.alpha * h);
+  const double nume = s.alpha * s.n * mm * (wcm_val - s.thr) * pow(ah, s.n - 1.0);
+  const double deno = pow(1.0 + pow(ah, s.n), mm + 1.0);
+  double c = nume / deno;
+  if (s.use_mvg) {
+    if (h > s.aev) c = 0.0;
+  } else if (h > 0.0) {
+    c = 0.0;
+  }
+  return c;
+}
+
+// conductivityFromHead / Ks (VanGenuchten.hpp:84-111)
+__device__ __forceinline__ double vg_kr(const CellSoil& s, double h) {
+  if (!s.use_vg) return exp(0.1634 * h);
+  const double mm = s.m;
+  const double se = pow(1.0 + pow(fabs(s.alpha * h), s.n), -mm);
+  double kr;
+  if (s.use_mvg) {
+    const double wcm_val = vg_wcm(s);
+    const double nume =
+        1.0 - pow(1.0 - pow(se * (s.ths - s.thr) / (wcm_val - s.thr), s.inv_m), mm);
+    const double deno = 1.0 - pow(1.0 - pow((s.ths - s.thr) / (wcm_val - s.thr), s.inv_m), mm);
+    kr = (deno == 0.0) ? 1.0 : pow(se, 0.5) * pow(nume / deno, 2.0);
+  } else {
+    kr = pow(se, 0.5) * pow(1.0 - pow(1.0 - pow(se, s.inv_m), mm), 2.0);
+  }
+  if (kr > 1.0) kr = 1.0;
+  if (s.use_mvg) {
+    if (h > s.aev) kr = 1.0;
+  } else if (h > 0.0) {
+    kr = 1.0;
+  }
+  return kr;
+}
+
+// dKdwc (VanGenuchten.hpp:114-136)
+__device__ __forceinline__ double vg_dKdwc(const CellSoil& s, double wc, double Ks) {
+  double theta = wc;
+  if (theta > 0.9999 * s.ths && theta < s.ths) theta = 0.9999 * s.ths;
+  const double mm = s.m;
+  const double se = (theta - s.thr) / (s.ths - s.thr);
+  if (s.use_mvg) {
+    const double wcm_val = vg_wcm(s);
+    const double c2 = (s.ths - s.thr) / (wcm_val - s.thr);
+    const double c1 = 1.0 / pow(1.0 - pow(1.0 - pow(c2, s.inv_m), mm), 2.0);
+    const double term0 = pow(1.0 - pow(c2 * se, s.inv_m), mm);
+    const double term1 = 0.5 * c1 * Ks * pow(se, -0.5) * (1.0 - term0) * (1.0 - term0);
+    const double term2 = 2.0 * c1 * Ks * c2 * pow(se, 0.5) * pow(c2 * se, s.inv_m - 1.0) *
+                         (1.0 - term0) * pow(1.0 - pow(c2 * se, s.inv_m), mm - 1.0);
+    return (term1 + term2) / (s.ths - s.thr);
+  }
+  const double term0 = pow(1.0 - pow(se, s.inv_m), mm);
+  const double term1 = 0.5 * Ks * pow(se, -0.5) * (1.0 - term0) * (1.0 - term0);
+  const double term2 = 2.0 * Ks * pow(se, (2.0 - mm) / (2.0 * mm)) * (1.0 - term0) *
+                       pow(1.0 - pow(se, s.inv_m), mm - 1.0);
+  return (term1 + term2) / (s.ths - s.thr);
+}
+
+}  // namespace fg

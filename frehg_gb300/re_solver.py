@@ -1,0 +1,246 @@
+"""Host-side mirror of the reference's ReSolver (src/re/ReSolver.hpp:48-156) over the C ABI.
+
+Method names follow the reference (camelCase aliases included) so callers and tests read like
+the reference's own.  Every call goes to libfrehg_gb300.so; when the library is missing the
+constructor raises -- there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .abi import ReCounters, ReParams, SoilParams, SolverConfig, check, dptr, load_library
+
+
+class Grid:
+    """Grid (src/core/Grid.hpp:153-231): sizes and the halo-padded index."""
+
+    def __init__(self, nx, ny, nz, dx=1.0, dy=1.0, dz=1.0, dz_incre=1.0):
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        self.dx, self.dy, self.dz, self.dz_incre = dx, dy, dz, dz_incre
+
+    def nCell(self):
+        return (self.nx + 2) * (self.ny + 2) * (self.nz + 2)
+
+    def nActiveCell(self):
+        return self.nx * self.ny * self.nz
+
+    def getIndex(self, i, j, k):
+        return (i + 1) + (j + 1) * (self.nx + 2) + (k + 1) * (self.nx + 2) * (self.ny + 2)
+
+
+class SoilMap:
+    """SoilMap (src/soil/SoilMap.hpp:28-92): class table + per-column or per-cell class ids."""
+
+    def __init__(self):
+        self.classes: list[SoilParams] = []
+        self.index = None
+        self.is3d = False
+
+    def setClasses(self, classes):
+        if not classes:
+            raise ValueError("SoilMap::setClasses: empty class table")
+        self.classes = list(classes)
+
+    def setClassIndex(self, nx, ny, idx):
+        idx = np.asarray(idx, dtype=np.int32).ravel()
+        if idx.size != nx * ny:
+            raise ValueError("SoilMap::setClassIndex: size mismatch")
+        self.index, self.is3d = idx, False
+
+    def setClassIndex3D(self, nx, ny, nz, idx):
+        idx = np.asarray(idx, dtype=np.int32).ravel()
+        if idx.size != nx * ny * nz:
+            raise ValueError("SoilMap::setClassIndex3D: size mismatch")
+        self.index, self.is3d = idx, True
+
+
+class Fields:
+    """Lazy view of GwFields (src/re/GwFields.hpp:52-59): fields['h'] is the halo array as a
+    (nz+2, ny+2, nx+2) numpy array copied from the device on access."""
+
+    def __init__(self, solver: "ReSolver"):
+        self._s = solver
+
+    def __getitem__(self, name):
+        return self._s.field(name)
+
+    def __getattr__(self, name):
+        if name.startswith("_"):
+            raise AttributeError(name)
+        return self._s.field(name)
+
+
+class ReSolver:
+    def __init__(self, grid: Grid, params: ReParams | None = None):
+        self._lib = load_library()
+        self.grid = grid
+        self._params = params.copy() if params is not None else ReParams()
+        h = C.c_void_p()
+        check(self._lib.frehg_re_create(grid.nx, grid.ny, grid.nz, C.byref(self._params),
+                                        C.byref(h)), "ReSolver")
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.frehg_re_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- configuration ---------------------------------------------------------------------
+    def set_params(self, p: ReParams):
+        self._params = p.copy()
+        check(self._lib.frehg_re_set_params(self._h, C.byref(self._params)), "setParams")
+
+    def params(self) -> ReParams:
+        p = ReParams()
+        check(self._lib.frehg_re_get_params(self._h, C.byref(p)), "params")
+        return p
+
+    def set_soil_map(self, m: SoilMap):
+        arr = (SoilParams * len(m.classes))(*m.classes)
+        idx = np.ascontiguousarray(m.index, dtype=np.int32)
+        check(self._lib.frehg_re_set_soil_map(self._h, arr, len(m.classes),
+                                              idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                              int(m.is3d)), "setSoilMap")
+
+    def set_cell_fields(self, Ks=None, alpha=None):
+        ks = None if Ks is None else np.ascontiguousarray(Ks, dtype=np.float64).ravel()
+        al = None if alpha is None else np.ascontiguousarray(alpha, dtype=np.float64).ravel()
+        n = self.grid.nActiveCell()
+        for a in (ks, al):
+            if a is not None and a.size != n:
+                raise ValueError("per-cell field must have nx*ny*nz values")
+        check(self._lib.frehg_re_set_cell_fields(self._h, dptr(ks), dptr(al)), "setCellFields")
+
+    def attach_solver(self, cfg):
+        if hasattr(cfg, "config"):
+            cfg = cfg.config
+        check(self._lib.frehg_re_attach_solver(self._h, C.byref(cfg)), "attachSolver")
+
+    # -- initial state ---------------------------------------------------------------------
+    def _interior(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        if a.size != self.grid.nActiveCell():
+            raise ValueError("expected nx*ny*nz values")
+        return a
+
+    def initialize_geometry(self):
+        check(self._lib.frehg_re_initialize_geometry(self._h), "initializeGeometry")
+
+    def set_initial_head(self, h):
+        a = self._interior(h)
+        check(self._lib.frehg_re_set_initial_head(self._h, dptr(a)), "setInitialHead")
+
+    def set_initial_water_content(self, wc):
+        a = self._interior(wc)
+        check(self._lib.frehg_re_set_initial_water_content(self._h, dptr(a)),
+              "setInitialWaterContent")
+
+    def finalize_initial_state(self):
+        check(self._lib.frehg_re_finalize_initial_state(self._h), "finalizeInitialState")
+
+    def initialize_uniform_column(self, wc0):
+        check(self._lib.frehg_re_initialize_uniform_column(self._h, float(wc0)),
+              "initializeUniformColumn")
+
+    def set_top_flux_field(self, q):
+        a = np.ascontiguousarray(q, dtype=np.float64).ravel()
+        if a.size != self.grid.nx * self.grid.ny:
+            raise ValueError(f"ReSolver::setTopFluxField: expected nx*ny={self.grid.nx * self.grid.ny}"
+                             f" values, got {a.size}")
+        check(self._lib.frehg_re_set_top_flux_field(self._h, dptr(a)), "setTopFluxField")
+
+    # -- stepping --------------------------------------------------------------------------
+    def advance_step(self):
+        check(self._lib.frehg_re_advance_step(self._h), "advanceStep")
+
+    def advance_steps(self, n):
+        check(self._lib.frehg_re_advance_steps(self._h, int(n)), "advanceSteps")
+
+    def dt(self):
+        v = C.c_double()
+        check(self._lib.frehg_re_dt(self._h, C.byref(v)), "dt")
+        return v.value
+
+    def dt_used(self):
+        v = C.c_double()
+        check(self._lib.frehg_re_dt_used(self._h, C.byref(v)), "dtUsed")
+        return v.value
+
+    def time(self):
+        v = C.c_double()
+        check(self._lib.frehg_re_time(self._h, C.byref(v)), "time")
+        return v.value
+
+    def set_dt(self, dt):
+        check(self._lib.frehg_re_set_dt(self._h, float(dt)), "setDt")
+
+    def prime_adaptive_dt(self, dt):
+        check(self._lib.frehg_re_prime_adaptive_dt(self._h, float(dt)), "primeAdaptiveDt")
+
+    # -- outputs ---------------------------------------------------------------------------
+    def field(self, name) -> np.ndarray:
+        g = self.grid
+        out = np.empty((g.nz + 2) * (g.ny + 2) * (g.nx + 2), dtype=np.float64)
+        check(self._lib.frehg_re_get_field(self._h, name.encode(), dptr(out)), f"fields.{name}")
+        return out.reshape(g.nz + 2, g.ny + 2, g.nx + 2)
+
+    def fields(self) -> Fields:
+        return Fields(self)
+
+    def interior(self, name, out=None) -> np.ndarray:
+        g = self.grid
+        if out is None:
+            out = np.empty((g.nz, g.ny, g.nx), dtype=np.float64)
+        check(self._lib.frehg_re_get_interior(self._h, name.encode(), dptr(out), 0), name)
+        return out
+
+    def interior_to_device(self, name, dev_ptr: int):
+        check(self._lib.frehg_re_get_interior(self._h, name.encode(),
+                                              C.cast(C.c_void_p(dev_ptr), C.POINTER(C.c_double)),
+                                              1), name)
+
+    def counters(self) -> ReCounters:
+        c = ReCounters()
+        check(self._lib.frehg_re_get_counters(self._h, C.byref(c)), "counters")
+        return c
+
+    def water_volume(self):
+        v = C.c_double()
+        check(self._lib.frehg_re_water_volume(self._h, C.byref(v)), "waterVolume")
+        return v.value
+
+    def boundary_volumes(self):
+        t, b = C.c_double(), C.c_double()
+        check(self._lib.frehg_re_boundary_volumes(self._h, C.byref(t), C.byref(b)),
+              "boundaryVolumes")
+        return t.value, b.value
+
+    def set_stream(self, cuda_stream: int | None):
+        check(self._lib.frehg_re_set_stream(self._h, C.c_void_p(cuda_stream or 0)), "setStream")
+
+    def sync(self):
+        check(self._lib.frehg_re_sync(self._h), "sync")
+
+    # reference spellings
+    setParams = set_params
+    setSoilMap = set_soil_map
+    attachSolver = attach_solver
+    initializeGeometry = initialize_geometry
+    setInitialHead = set_initial_head
+    setInitialWaterContent = set_initial_water_content
+    finalizeInitialState = finalize_initial_state
+    initializeUniformColumn = initialize_uniform_column
+    setTopFluxField = set_top_flux_field
+    advanceStep = advance_step
+    dtUsed = dt_used
+    setDt = set_dt
+    primeAdaptiveDt = prime_adaptive_dt
