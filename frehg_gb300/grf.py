@@ -36,7 +36,7 @@ def exponential_grf(shape, corr, seed: int) -> np.ndarray:
     spec = np.fft.rfftn(noise)
     del noise
     spec *= amp
-    field = np.fft.irfftn(spec, s=shape)
+    field = np.fft.irfftn(spec, s=shape, axes=(0, 1, 2))
     field -= field.mean()
     field /= field.std()
     return np.ascontiguousarray(field)
