@@ -162,6 +162,16 @@ class ReCounters(C.Structure):
         ("last_ksp_iterations", C.c_int32),
         ("last_picard_iterations", C.c_int32),
         ("last_residual_norm", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [
+        ("name", C.c_char * 32),
+        ("launches", C.c_int64),
+        ("total_ms", C.c_double),
+        ("bytes_per_launch", C.c_double),
     ]
 
 
@@ -204,6 +214,8 @@ SIGNATURES = {
     "frehg_re_get_counters": (C.c_int, [_VP, C.POINTER(ReCounters)]),
     "frehg_re_water_volume": (C.c_int, [_VP, _PD]),
     "frehg_re_boundary_volumes": (C.c_int, [_VP, _PD, _PD]),
+    "frehg_re_set_profiling": (C.c_int, [_VP, C.c_int]),
+    "frehg_re_kernel_stats": (C.c_int, [_VP, C.POINTER(KernelStat), C.c_int, _PI]),
     "frehg_re_set_stream": (C.c_int, [_VP, _VP]),
     "frehg_re_sync": (C.c_int, [_VP]),
     "frehg_cg_create": (C.c_int, [C.POINTER(SolverConfig), C.POINTER(_VP)]),

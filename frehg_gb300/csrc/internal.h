@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "../../include/frehg_gb300.h"
 
@@ -37,6 +38,46 @@ void clear_error();
       ::fg::set_error(__VA_ARGS__);        \
       return FREHG_ERR_BAD_ARG;            \
     }                                      \
+  } while (0)
+
+// ------------------------------------------------------------------------------------------
+// Launch accounting and optional per-kernel event timing.
+class Profiler {
+ public:
+  bool on = false;
+  int64_t launches = 0;
+  ~Profiler();
+  void reset();
+  // bracket one launch: begin() before, end() after (no-ops while off)
+  int begin(cudaStream_t st);
+  void end(int slot, cudaStream_t st, const char* name, double bytes);
+  // after the stream has been synchronised: fold finished event pairs into the table
+  int flush();
+  struct Stat {
+    std::string name;
+    int64_t launches = 0;
+    double ms = 0.0;
+    double bytes = 0.0;
+  };
+  std::vector<Stat> stats;
+
+ private:
+  struct Pending {
+    cudaEvent_t a, b;
+    std::string name;
+    double bytes;
+  };
+  std::vector<Pending> pending_;
+  std::vector<cudaEvent_t> pool_;
+  cudaEvent_t get_event();
+};
+
+// Launch bracket: counts the launch and, while profiling, times it with CUDA events.
+#define FG_LAUNCH(prof, st, name, bytes, ...)           \
+  do {                                                  \
+    const int slot_ = (prof) ? (prof)->begin(st) : -1; \
+    __VA_ARGS__;                                        \
+    if (prof) (prof)->end(slot_, st, name, bytes);      \
   } while (0)
 
 // Upper bound of the blocks any reduction kernel launches (partials buffers are sized to it).
@@ -125,6 +166,8 @@ class KrylovSolver {
   cudaGraphExec_t g64 = nullptr;
   cudaGraphExec_t g32 = nullptr;
   const void* g64_key = nullptr;
+  const void* g64_key2 = nullptr;
+  Profiler* prof = nullptr;  // owner's profiler (launch counts, optional event timing)
   const void* g32_key = nullptr;
   cudaStream_t g_stream = nullptr;
   size_t g_n = 0;
@@ -135,6 +178,7 @@ class KrylovSolver {
   int solve_mixed(Stencil64& A, double* x_out, const frehg_solver_config& cfg, cudaStream_t st,
                   CgResult* res);
   int run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk);
+  int finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResult* res, int nb);
 };
 
 // Launch helpers shared by the stencil kernels: a (32 x 8) thread tile over axes 0/1 marching

@@ -348,10 +348,13 @@ int KrylovSolver::ensure(size_t n) {
 int KrylovSolver::scale(Stencil64& A, cudaStream_t st) {
   if (A.scaled) return FREHG_OK;
   const int nb = reduction_blocks(A.n, 256, 4);
-  k_diag_rsqrt<<<nb, 256, 0, st>>>(A.s, A.n);
+  const double n = (double)A.n;
+  FG_LAUNCH(prof, st, "k_diag_rsqrt", 16.0 * n, k_diag_rsqrt<<<nb, 256, 0, st>>>(A.s, A.n));
   FG_CUDA(cudaGetLastError());
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
-  k_scale_offdiag<<<L.grid, L.block, 0, st>>>(A.a0, A.a1, A.a2, A.s, A.n0, A.n1, A.n2, L.planes);
+  FG_LAUNCH(prof, st, "k_scale_offdiag", 56.0 * n,
+            k_scale_offdiag<<<L.grid, L.block, 0, st>>>(A.a0, A.a1, A.a2, A.s, A.n0, A.n1, A.n2,
+                                                        L.planes));
   FG_CUDA(cudaGetLastError());
   A.scaled = true;
   return FREHG_OK;
@@ -362,6 +365,7 @@ int KrylovSolver::run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int
   const int max_launch = max_it / chunk + 2;
   for (int q = 0; q < max_launch; ++q) {
     FG_CUDA(cudaGraphLaunch(g, st));
+    if (prof) prof->launches += 3 * chunk;
     FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (hst->status != 0) return FREHG_OK;
@@ -396,12 +400,35 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
   init.max_it = cfg.max_it;
   FG_CUDA(cudaMemcpyAsync(dst, &init, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
   const int nb = reduction_blocks(n, 256, 4);
-  k_cg_init<<<nb, 256, 0, st>>>(A.s, A.b, x, r, n, dst, partials);
+  const double dn = (double)n;
+  FG_LAUNCH(prof, st, "k_cg_init", 32.0 * dn,
+            k_cg_init<<<nb, 256, 0, st>>>(A.s, A.b, x, r, n, dst, partials));
   FG_CUDA(cudaGetLastError());
 
   const int chunk = chunk_for(n);
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
-  const bool rebuild = !g64 || g64_key != (const void*)&A || g_stream != st || g_n != n;
+  if (prof && prof->on) {
+    // profiled path: the same kernels launched one by one between CUDA events
+    FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    for (int q = 0; q < cfg.max_it / chunk + 2 && hst->status == 0; ++q) {
+      for (int it = 0; it < chunk; ++it) {
+        FG_LAUNCH(prof, st, "k_cg_p", 24.0 * dn, k_cg_p<<<nb, 256, 0, st>>>(r, p, n, dst));
+        FG_LAUNCH(prof, st, "k_cg_spmv", 40.0 * dn,
+                  k_cg_spmv<<<L.grid, L.block, 0, st>>>(A.a0, A.a1, A.a2, p, w, A.n0, A.n1, A.n2,
+                                                        L.planes, dst, partials));
+        FG_LAUNCH(prof, st, "k_cg_update", 56.0 * dn,
+                  k_cg_update<<<nb, 256, 0, st>>>(x, r, p, w, A.s, n, dst, partials));
+      }
+      FG_CUDA(cudaGetLastError());
+      FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaStreamSynchronize(st));
+      FG_TRY(prof->flush());
+    }
+    return finish64(A, x_out, st, res, nb);
+  }
+  const bool rebuild = !g64 || g64_key != (const void*)A.a0 || g64_key2 != (const void*)A.s ||
+                       g_stream != st || g_n != n;
   if (rebuild) {
     if (g64) cudaGraphExecDestroy(g64);
     g64 = nullptr;
@@ -427,7 +454,8 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
       set_error("graph instantiate failed: %s", cudaGetErrorString(e));
       return FREHG_ERR_CUDA;
     }
-    g64_key = &A;
+    g64_key = A.a0;
+    g64_key2 = A.s;
     g_stream = st;
     g_n = n;
   }
@@ -435,7 +463,12 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
   FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
   FG_CUDA(cudaStreamSynchronize(st));
   if (hst->status == 0) FG_TRY(run_chunks(g64, st, cfg.max_it, chunk));
-  k_unscale<<<nb, 256, 0, st>>>(A.s, x, x_out, n);
+  return finish64(A, x_out, st, res, nb);
+}
+
+int KrylovSolver::finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResult* res, int nb) {
+  FG_LAUNCH(prof, st, "k_unscale", 24.0 * (double)A.n,
+            k_unscale<<<nb, 256, 0, st>>>(A.s, x, x_out, A.n));
   FG_CUDA(cudaGetLastError());
   res->its = hst->its;
   res->reason = hst->status;

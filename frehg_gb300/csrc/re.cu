@@ -50,8 +50,9 @@ struct frehg_re {
   // operator + Krylov
   Stencil64 A;
   KrylovSolver ksp;
-  // counters
+  // counters / profiling
   frehg_re_counters cnt;
+  Profiler prof;
   ~frehg_re();
 };
 
@@ -263,6 +264,11 @@ __global__ void k_volume(ReArgs a, const double* __restrict__ w, double* out) {
 
 static int nblocks(size_t n) { return reduction_blocks(n, 256, 4); }
 
+// bytes one cell's soil lookup reads (per-cell Ks / alpha fields, class ids)
+static double soil_bytes(const frehg_re* re) {
+  return (re->fKs ? 8.0 : 0.0) + (re->falpha ? 8.0 : 0.0) + (re->cid && re->cid3d ? 1.0 : 0.0);
+}
+
 // ------------------------------------------------------------------------------------------
 // PCA step (ReSolver::advanceStep, ReSolver.cpp:931-969)
 
@@ -270,13 +276,17 @@ static int pca_step(frehg_re* re) {
   cudaStream_t st = re->stream;
   ReArgs a = make_args(re);
   const int nb = nblocks(re->n);
-  k_step_begin<<<1, 1, 0, st>>>(re->sc);
+  Profiler* prof = &re->prof;
+  const double n = (double)re->n, sb = soil_bytes(re);
+  FG_LAUNCH(prof, st, "k_step_begin", 0.0, k_step_begin<<<1, 1, 0, st>>>(re->sc));
   // computeKFace inputs at h^n
-  k_kr<<<nb, 256, 0, st>>>(a, a.h_old, re->kr);
+  FG_LAUNCH(prof, st, "k_kr", (16.0 + sb) * n, k_kr<<<nb, 256, 0, st>>>(a, a.h_old, re->kr));
   // groundwaterMatCoeff + groundwaterRhs + assembly
   const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
   re->A.scaled = false;
-  k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b);
+  FG_LAUNCH(prof, st, "k_assemble", (64.0 + sb) * n,
+            k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
+                                                   re->A.b));
   FG_CUDA(cudaGetLastError());
   // LinearSolver::solve
   CgResult res;
@@ -286,10 +296,11 @@ static int pca_step(frehg_re* re) {
   re->cnt.ksp_iterations += res.its;
   if (rc != FREHG_OK) return rc;
   // enforceHeadBc + computeKFace + updateDiagnostics at h^{n+1} (the solve wrote h^{n+1})
-  k_post<<<nb, 256, 0, st>>>(a);
+  FG_LAUNCH(prof, st, "k_post", (24.0 + sb) * n, k_post<<<nb, 256, 0, st>>>(a));
   FG_CUDA(cudaGetLastError());
   // groundwaterFlux + updateWaterContent (+ dq of adaptiveTimeStep, boundary budgets)
-  k_correct<<<L.grid, L.block, 0, st>>>(a);
+  FG_LAUNCH(prof, st, "k_correct", (73.0 + sb) * n,
+            k_correct<<<L.grid, L.block, 0, st>>>(a));
   FG_CUDA(cudaGetLastError());
   // reallocateWaterContent: relax to the sequential sweep's fixed point
   const int top_sat = (re->p.bc_type[5] == 1 && re->p.htop >= 0.0) ? 1 : 0;
@@ -298,13 +309,15 @@ static int pca_step(frehg_re* re) {
   int sweeps = 0;
   for (;;) {
     FG_CUDA(cudaMemsetAsync(&re->sc->changed, 0, sizeof(int), st));
-    k_realloc_sweep<<<cb, 128, 0, st>>>(a, top_sat);
+    FG_LAUNCH(prof, st, "k_realloc_sweep", 2.0 * n,
+              k_realloc_sweep<<<cb, 128, 0, st>>>(a, top_sat));
     FG_CUDA(cudaGetLastError());
     ++sweeps;
     int changed = 0;
     FG_CUDA(cudaMemcpyAsync(&re->sc_host->changed, &re->sc->changed, sizeof(int),
                             cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
+    if (prof->on) FG_TRY(prof->flush());
     changed = re->sc_host->changed;
     if (!changed) break;
     if (sweeps > max_sweeps) {
@@ -314,8 +327,13 @@ static int pca_step(frehg_re* re) {
   }
   re->cnt.realloc_sweeps += sweeps;
   // apply reallocation, clampWaterContent, adaptiveTimeStep
-  k_finalize<<<nb, 256, 0, st>>>(a, top_sat);
+  FG_LAUNCH(prof, st, "k_finalize", (25.0 + sb) * n,
+            k_finalize<<<nb, 256, 0, st>>>(a, top_sat));
   FG_CUDA(cudaGetLastError());
+  if (prof->on) {
+    FG_CUDA(cudaStreamSynchronize(st));
+    FG_TRY(prof->flush());
+  }
   re->cur = 1 - re->cur;
   re->ghosts_valid = true;
   return FREHG_OK;
@@ -414,6 +432,7 @@ int frehg_re_create(int nx, int ny, int nz, const frehg_re_params* p, frehg_re**
   cudaMemset(re->qztop, 0, re->ncol * sizeof(double));
   if (upload_class0(re) != FREHG_OK) return fail(FREHG_ERR_CUDA);
   if (re->ksp.ensure(n) != FREHG_OK) return fail(FREHG_ERR_CUDA);
+  re->ksp.prof = &re->prof;
   *out = re;
   return FREHG_OK;
 }
@@ -773,6 +792,35 @@ int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c) {
   clear_error();
   FG_ARG(re && c, "null argument");
   *c = re->cnt;
+  c->kernel_launches = re->prof.launches;
+  return FREHG_OK;
+}
+
+int frehg_re_set_profiling(frehg_re* re, int on) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  if (re->prof.on) FG_TRY(re->prof.flush());
+  if (on) re->prof.reset();
+  re->prof.on = on != 0;
+  return FREHG_OK;
+}
+
+int frehg_re_kernel_stats(frehg_re* re, frehg_kernel_stat* out, int max, int* count) {
+  clear_error();
+  FG_ARG(re && count && (max == 0 || out), "null argument");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_TRY(re->prof.flush());
+  const int n = (int)re->prof.stats.size();
+  *count = n;
+  for (int q = 0; q < n && q < max; ++q) {
+    const Profiler::Stat& s = re->prof.stats[q];
+    memset(&out[q], 0, sizeof(out[q]));
+    strncpy(out[q].name, s.name.c_str(), sizeof(out[q].name) - 1);
+    out[q].launches = s.launches;
+    out[q].total_ms = s.ms;
+    out[q].bytes_per_launch = s.bytes;
+  }
   return FREHG_OK;
 }
 

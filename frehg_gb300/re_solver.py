@@ -10,7 +10,8 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import ReCounters, ReParams, SoilParams, SolverConfig, check, dptr, load_library
+from .abi import (KernelStat, ReCounters, ReParams, SoilParams, SolverConfig, check, dptr,
+                  load_library)
 
 
 class Grid:
@@ -223,6 +224,17 @@ class ReSolver:
         check(self._lib.frehg_re_boundary_volumes(self._h, C.byref(t), C.byref(b)),
               "boundaryVolumes")
         return t.value, b.value
+
+    def set_profiling(self, on: bool):
+        check(self._lib.frehg_re_set_profiling(self._h, int(bool(on))), "setProfiling")
+
+    def kernel_stats(self) -> list[dict]:
+        n = C.c_int()
+        check(self._lib.frehg_re_kernel_stats(self._h, None, 0, C.byref(n)), "kernelStats")
+        arr = (KernelStat * max(n.value, 1))()
+        check(self._lib.frehg_re_kernel_stats(self._h, arr, n.value, C.byref(n)), "kernelStats")
+        return [dict(name=a.name.decode(), launches=a.launches, total_ms=a.total_ms,
+                     bytes_per_launch=a.bytes_per_launch) for a in arr[:n.value]]
 
     def set_stream(self, cuda_stream: int | None):
         check(self._lib.frehg_re_set_stream(self._h, C.c_void_p(cuda_stream or 0)), "setStream")

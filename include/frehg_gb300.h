@@ -186,6 +186,7 @@ typedef struct frehg_re_counters {
   int32_t last_ksp_iterations;
   int32_t last_picard_iterations;
   double last_residual_norm;
+  int64_t kernel_launches;   /* kernels this handle launched (graph nodes included)      */
 } frehg_re_counters;
 int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c);
 
@@ -193,6 +194,19 @@ int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c);
  * cumulative top / bottom boundary inflow volumes (not in reference). */
 int frehg_re_water_volume(frehg_re* re, double* vol);
 int frehg_re_boundary_volumes(frehg_re* re, double* top_in, double* bottom_in);
+
+/* Per-kernel timing (not in reference; benchmarking aid).  While profiling is on, every kernel
+ * the handle launches is bracketed by CUDA events on the handle's stream (the Krylov loop then
+ * runs without its CUDA graph), and duration, launch count and the algorithmic bytes of one
+ * launch are accumulated per kernel name.  Turning profiling on clears the table. */
+typedef struct frehg_kernel_stat {
+  char name[32];
+  int64_t launches;
+  double total_ms;
+  double bytes_per_launch;
+} frehg_kernel_stat;
+int frehg_re_set_profiling(frehg_re* re, int on);
+int frehg_re_kernel_stats(frehg_re* re, frehg_kernel_stat* out, int max, int* count);
 
 /* Stream control: all work of the handle is issued on this stream (cudaStream_t passed as
  * void*; NULL = the handle's own stream).  frehg_re_sync waits for it. */
