@@ -41,16 +41,20 @@ def parse():
     ap.add_argument("--scheme", default="pca", choices=["pca", "picard"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--ref-window", type=int, default=64,
+    ap.add_argument("--ref-window", type=int, default=128,
                     help="columns per side of the CPU sample window")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=2)
+    ap.add_argument("--nx", type=int, default=None, help="window of the workload (smaller case)")
+    ap.add_argument("--ny", type=int, default=None)
     return ap.parse_args()
 
 
 def workload(args, nx=None, ny=None):
     from frehg_gb300 import workloads as W
     prec = 1 if args.precision == "mixed" else 0
+    if nx is None and args.nx:
+        nx, ny = args.nx, args.ny or args.nx
     if args.config == "c0":
         kw = {} if nx is None else dict(nx=nx, ny=ny)
         w = W.config0(args.scheme, **kw)
@@ -303,7 +307,8 @@ def run_gpu(args):
     s.set_profiling(1)
     for _ in range(args.profile_steps):
         s.advance_step()
-    stats = s.kernel_stats()
+    stats = s.kernel_stats() if args.profile_steps > 0 else [
+        {"name": "none", "launches": 1, "total_ms": 1.0, "bytes_per_launch": 0.0}]
     s.set_profiling(0)
     tot = sum(st["total_ms"] for st in stats) or 1.0
     dom = max(stats, key=lambda st: st["total_ms"])
