@@ -35,7 +35,7 @@ extern "C" {
 
 /* ------------------------------------------------------------------------------------------ */
 /* Status codes.  The reference throws std::runtime_error (PetscLinearSolver.cpp:21-25,206-211); */
-/* the C++ wrappers in include/frehg2_gpu.hpp turn any non-zero code into that exception.      */
+/* a C++ caller rethrows any non-zero code as that exception.                                  */
 /* ------------------------------------------------------------------------------------------ */
 enum {
   FREHG_OK = 0,
