@@ -186,6 +186,7 @@ class KrylovSolver {
 struct StencilLaunch {
   dim3 grid, block;
   int planes;  // axis-2 planes per block
+  int tiles;   // 32 x 8 tiles over axes 0/1 (blocks stride over them)
 };
 StencilLaunch stencil_launch(int n0, int n1, int n2);
 

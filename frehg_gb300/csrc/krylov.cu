@@ -49,8 +49,13 @@ StencilLaunch stencil_launch(int n0, int n1, int n2) {
   if (z > n2) z = n2;
   int planes = (int)((n2 + z - 1) / z);
   z = (n2 + planes - 1) / planes;
+  // blocks stride over tiles when there are more tiles than reduction partial slots
+  long gx = tiles;
+  const long cap = kMaxRedBlocks / z;
+  if (gx > cap) gx = cap;
   L.planes = planes;
-  L.grid = dim3((unsigned)tiles, (unsigned)z, 1);
+  L.tiles = (int)tiles;
+  L.grid = dim3((unsigned)gx, (unsigned)z, 1);
   return L;
 }
 
@@ -75,20 +80,22 @@ __global__ void k_diag_rsqrt(double* __restrict__ s, size_t n) {
 
 __global__ void k_scale_offdiag(double* __restrict__ a0, double* __restrict__ a1,
                                 double* __restrict__ a2, const double* __restrict__ s, int n0,
-                                int n1, int n2, int planes) {
+                                int n1, int n2, int planes, int tiles) {
   const int t0 = (n0 + 31) / 32;
-  const int i0 = (blockIdx.x % t0) * 32 + threadIdx.x;
-  const int i1 = (blockIdx.x / t0) * 8 + threadIdx.y;
-  if (i0 >= n0 || i1 >= n1) return;
-  const size_t s01 = (size_t)n0 * n1;
-  const int kb = blockIdx.y * planes;
-  const int ke = min(n2, kb + planes);
-  for (int k = kb; k < ke; ++k) {
-    const size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * k;
-    const double sc = s[c];
-    if (i0 + 1 < n0) a0[c] *= sc * s[c + 1]; else a0[c] = 0.0;
-    if (i1 + 1 < n1) a1[c] *= sc * s[c + n0]; else a1[c] = 0.0;
-    if (k + 1 < n2) a2[c] *= sc * s[c + s01]; else a2[c] = 0.0;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i0 = (tile % t0) * 32 + threadIdx.x;
+    const int i1 = (tile / t0) * 8 + threadIdx.y;
+    if (i0 >= n0 || i1 >= n1) continue;
+    const size_t s01 = (size_t)n0 * n1;
+    const int kb = blockIdx.y * planes;
+    const int ke = min(n2, kb + planes);
+    for (int k = kb; k < ke; ++k) {
+      const size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * k;
+      const double sc = s[c];
+      if (i0 + 1 < n0) a0[c] *= sc * s[c + 1]; else a0[c] = 0.0;
+      if (i1 + 1 < n1) a1[c] *= sc * s[c + n0]; else a1[c] = 0.0;
+      if (k + 1 < n2) a2[c] *= sc * s[c + s01]; else a2[c] = 0.0;
+    }
   }
 }
 
@@ -159,13 +166,15 @@ __global__ void __launch_bounds__(256) k_cg_spmv(const double* __restrict__ a0,
                                                  const double* __restrict__ a2,
                                                  const double* __restrict__ p,
                                                  double* __restrict__ w, int n0, int n1, int n2,
-                                                 int planes, CgDevState* st, double* partials) {
+                                                 int planes, int tiles, CgDevState* st,
+                                                 double* partials) {
   if (st->status) return;
   const int t0 = (n0 + 31) / 32;
-  const int i0 = (blockIdx.x % t0) * 32 + threadIdx.x;
-  const int i1 = (blockIdx.x / t0) * 8 + threadIdx.y;
   double acc[1] = {0.0};
-  if (i0 < n0 && i1 < n1) {
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i0 = (tile % t0) * 32 + threadIdx.x;
+    const int i1 = (tile / t0) * 8 + threadIdx.y;
+    if (i0 >= n0 || i1 >= n1) continue;
     const size_t s01 = (size_t)n0 * n1;
     const int kb = blockIdx.y * planes;
     const int ke = min(n2, kb + planes);
@@ -354,7 +363,7 @@ int KrylovSolver::scale(Stencil64& A, cudaStream_t st) {
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
   FG_LAUNCH(prof, st, "k_scale_offdiag", 56.0 * n,
             k_scale_offdiag<<<L.grid, L.block, 0, st>>>(A.a0, A.a1, A.a2, A.s, A.n0, A.n1, A.n2,
-                                                        L.planes));
+                                                        L.planes, L.tiles));
   FG_CUDA(cudaGetLastError());
   A.scaled = true;
   return FREHG_OK;
@@ -416,7 +425,7 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
         FG_LAUNCH(prof, st, "k_cg_p", 24.0 * dn, k_cg_p<<<nb, 256, 0, st>>>(r, p, n, dst));
         FG_LAUNCH(prof, st, "k_cg_spmv", 40.0 * dn,
                   k_cg_spmv<<<L.grid, L.block, 0, st>>>(A.a0, A.a1, A.a2, p, w, A.n0, A.n1, A.n2,
-                                                        L.planes, dst, partials));
+                                                        L.planes, L.tiles, dst, partials));
         FG_LAUNCH(prof, st, "k_cg_update", 56.0 * dn,
                   k_cg_update<<<nb, 256, 0, st>>>(x, r, p, w, A.s, n, dst, partials));
       }
@@ -439,7 +448,7 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
     for (int q = 0; q < chunk; ++q) {
       k_cg_p<<<nb, 256, 0, cap_st>>>(r, p, n, dst);
       k_cg_spmv<<<L.grid, L.block, 0, cap_st>>>(A.a0, A.a1, A.a2, p, w, A.n0, A.n1, A.n2,
-                                                L.planes, dst, partials);
+                                                L.planes, L.tiles, dst, partials);
       k_cg_update<<<nb, 256, 0, cap_st>>>(x, r, p, w, A.s, n, dst, partials);
     }
     cudaError_t e = cudaStreamEndCapture(cap_st, &graph);

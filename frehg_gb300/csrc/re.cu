@@ -286,7 +286,7 @@ static int pca_step(frehg_re* re) {
   re->A.scaled = false;
   FG_LAUNCH(prof, st, "k_assemble", (64.0 + sb) * n,
             k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
-                                                   re->A.b));
+                                                   re->A.b, L.planes, L.tiles));
   FG_CUDA(cudaGetLastError());
   // LinearSolver::solve
   CgResult res;
@@ -300,7 +300,7 @@ static int pca_step(frehg_re* re) {
   FG_CUDA(cudaGetLastError());
   // groundwaterFlux + updateWaterContent (+ dq of adaptiveTimeStep, boundary budgets)
   FG_LAUNCH(prof, st, "k_correct", (73.0 + sb) * n,
-            k_correct<<<L.grid, L.block, 0, st>>>(a));
+            k_correct<<<L.grid, L.block, 0, st>>>(a, L.planes, L.tiles));
   FG_CUDA(cudaGetLastError());
   // reallocateWaterContent: relax to the sequential sweep's fixed point
   const int top_sat = (re->p.bc_type[5] == 1 && re->p.htop >= 0.0) ? 1 : 0;

@@ -150,12 +150,13 @@ __global__ void k_kr(ReArgs a, const double* __restrict__ h, double* __restrict_
 __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__ dg,
                                                   double* __restrict__ a0, double* __restrict__ a1,
                                                   double* __restrict__ a2,
-                                                  double* __restrict__ bvec) {
+                                                  double* __restrict__ bvec, int planes,
+                                                  int tiles) {
   const int t0 = (a.nx + 31) / 32;
-  const int i = (blockIdx.x % t0) * 32 + threadIdx.x;
-  const int j = (blockIdx.x / t0) * 8 + threadIdx.y;
-  if (i >= a.nx || j >= a.ny) return;
-  const int planes = (a.nz + gridDim.y - 1) / gridDim.y;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+  const int i = (tile % t0) * 32 + threadIdx.x;
+  const int j = (tile / t0) * 8 + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) continue;
   const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
   const size_t col = (size_t)i + (size_t)a.nx * j;
   const double dx = a.dx, dy = a.dy, dzk = a.dz;
@@ -267,6 +268,7 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
     a2[c] = (k + 1 < a.nz) ? Gzp : 0.0;
     bvec[c] = g;
   }
+  }
 }
 
 // kr(h^{n+1}) and theta(h^{n+1}) once the solve has written h^{n+1} (re_solve_unpack).
@@ -290,16 +292,16 @@ __device__ __forceinline__ double flux_z_inner(const ReArgs& a, double Kc, doubl
 }
 
 // groundwaterFlux + updateWaterContent + adaptiveTimeStep's dq (ReSolver.cpp:671-786, 891-905)
-__global__ void __launch_bounds__(256) k_correct(ReArgs a) {
+__global__ void __launch_bounds__(256) k_correct(ReArgs a, int planes, int tiles) {
   const double dtg = a.sc->dt_used;
   const double dtq = a.sc->dtn;  // adaptiveTimeStep resets params_.dt = dtn_ before dq
   const int t0 = (a.nx + 31) / 32;
-  const int i = (blockIdx.x % t0) * 32 + threadIdx.x;
-  const int j = (blockIdx.x / t0) * 8 + threadIdx.y;
   double dqmax = 0.0;
   double vol[2] = {0.0, 0.0};
-  if (i < a.nx && j < a.ny) {
-    const int planes = (a.nz + gridDim.y - 1) / gridDim.y;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i = (tile % t0) * 32 + threadIdx.x;
+    const int j = (tile / t0) * 8 + threadIdx.y;
+    if (i >= a.nx || j >= a.ny) continue;
     const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
     const size_t col = (size_t)i + (size_t)a.nx * j;
     const double dx = a.dx, dy = a.dy, dzk = a.dz;
