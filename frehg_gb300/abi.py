@@ -234,6 +234,8 @@ SIGNATURES = {
     "frehg_cg_iteration_count": (C.c_int, [_VP, _PI]),
     "frehg_cg_residual_norm": (C.c_int, [_VP, _PD]),
     "frehg_cg_converged_reason": (C.c_int, [_VP, _PI]),
+    "frehg_cg_solve_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _VP,
+                                         _VP, C.POINTER(SolverConfig), _VP, _PI, _PD]),
     "frehg_build_arch": (C.c_int, []),
 }
 

@@ -254,6 +254,25 @@ int frehg_cg_iteration_count(const frehg_cg* cg, int* its);   /* getIterationCou
 int frehg_cg_residual_norm(const frehg_cg* cg, double* rnorm); /* getResidualNorm   */
 int frehg_cg_converged_reason(const frehg_cg* cg, int* reason); /* KSPConvergedReason */
 
+/* Allocation-free CG solve.  No counterpart in the reference: it exists for callers that may
+ * not allocate GPU memory themselves (a component under a host framework that owns the device
+ * memory budget, or a time-critical loop that cannot take cudaMalloc's synchronisation).  The
+ * caller passes device arrays only: the operator in owned order (diag; a_k, a_i, a_j = coupling
+ * of each row with its k+1, i+1, j+1 neighbour, 0 where that neighbour is absent), b and x.
+ * The solver's work space is one fixed device array inside the library, so:
+ *   - at most 262,144 unknowns (nx*ny*nz); larger systems get FREHG_ERR_BAD_ARG;
+ *   - every GPU that loads the library keeps that array (about 16 MB) until the process ends;
+ *   - the first call on a device looks up the array's address with that device current --
+ *     make it before any stream capture on the device;
+ *   - all calls share the array: calls that overlap on the GPU race; serialise them;
+ *   - no cudaMalloc, cudaFree or other allocating routine is called.
+ * stream: cudaStream_t as void* (NULL = the legacy default stream).  Same stopping rule,
+ * iteration count and residual norm as frehg_cg_solve (Jacobi-PCG, PETSc semantics). */
+int frehg_cg_solve_noalloc(int nx, int ny, int nz, const double* diag, const double* a_k,
+                           const double* a_i, const double* a_j, const double* b, double* x,
+                           const frehg_solver_config* cfg, void* stream, int* its,
+                           double* rnorm);
+
 /* Build information: returns the sm architecture the library was compiled for (e.g. 103). */
 int frehg_build_arch(void);
 
