@@ -163,6 +163,8 @@ class ReCounters(C.Structure):
         ("last_picard_iterations", C.c_int32),
         ("last_residual_norm", C.c_double),
         ("kernel_launches", C.c_int64),
+        ("ir_sweeps", C.c_int64),
+        ("elastic_volume", C.c_double),
     ]
 
 

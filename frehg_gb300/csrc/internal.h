@@ -159,9 +159,15 @@ class KrylovSolver {
   CgDevState* dst = nullptr;
   CgDevState* hst = nullptr;  // pinned mirror
   // mixed precision buffers
+  int ensure32(size_t n);
+  size_t cap32 = 0;
   float *xf = nullptr, *rf = nullptr, *pf = nullptr, *wf = nullptr;
   double* rres = nullptr;  // fp64 true residual
   Stencil32 op32;
+  CgDevState* dst32 = nullptr;  // inner FP32 solve state
+  CgDevState* hst32 = nullptr;
+  cudaStream_t g_stream32 = nullptr;
+  size_t g_n32 = 0;
   // graphs
   cudaGraphExec_t g64 = nullptr;
   cudaGraphExec_t g32 = nullptr;

@@ -326,6 +326,8 @@ KrylovSolver::~KrylovSolver() {
   cudaFree(pf);
   cudaFree(wf);
   cudaFree(rres);
+  cudaFree(dst32);
+  cudaFreeHost(hst32);
   op32.release();
 }
 
@@ -490,17 +492,6 @@ int KrylovSolver::finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResul
     return hst->status == kDivergedNanOrInf ? FREHG_ERR_NONFINITE : FREHG_ERR_NOT_CONVERGED;
   }
   return FREHG_OK;
-}
-
-int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_config& cfg,
-                              cudaStream_t st, CgResult* res) {
-  (void)A;
-  (void)x_out;
-  (void)cfg;
-  (void)st;
-  (void)res;
-  set_error("mixed-precision Krylov path is not built in this version");
-  return FREHG_ERR_UNSUPPORTED;
 }
 
 }  // namespace fg

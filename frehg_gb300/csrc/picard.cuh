@@ -1,8 +1,185 @@
-// Mixed-form modified Picard step on the device (not in reference).
+// Mixed-form modified Picard step on the device (not in reference: the reference only has the
+// PCA scheme).  The same scheme as the oracle's FP64 statement (Celia, Bouloutas & Zarba 1990):
+//   per iterate h^m, with K and C frozen at h^m,
+//   [V(C + Ss th^n/ths) + dt sum T] d_c - dt sum_nb T d_nb = -Rdt_c,
+//   Rdt_c = V(th(h^m) - th^n) + V Ss (th^n/ths)(h^m - h^n) - dt Q_c(h^m)   (FP64 residual),
+//   h^{m+1} = h^m + d until |d|_inf < picard_tol;
+// then the conservative update th^{n+1} = th^n + [dt Q_c(h^{n+1}) - V Ss (th^n/ths)(h^{n+1}-h^n)]/V
+// with the last frozen K, so the water budget closes to rounding.
 #pragma once
-struct frehg_re;
-static int picard_step(frehg_re* re) {
-  (void)re;
-  fg::set_error("the Picard scheme is not built in this version");
-  return FREHG_ERR_UNSUPPORTED;
+
+#include "re_kernels.cuh"
+
+namespace fg {
+
+__device__ __forceinline__ double pic_mean(int harmonic, double a, double b) {
+  if (!harmonic) return 0.5 * (a + b);
+  const double s = a + b;
+  return s > 0.0 ? 2.0 * a * b / s : 0.0;
 }
+
+__device__ __forceinline__ double pic_qtop(const ReArgs& a, size_t col) {
+  if (a.rain_rate != 0.0) return a.sc->time < a.rain_until ? a.rain_rate : 0.0;
+  return a.has_qtop ? a.qtop_field[col] : a.qtop;
+}
+
+// Net inflow Q_c of cell (i,j,k) at the current iterate (a.h_new) with the frozen cell
+// conductivities Ks*kr; optionally the transmissibility sum and the +x/+y/+z couplings, and the
+// part of Q_c through the top / bottom domain faces.
+struct PicRow {
+  double q, tsum, tx, ty, tz, top, bot;
+};
+
+__device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, size_t c,
+                                          size_t col, int i, int j, int k) {
+  const int hm = a.face_mean;
+  const double dx = a.dx, dy = a.dy, dz = a.dz;
+  const double Ax = dy * dz, Ay = dx * dz, Az = dx * dy;
+  const double hc = a.h_new[c];
+  const double krc = a.kr[c];
+  const double Kxc = s.Ksx * krc, Kyc = s.Ksy * krc, Kzc = s.Ksz * krc;
+  PicRow r = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double t;
+  if (i > 0) {
+    const CellSoil sm = soil_of(a.soil, c - 1, col - 1);
+    t = pic_mean(hm, sm.Ksx * a.kr[c - 1], Kxc) * Ax / dx;
+    r.q += t * (a.h_new[c - 1] - hc);
+    r.tsum += t;
+  }
+  if (i + 1 < a.nx) {
+    const CellSoil sp = soil_of(a.soil, c + 1, col + 1);
+    t = pic_mean(hm, Kxc, sp.Ksx * a.kr[c + 1]) * Ax / dx;
+    r.q += t * (a.h_new[c + 1] - hc);
+    r.tsum += t;
+    r.tx = t;
+  }
+  if (j > 0) {
+    const CellSoil sm = soil_of(a.soil, c - a.nx, col - a.nx);
+    t = pic_mean(hm, sm.Ksy * a.kr[c - a.nx], Kyc) * Ay / dy;
+    r.q += t * (a.h_new[c - a.nx] - hc);
+    r.tsum += t;
+  }
+  if (j + 1 < a.ny) {
+    const CellSoil sp = soil_of(a.soil, c + a.nx, col + a.nx);
+    t = pic_mean(hm, Kyc, sp.Ksy * a.kr[c + a.nx]) * Ay / dy;
+    r.q += t * (a.h_new[c + a.nx] - hc);
+    r.tsum += t;
+    r.ty = t;
+  }
+  // face above
+  if (k > 0) {
+    const CellSoil sm = soil_of(a.soil, c - a.ncol, col);
+    const double kf = pic_mean(hm, sm.Ksz * a.kr[c - a.ncol], Kzc);
+    t = kf * Az / dz;
+    r.q += t * (a.h_new[c - a.ncol] - hc) + Az * kf;
+    r.tsum += t;
+  } else if (a.bc5 == 1) {
+    const double kf = s.Ksz;
+    t = kf * Az / (0.5 * dz);
+    r.top = t * (a.htop - hc) + Az * kf;
+    r.q += r.top;
+    r.tsum += t;
+  } else if (a.bc5 == 2) {
+    r.top = -pic_qtop(a, col) * Az;
+    r.q += r.top;
+  }
+  // face below
+  if (k + 1 < a.nz) {
+    const CellSoil sp = soil_of(a.soil, c + a.ncol, col);
+    const double kf = pic_mean(hm, Kzc, sp.Ksz * a.kr[c + a.ncol]);
+    t = kf * Az / dz;
+    r.q += t * (a.h_new[c + a.ncol] - hc) - Az * kf;
+    r.tsum += t;
+    r.tz = t;
+  } else if (a.bc4 == 1) {
+    const double kb = s.Ksz * vg_kr(s, a.hbot);
+    const double kf = pic_mean(hm, Kzc, kb);
+    t = kf * Az / (0.5 * dz);
+    r.bot = t * (a.hbot - hc) - Az * kf;
+    r.q += r.bot;
+    r.tsum += t;
+  } else if (a.bc4 == 2) {
+    r.bot = a.qbot * Az;
+    r.q += r.bot;
+  } else if (a.bc4 == 3) {
+    r.bot = -Kzc * Az;
+    r.q += r.bot;
+  }
+  return r;
+}
+
+// Linearised system of one Picard iteration (diagonal into dg, +x/+y/+z couplings, rhs).
+__global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restrict__ dg,
+                                                      double* __restrict__ a0,
+                                                      double* __restrict__ a1,
+                                                      double* __restrict__ a2,
+                                                      double* __restrict__ bvec) {
+  const double dt = a.sc->dt_used;
+  const double V = a.dx * a.dy * a.dz;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = c % a.ncol;
+    const int k = (int)(c / a.ncol), i = (int)(col % a.nx), j = (int)(col / a.nx);
+    const CellSoil s = soil_of(a.soil, c, col);
+    const double hc = a.h_new[c];
+    const double wcn = a.w_old[c];
+    const double th = vg_theta(s, hc);
+    const double C = vg_capacity(s, hc);
+    const PicRow r = pic_row(a, s, c, col, i, j, k);
+    dg[c] = V * (C + s.Ss * wcn / s.ths) + dt * r.tsum;
+    a0[c] = -dt * r.tx;
+    a1[c] = -dt * r.ty;
+    a2[c] = -dt * r.tz;
+    const double rdt = V * (th - wcn) + V * s.Ss * (wcn / s.ths) * (hc - a.h_old[c]) - dt * r.q;
+    bvec[c] = -rdt;
+  }
+}
+
+// h^{m+1} = h^m + d and |d|_inf
+__global__ void k_pic_update(ReArgs a, const double* __restrict__ d) {
+  double m = 0.0;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const double dc = d[c];
+    a.h_new[c] += dc;
+    m = fmax(m, fabs(dc));
+  }
+  double tot;
+  if (grid_max(m, a.partials + 2 * kMaxRedBlocks, &a.sc->arrive[1], &tot) && flat_tid() == 0)
+    a.sc->dq_max = tot;
+}
+
+// conservative water-content update + boundary / elastic volumes + time
+__global__ void k_pic_final(ReArgs a) {
+  const double dt = a.sc->dt_used;
+  const double V = a.dx * a.dy * a.dz;
+  double v[3] = {0.0, 0.0, 0.0};
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = c % a.ncol;
+    const int k = (int)(c / a.ncol), i = (int)(col % a.nx), j = (int)(col / a.nx);
+    const CellSoil s = soil_of(a.soil, c, col);
+    const double wcn = a.w_old[c];
+    const PicRow r = pic_row(a, s, c, col, i, j, k);
+    const double el = V * s.Ss * (wcn / s.ths) * (a.h_new[c] - a.h_old[c]);
+    a.w_new[c] = wcn + (dt * r.q - el) / V;
+    v[0] += r.top * dt;
+    v[1] += r.bot * dt;
+    v[2] += el;
+  }
+  double tot[3];
+  if (grid_sum<3>(v, a.partials, &a.sc->arrive[0], tot) && flat_tid() == 0) {
+    a.sc->vol_top += tot[0];
+    a.sc->vol_bot += tot[1];
+    a.sc->vol_elastic += tot[2];
+    a.sc->time += dt;
+  }
+}
+
+__global__ void k_copy64(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x)
+    dst[c] = src[c];
+}
+
+}  // namespace fg

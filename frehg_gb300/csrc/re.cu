@@ -163,6 +163,9 @@ static ReArgs make_args(frehg_re* re) {
   a.adaptive = re->p.adaptive_dt;
   a.use_corrector = re->p.use_corrector;
   a.has_qtop = re->has_qtop;
+  a.face_mean = re->p.face_mean;
+  a.rain_rate = re->p.rain_rate;
+  a.rain_until = re->p.rain_until;
   a.soil.cls = re->cls;
   a.soil.cid = re->cid;
   a.soil.cid3d = re->cid3d;
@@ -294,6 +297,7 @@ static int pca_step(frehg_re* re) {
   re->cnt.last_ksp_iterations = res.its;
   re->cnt.last_residual_norm = res.rnorm;
   re->cnt.ksp_iterations += res.its;
+  re->cnt.ir_sweeps += res.ir_its;
   if (rc != FREHG_OK) return rc;
   // enforceHeadBc + computeKFace + updateDiagnostics at h^{n+1} (the solve wrote h^{n+1})
   FG_LAUNCH(prof, st, "k_post", (24.0 + sb) * n, k_post<<<nb, 256, 0, st>>>(a));
@@ -334,6 +338,94 @@ static int pca_step(frehg_re* re) {
     FG_CUDA(cudaStreamSynchronize(st));
     FG_TRY(prof->flush());
   }
+  re->cur = 1 - re->cur;
+  re->ghosts_valid = true;
+  return FREHG_OK;
+}
+
+static int read_scalars(const frehg_re* re) {
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
+  return FREHG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Mixed-form modified Picard step (not in reference).  Host loop over Picard iterations: each
+// iteration assembles on the device, solves with the Krylov solver, updates h and reads |d|_inf.
+
+static int picard_step(frehg_re* re) {
+  cudaStream_t st = re->stream;
+  Profiler* prof = &re->prof;
+  const double n = (double)re->n, sb = soil_bytes(re);
+  const int nb = nblocks(re->n);
+  FG_TRY(read_scalars(re));
+  double dt = re->sc_host->dt;
+  ReArgs a = make_args(re);
+  int its = 0;
+  for (;;) {
+    FG_CUDA(cudaMemcpyAsync(&re->sc->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st));
+    FG_LAUNCH(prof, st, "k_step_begin", 0.0, k_step_begin<<<1, 1, 0, st>>>(re->sc));
+    FG_LAUNCH(prof, st, "k_copy64", 16.0 * n,
+              k_copy64<<<nb, 256, 0, st>>>(a.h_new, a.h_old, re->n));
+    bool converged = false;
+    int fail = FREHG_OK;
+    for (its = 0; its < re->p.picard_max_it; ++its) {
+      FG_LAUNCH(prof, st, "k_kr", (16.0 + sb) * n, k_kr<<<nb, 256, 0, st>>>(a, a.h_new, re->kr));
+      re->A.scaled = false;
+      FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
+                k_pic_assemble<<<nb, 256, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
+                                                   re->A.b));
+      FG_CUDA(cudaGetLastError());
+      CgResult res;
+      const int rc = re->ksp.solve(re->A, re->scratch, re->cfg, st, &res);
+      re->cnt.last_ksp_iterations = res.its;
+      re->cnt.last_residual_norm = res.rnorm;
+      re->cnt.ksp_iterations += res.its;
+      re->cnt.ir_sweeps += res.ir_its;
+      if (rc != FREHG_OK) {
+        fail = rc;
+        break;
+      }
+      FG_LAUNCH(prof, st, "k_pic_update", 24.0 * n,
+                k_pic_update<<<nb, 256, 0, st>>>(a, re->scratch));
+      FG_CUDA(cudaGetLastError());
+      FG_CUDA(cudaMemcpyAsync(&re->sc_host->dq_max, &re->sc->dq_max, sizeof(double),
+                              cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaStreamSynchronize(st));
+      if (prof->on) FG_TRY(prof->flush());
+      re->cnt.picard_iterations += 1;
+      if (re->sc_host->dq_max < re->p.picard_tol) {
+        converged = true;
+        ++its;
+        break;
+      }
+    }
+    if (converged) break;
+    if (!re->p.picard_dt_adapt || dt <= re->p.dt_min) {
+      if (fail == FREHG_OK) {
+        set_error("Picard iteration did not reach |dh| < %g in %d iterations (dt %g)",
+                  re->p.picard_tol, re->p.picard_max_it, dt);
+        fail = FREHG_ERR_NOT_CONVERGED;
+      }
+      re->cnt.last_picard_iterations = its;
+      return fail;
+    }
+    dt = fmax(0.5 * dt, re->p.dt_min);  // retry the step with half the time step
+  }
+  FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n, k_pic_final<<<nb, 256, 0, st>>>(a));
+  FG_CUDA(cudaGetLastError());
+  re->cnt.last_picard_iterations = its;
+  if (re->p.picard_dt_adapt) {
+    double nd = dt;
+    if (its <= 3)
+      nd = fmin(dt * 1.25, re->p.dt_max);
+    else if (its >= 8)
+      nd = fmax(dt * 0.7, re->p.dt_min);
+    FG_CUDA(cudaMemcpyAsync(&re->sc->dt, &nd, sizeof(double), cudaMemcpyHostToDevice, st));
+    re->p.dt = nd;
+  }
+  FG_CUDA(cudaStreamSynchronize(st));
+  if (prof->on) FG_TRY(prof->flush());
   re->cur = 1 - re->cur;
   re->ghosts_valid = true;
   return FREHG_OK;
@@ -609,11 +701,6 @@ int frehg_re_advance_steps(frehg_re* re, int nsteps) {
   return FREHG_OK;
 }
 
-static int read_scalars(const frehg_re* re) {
-  FG_CUDA(cudaStreamSynchronize(re->stream));
-  FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
-  return FREHG_OK;
-}
 
 int frehg_re_dt(const frehg_re* re, double* dt) {
   clear_error();
@@ -793,6 +880,8 @@ int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c) {
   FG_ARG(re && c, "null argument");
   *c = re->cnt;
   c->kernel_launches = re->prof.launches;
+  FG_TRY(read_scalars(re));
+  c->elastic_volume = re->sc_host->vol_elastic;
   return FREHG_OK;
 }
 

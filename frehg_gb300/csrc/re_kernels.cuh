@@ -59,6 +59,8 @@ struct ReArgs {
   double co_max, dt_min, dt_max;
   int bc4, bc5;
   int full3d, ghosts_valid, adaptive, use_corrector, has_qtop;
+  int face_mean;                   // Picard: 0 arithmetic, 1 harmonic
+  double rain_rate, rain_until;    // Picard: time-varying top flux
   SoilView soil;
   const double* h_old;  // h^n (and hn)
   const double* w_old;  // wc^n (and wcn)

@@ -225,6 +225,10 @@ class ReSolver:
               "boundaryVolumes")
         return t.value, b.value
 
+    def elastic_volume(self):
+        """Cumulative specific-storage volume of the Picard step (not in reference)."""
+        return self.counters().elastic_volume
+
     def set_profiling(self, on: bool):
         check(self._lib.frehg_re_set_profiling(self._h, int(bool(on))), "setProfiling")
 

@@ -187,6 +187,8 @@ typedef struct frehg_re_counters {
   int32_t last_picard_iterations;
   double last_residual_norm;
   int64_t kernel_launches;   /* kernels this handle launched (graph nodes included)      */
+  int64_t ir_sweeps;         /* mixed precision: FP64 refinement sweeps (not in reference)  */
+  double elastic_volume;     /* Picard: cumulative specific-storage volume [m^3]            */
 } frehg_re_counters;
 int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c);
 

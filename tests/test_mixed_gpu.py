@@ -1,0 +1,53 @@
+"""Mixed precision: FP32 Jacobi-PCG with compensated dots under FP64 iterative refinement to
+the FP64 true residual (not in reference).  Head error against the plain FP64 GPU path on the
+same inputs is checked per step (1e-8 m) and the true residual of every solve is verified."""
+import numpy as np
+import pytest
+
+from frehg_gb300 import workloads as W
+from frehg_gb300.abi import SolverConfig
+
+pytestmark = pytest.mark.gpu
+
+
+def make(w):
+    from frehg_gb300.re_solver import Grid, ReSolver
+    g = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
+    w.apply(g)
+    return g
+
+
+@pytest.mark.parametrize("scheme", ["pca", "picard"])
+def test_mixed_matches_fp64(gpu_lib, scheme):
+    w64 = W.config1(scheme, nx=32, ny=24, nz=32, steps=8)
+    w32 = W.config1(scheme, nx=32, ny=24, nz=32, steps=8, precision=1)
+    w32.solver.ir_rtol = 1e-12
+    a, b = make(w64), make(w32)
+    for s in range(w64.steps):
+        a.advance_step()
+        b.advance_step()
+        dh = np.abs(a.interior("h") - b.interior("h")).max()
+        assert dh <= 1e-8, f"step {s}: mixed vs fp64 head error {dh:.3e}"
+
+
+def test_mixed_seam_true_residual(gpu_lib):
+    from frehg_gb300.linear import makeLinearSolver
+    from tests.test_linear_seam_gpu import assemble, spd_stencil
+    nx, ny, nz = 12, 10, 16
+    coef, b = spd_stencil(nx, ny, nz, seed=7)
+    s = makeLinearSolver("gb300", SolverConfig("cg", "jacobi", rtol=1e-12, precision=1,
+                                               ir_rtol=1e-11, inner_rtol=1e-4))
+    A = s.createSystem(nx, ny, nz)
+    assemble(A, coef, nx, ny, nz)
+    x = s.solve(A, b)
+    # true residual in FP64 on the host
+    n = nx * ny * nz
+    offs = [0, -nz, nz, -nz * nx, nz * nx, -1, 1]
+    ax = np.zeros(n)
+    for r in range(n):
+        k, i, j = r % nz, (r // nz) % nx, r // (nz * nx)
+        present = [True, i > 0, i < nx - 1, j > 0, j < ny - 1, k > 0, k < nz - 1]
+        for q, (o, p) in enumerate(zip(offs, present)):
+            if p:
+                ax[r] += coef[r, q] * x[r + o]
+    assert np.linalg.norm(b - ax) <= 1.5e-11 * np.linalg.norm(b)
