@@ -16,6 +16,8 @@
 #include "reduce.cuh"
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 namespace fg {
@@ -32,15 +34,13 @@ struct Kahan32 {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-// r~ = s b - A~ x~ (FP64), written as FP32 into rf; e = 0; sums of r~^2 (FP32 view) for the
-// inner solve, (r~/s)^2 for the true residual and b^2 for ||b||.  The last block runs the
-// refinement test and initialises the inner CG state.
+// r~ = s b - A~ x~ (FP64, kept in rres); e = 0; sums of r~^2 (scale of the inner system),
+// (r~/s)^2 for the true residual and b^2 for ||b||.  The last block runs the refinement test.
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ s, const double* __restrict__ b, const double* __restrict__ x,
-    float* __restrict__ rf, float* __restrict__ ef, int n0, int n1, int n2, int planes,
-    int tiles, CgDevState* ir, CgDevState* in, double* partials, double ir_rtol,
-    double inner_rtol) {
+    double* __restrict__ rres, float* __restrict__ ef, int n0, int n1, int n2, int planes,
+    int tiles, CgDevState* ir, double* partials, double ir_rtol) {
   if (ir->status) return;
   const int t0 = (n0 + 31) / 32;
   double v[3] = {0.0, 0.0, 0.0};
@@ -61,10 +61,9 @@ __global__ void __launch_bounds__(256) k_ir_residual(
       if (k + 1 < n2) ax = fma(a2[c], x[c + s01], ax);
       const double sc = s[c], bc = b[c];
       const double r = fma(sc, bc, -ax);
-      const float r32 = (float)r;
-      rf[c] = r32;
+      rres[c] = r;
       ef[c] = 0.0f;
-      v[0] = fma((double)r32, (double)r32, v[0]);
+      v[0] = fma(r, r, v[0]);
       const double ru = r / sc;
       v[1] = fma(ru, ru, v[1]);
       v[2] = fma(bc, bc, v[2]);
@@ -77,19 +76,40 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     if (ir->ir_its == 0) ir->ir_bnorm = sqrt(tot[2]);
     ir->ir_rnorm = rn;
     ir->dp = rn;
+    ir->a = sqrt(tot[0]);  // scale of the inner right-hand side
     if (isnan(rn) || isinf(rn)) {
       ir->status = kDivergedNanOrInf;
-    } else if (rn <= fmax(ir_rtol * ir->ir_bnorm, ir->atol)) {
+    } else if (rn <= fmax(ir_rtol * ir->ir_bnorm, ir->atol) || tot[0] == 0.0) {
       ir->status = rn < ir->atol ? kConvergedAtol : kConvergedRtol;
     }
-    // inner CG state
+  }
+}
+
+// Inner right-hand side rf = fp32(r~ / ||r~||): unit norm, so FP32 products cannot underflow
+// however small the refinement residual is.  The last block initialises the inner CG state.
+__global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ rf, size_t n,
+                           const CgDevState* ir, CgDevState* in, double* partials,
+                           double inner_rtol) {
+  if (ir->status) return;
+  const double sig = 1.0 / ir->a;
+  Kahan32 acc;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const float r32 = (float)(rres[c] * sig);
+    rf[c] = r32;
+    acc.add(r32 * r32);
+  }
+  double loc[1] = {acc.value()};
+  double tot[1];
+  if (!grid_sum<1>(loc, partials, &in->arrive[0], tot)) return;
+  if (flat_tid() == 0) {
     in->beta = tot[0];
     in->rnorm0 = sqrt(tot[0]);
     in->ttol = inner_rtol * in->rnorm0;
     in->iter = 0;
     in->its = 0;
     in->dpi = 0.0;
-    in->status = (ir->status || tot[0] == 0.0) ? kConvergedAtol : 0;
+    in->status = tot[0] == 0.0 ? kConvergedAtol : 0;
   }
 }
 
@@ -193,10 +213,13 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
   }
 }
 
-__global__ void k_ir_update(double* __restrict__ x, const float* __restrict__ e, size_t n) {
+// x~ += ||r~|| e (the inner system was solved for the unit-norm residual)
+__global__ void k_ir_update(double* __restrict__ x, const float* __restrict__ e, size_t n,
+                            const CgDevState* ir) {
+  const double scale = ir->a;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
        c += (size_t)gridDim.x * blockDim.x)
-    x[c] += (double)e[c];
+    x[c] = fma(scale, (double)e[c], x[c]);
 }
 
 __global__ void k_to_f32(const double* __restrict__ a0, const double* __restrict__ a1,
@@ -233,6 +256,9 @@ int KrylovSolver::ensure32(size_t n) {
   FG_CUDA(cudaMalloc(&rf, n * sizeof(float)));
   FG_CUDA(cudaMalloc(&pf, n * sizeof(float)));
   FG_CUDA(cudaMalloc(&wf, n * sizeof(float)));
+  cudaFree(rres);
+  rres = nullptr;
+  FG_CUDA(cudaMalloc(&rres, n * sizeof(double)));
   FG_TRY(op32.alloc(n));
   if (!dst32) {
     FG_CUDA(cudaMalloc(&dst32, sizeof(CgDevState)));
@@ -296,11 +322,14 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
 
   const int max_sweeps = 60;
   int inner_total = 0, sweeps = 0;
+  const bool dbg = getenv("FREHG_DEBUG_IR") != nullptr;
   for (;;) {
     FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
               k_ir_residual<<<L.grid, L.block, 0, st>>>(
-                  A.a0, A.a1, A.a2, A.s, A.b, x, rf, xf, A.n0, A.n1, A.n2, L.planes, L.tiles, dst,
-                  dst32, partials, cfg.ir_rtol, cfg.inner_rtol));
+                  A.a0, A.a1, A.a2, A.s, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes, L.tiles,
+                  dst, partials, cfg.ir_rtol));
+    FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
+              k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials, cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());
     FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
@@ -331,7 +360,12 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       if (prof && prof->on) FG_TRY(prof->flush());
     }
     inner_total += hst32->its;
-    FG_LAUNCH(prof, st, "k_ir_update", 20.0 * dn, k_ir_update<<<nb, 256, 0, st>>>(x, xf, n));
+    if (dbg)
+      fprintf(stderr, "ir sweep %d: true |r| %.3e / |b| %.3e ; inner its %d status %d |r0| %.3e -> %.3e\n",
+              sweeps, hst->ir_rnorm, hst->ir_bnorm, hst32->its, hst32->status, hst32->rnorm0,
+              hst32->dp);
+    FG_LAUNCH(prof, st, "k_ir_update", 20.0 * dn,
+              k_ir_update<<<nb, 256, 0, st>>>(x, xf, n, dst));
     FG_CUDA(cudaGetLastError());
     ++sweeps;
     // next sweep's residual kernel re-arms the refinement bookkeeping
