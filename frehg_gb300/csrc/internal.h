@@ -81,7 +81,7 @@ class Profiler {
   } while (0)
 
 // Upper bound of the blocks any reduction kernel launches (partials buffers are sized to it).
-constexpr int kMaxRedBlocks = 4096;
+constexpr int kMaxRedBlocks = 32768;
 constexpr int kNumSMs = 152;
 
 // ------------------------------------------------------------------------------------------
@@ -168,6 +168,7 @@ class KrylovSolver {
   CgDevState* hst32 = nullptr;
   cudaStream_t g_stream32 = nullptr;
   size_t g_n32 = 0;
+  long g32_shape = 0;
   // graphs
   cudaGraphExec_t g64 = nullptr;
   cudaGraphExec_t g32 = nullptr;

@@ -23,6 +23,7 @@
 #include "reduce.cuh"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace fg {
@@ -43,7 +44,12 @@ StencilLaunch stencil_launch(int n0, int n1, int n2) {
   L.block = dim3(32, 8, 1);
   const int t0 = (n0 + 31) / 32, t1 = (n1 + 7) / 8;
   const long tiles = (long)t0 * t1;
-  const long target = (long)kNumSMs * 8;
+  static const long waves = [] {
+    const char* e = getenv("FREHG_STENCIL_WAVES");
+    const long v = e ? atol(e) : 2;
+    return v < 1 ? 1L : v;
+  }();
+  const long target = (long)kNumSMs * 8 * waves;
   long z = target / (tiles > 0 ? tiles : 1);
   if (z < 1) z = 1;
   if (z > n2) z = n2;
@@ -136,16 +142,29 @@ __global__ void k_cg_init(const double* __restrict__ s, const double* __restrict
   }
 }
 
-// p = r~ (first iteration) or p = r~ + bcoef p
+// p = r~ (first iteration) or p = r~ + bcoef p   (16-byte vector accesses)
 __global__ void k_cg_p(const double* __restrict__ r, double* __restrict__ p, size_t n,
                        const CgDevState* st) {
   if (st->status) return;
   const double bc = st->bcoef;
   const bool first = st->iter == 0;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
-       c += (size_t)gridDim.x * blockDim.x) {
-    p[c] = first ? r[c] : fma(bc, p[c], r[c]);
+  const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const double2* r2 = reinterpret_cast<const double2*>(r);
+  double2* p2 = reinterpret_cast<double2*>(p);
+  for (size_t q = gid; q < n / 2; q += stride) {
+    const double2 rv = r2[q];
+    double2 pv;
+    if (first) {
+      pv = rv;
+    } else {
+      pv = p2[q];
+      pv.x = fma(bc, pv.x, rv.x);
+      pv.y = fma(bc, pv.y, rv.y);
+    }
+    p2[q] = pv;
   }
+  if ((n & 1) && gid == 0) p[n - 1] = first ? r[n - 1] : fma(bc, p[n - 1], r[n - 1]);
 }
 
 // w = A~ p (unit diagonal) and p.w; the last block forms alpha.
@@ -223,8 +242,30 @@ __global__ void k_cg_update(double* __restrict__ x, double* __restrict__ r,
   if (st->status) return;
   const double a = st->a;
   double v[2] = {0.0, 0.0};
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
-       c += (size_t)gridDim.x * blockDim.x) {
+  const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  double2* x2 = reinterpret_cast<double2*>(x);
+  double2* r2 = reinterpret_cast<double2*>(r);
+  const double2* p2 = reinterpret_cast<const double2*>(p);
+  const double2* w2 = reinterpret_cast<const double2*>(w);
+  const double2* s2 = reinterpret_cast<const double2*>(s);
+  for (size_t q = gid; q < n / 2; q += stride) {
+    double2 xv = x2[q], rv = r2[q];
+    const double2 pv = p2[q], wv = w2[q], sv = s2[q];
+    xv.x = fma(a, pv.x, xv.x);
+    xv.y = fma(a, pv.y, xv.y);
+    rv.x = fma(-a, wv.x, rv.x);
+    rv.y = fma(-a, wv.y, rv.y);
+    x2[q] = xv;
+    r2[q] = rv;
+    v[0] = fma(rv.x, rv.x, v[0]);
+    v[0] = fma(rv.y, rv.y, v[0]);
+    const double zx = sv.x * rv.x, zy = sv.y * rv.y;
+    v[1] = fma(zx, zx, v[1]);
+    v[1] = fma(zy, zy, v[1]);
+  }
+  if ((n & 1) && gid == 0) {
+    const size_t c = n - 1;
     x[c] = fma(a, p[c], x[c]);
     const double rc = fma(-a, w[c], r[c]);
     r[c] = rc;

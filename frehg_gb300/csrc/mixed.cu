@@ -118,9 +118,28 @@ __global__ void k32_p(const float* __restrict__ r, float* __restrict__ p, size_t
   if (st->status) return;
   const float bc = (float)st->bcoef;
   const bool first = st->iter == 0;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
-       c += (size_t)gridDim.x * blockDim.x)
+  const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const float4* r4 = reinterpret_cast<const float4*>(r);
+  float4* p4 = reinterpret_cast<float4*>(p);
+  for (size_t q = gid; q < n / 4; q += stride) {
+    const float4 rv = r4[q];
+    float4 pv;
+    if (first) {
+      pv = rv;
+    } else {
+      pv = p4[q];
+      pv.x = fmaf(bc, pv.x, rv.x);
+      pv.y = fmaf(bc, pv.y, rv.y);
+      pv.z = fmaf(bc, pv.z, rv.z);
+      pv.w = fmaf(bc, pv.w, rv.w);
+    }
+    p4[q] = pv;
+  }
+  if (gid < (n & 3)) {
+    const size_t c = (n & ~(size_t)3) + gid;
     p[c] = first ? r[c] : fmaf(bc, p[c], r[c]);
+  }
 }
 
 __global__ void __launch_bounds__(256) k32_spmv(const float* __restrict__ a0,
@@ -178,14 +197,164 @@ __global__ void __launch_bounds__(256) k32_spmv(const float* __restrict__ a0,
   }
 }
 
+// Vectorised variant for n0 % 4 == 0: a thread owns 4 consecutive cells along axis 0 (16-byte
+// loads of p and the couplings); the axis-0 neighbours across threads come from warp shuffles,
+// the axis-2 neighbours roll in registers while the thread marches through its planes.
+__device__ __forceinline__ float4 ld4(const float* __restrict__ a, size_t c) {
+  return *reinterpret_cast<const float4*>(a + c);
+}
+
+__global__ void __launch_bounds__(128) k32_spmv_v4(const float* __restrict__ a0,
+                                                   const float* __restrict__ a1,
+                                                   const float* __restrict__ a2,
+                                                   const float* __restrict__ p,
+                                                   float* __restrict__ w, int n0, int n1, int n2,
+                                                   int planes, int tiles, CgDevState* st,
+                                                   double* partials) {
+  if (st->status) return;
+  const int t0 = (n0 + 127) / 128;
+  const int lane = threadIdx.x;
+  const unsigned full = 0xffffffffu;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  Kahan32 acc;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i0 = (tile % t0) * 128 + lane * 4;
+    const int i1 = (tile / t0) * 4 + threadIdx.y;
+    const bool act = i0 < n0 && i1 < n1;
+    const size_t s01 = (size_t)n0 * n1;
+    const int kb = blockIdx.y * planes, ke = min(n2, kb + planes);
+    size_t c = act ? (size_t)i0 + (size_t)n0 * i1 + s01 * kb : 0;
+    float4 pc = act ? ld4(p, c) : z4;
+    float4 pm = z4, am = z4;
+    if (act && kb > 0) {
+      pm = ld4(p, c - s01);
+      am = ld4(a2, c - s01);
+    }
+    for (int k = kb; k < ke; ++k) {
+      const bool up = act && k + 1 < n2;
+      const float4 pp = up ? ld4(p, c + s01) : z4;
+      const float4 A0 = act ? ld4(a0, c) : z4;
+      const float4 A1 = act ? ld4(a1, c) : z4;
+      const float4 A2 = act ? ld4(a2, c) : z4;
+      const bool hs = act && i1 > 0, hn = act && i1 + 1 < n1;
+      const float4 PS = hs ? ld4(p, c - n0) : z4;
+      const float4 AS = hs ? ld4(a1, c - n0) : z4;
+      const float4 PN = hn ? ld4(p, c + n0) : z4;
+      float pl = __shfl_up_sync(full, pc.w, 1);
+      float al = __shfl_up_sync(full, A0.w, 1);
+      float pr = __shfl_down_sync(full, pc.x, 1);
+      if (lane == 0) {
+        const bool l = act && i0 > 0;
+        pl = l ? p[c - 1] : 0.f;
+        al = l ? a0[c - 1] : 0.f;
+      }
+      if (lane == 31) pr = (act && i0 + 4 < n0) ? p[c + 4] : 0.f;
+      float4 v;
+      v.x = pc.x;
+      v.x = fmaf(al, pl, v.x);
+      v.x = fmaf(A0.x, pc.y, v.x);
+      v.y = fmaf(A0.x, pc.x, pc.y);
+      v.y = fmaf(A0.y, pc.z, v.y);
+      v.z = fmaf(A0.y, pc.y, pc.z);
+      v.z = fmaf(A0.z, pc.w, v.z);
+      v.w = fmaf(A0.z, pc.z, pc.w);
+      v.w = fmaf(A0.w, pr, v.w);
+      v.x = fmaf(AS.x, PS.x, v.x);
+      v.y = fmaf(AS.y, PS.y, v.y);
+      v.z = fmaf(AS.z, PS.z, v.z);
+      v.w = fmaf(AS.w, PS.w, v.w);
+      v.x = fmaf(A1.x, PN.x, v.x);
+      v.y = fmaf(A1.y, PN.y, v.y);
+      v.z = fmaf(A1.z, PN.z, v.z);
+      v.w = fmaf(A1.w, PN.w, v.w);
+      v.x = fmaf(am.x, pm.x, v.x);
+      v.y = fmaf(am.y, pm.y, v.y);
+      v.z = fmaf(am.z, pm.z, v.z);
+      v.w = fmaf(am.w, pm.w, v.w);
+      v.x = fmaf(A2.x, pp.x, v.x);
+      v.y = fmaf(A2.y, pp.y, v.y);
+      v.z = fmaf(A2.z, pp.z, v.z);
+      v.w = fmaf(A2.w, pp.w, v.w);
+      if (act) {
+        *reinterpret_cast<float4*>(w + c) = v;
+        acc.add(pc.x * v.x);
+        acc.add(pc.y * v.y);
+        acc.add(pc.z * v.z);
+        acc.add(pc.w * v.w);
+      }
+      pm = pc;
+      pc = pp;
+      am = A2;
+      c += s01;
+    }
+  }
+  double loc[1] = {acc.value()};
+  double tot[1];
+  if (!grid_sum<1>(loc, partials, &st->arrive[1], tot)) return;
+  if (flat_tid() == 0) {
+    const double dpi = tot[0];
+    st->its = st->iter + 1;
+    if (!(dpi > 0.0)) {
+      st->status = isnan(dpi) ? kDivergedNanOrInf : kDivergedIndefiniteMat;
+      return;
+    }
+    st->dpi = dpi;
+    st->a = st->beta / dpi;
+  }
+}
+
+// launch geometry of k32_spmv_v4: (32 x 4) threads cover 128 x 4 cells of a plane
+static StencilLaunch launch_v4(int n0, int n1, int n2) {
+  StencilLaunch L;
+  L.block = dim3(32, 4, 1);
+  const long tiles = (long)((n0 + 127) / 128) * ((n1 + 3) / 4);
+  const long target = (long)kNumSMs * 16 * 2;
+  long z = target / (tiles > 0 ? tiles : 1);
+  if (z < 1) z = 1;
+  if (z > n2) z = n2;
+  int planes = (int)((n2 + z - 1) / z);
+  z = (n2 + planes - 1) / planes;
+  long gx = tiles;
+  const long cap = kMaxRedBlocks / z;
+  if (gx > cap) gx = cap;
+  L.planes = planes;
+  L.tiles = (int)tiles;
+  L.grid = dim3((unsigned)gx, (unsigned)z, 1);
+  return L;
+}
+
 __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
                            const float* __restrict__ p, const float* __restrict__ w, size_t n,
                            CgDevState* st, double* partials) {
   if (st->status) return;
   const float a = (float)st->a;
   Kahan32 acc;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
-       c += (size_t)gridDim.x * blockDim.x) {
+  const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  float4* e4 = reinterpret_cast<float4*>(e);
+  float4* r4 = reinterpret_cast<float4*>(r);
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+  for (size_t q = gid; q < n / 4; q += stride) {
+    float4 ev = e4[q], rv = r4[q];
+    const float4 pv = p4[q], wv = w4[q];
+    ev.x = fmaf(a, pv.x, ev.x);
+    ev.y = fmaf(a, pv.y, ev.y);
+    ev.z = fmaf(a, pv.z, ev.z);
+    ev.w = fmaf(a, pv.w, ev.w);
+    rv.x = fmaf(-a, wv.x, rv.x);
+    rv.y = fmaf(-a, wv.y, rv.y);
+    rv.z = fmaf(-a, wv.z, rv.z);
+    rv.w = fmaf(-a, wv.w, rv.w);
+    e4[q] = ev;
+    r4[q] = rv;
+    acc.add(rv.x * rv.x);
+    acc.add(rv.y * rv.y);
+    acc.add(rv.z * rv.z);
+    acc.add(rv.w * rv.w);
+  }
+  if (gid < (n & 3)) {
+    const size_t c = (n & ~(size_t)3) + gid;
     e[c] = fmaf(a, p[c], e[c]);
     const float rc = fmaf(-a, w[c], r[c]);
     r[c] = rc;
@@ -276,6 +445,8 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   const int nb = reduction_blocks(n, 256, 4);
   const double dn = (double)n;
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
+  const bool vec4 = (A.n0 % 4) == 0 && getenv("FREHG_NO_VEC4") == nullptr;
+  const StencilLaunch L4 = launch_v4(A.n0, A.n1, A.n2);
   FG_LAUNCH(prof, st, "k_to_f32", 36.0 * dn,
             k_to_f32<<<nb, 256, 0, st>>>(A.a0, A.a1, A.a2, op32.a0, op32.a1, op32.a2, n));
   FG_LAUNCH(prof, st, "k_zero64", 8.0 * dn, k_zero64<<<nb, 256, 0, st>>>(x, n));
@@ -289,7 +460,8 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
 
   const int chunk = 32;
-  const bool rebuild = !g32 || g32_key != (const void*)op32.a0 || g_stream32 != st || g_n32 != n;
+  const bool rebuild = !g32 || g32_key != (const void*)op32.a0 || g_stream32 != st || g_n32 != n ||
+                       g32_shape != (long)A.n0 * 1000003L + A.n1;
   if (!(prof && prof->on) && rebuild) {
     if (g32) cudaGraphExecDestroy(g32);
     g32 = nullptr;
@@ -299,8 +471,13 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     FG_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
     for (int q = 0; q < chunk; ++q) {
       k32_p<<<nb, 256, 0, cap_st>>>(rf, pf, n, dst32);
-      k32_spmv<<<L.grid, L.block, 0, cap_st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1,
-                                               A.n2, L.planes, L.tiles, dst32, partials);
+      if (vec4)
+        k32_spmv_v4<<<L4.grid, L4.block, 0, cap_st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0,
+                                                       A.n1, A.n2, L4.planes, L4.tiles, dst32,
+                                                       partials);
+      else
+        k32_spmv<<<L.grid, L.block, 0, cap_st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1,
+                                                 A.n2, L.planes, L.tiles, dst32, partials);
       k32_update<<<nb, 256, 0, cap_st>>>(xf, rf, pf, wf, n, dst32, partials);
     }
     cudaError_t e = cudaStreamEndCapture(cap_st, &graph);
@@ -318,6 +495,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     g32_key = op32.a0;
     g_stream32 = st;
     g_n32 = n;
+    g32_shape = (long)A.n0 * 1000003L + A.n1;
   }
 
   const int max_sweeps = 60;
@@ -343,10 +521,16 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       if (prof && prof->on) {
         for (int it = 0; it < chunk; ++it) {
           FG_LAUNCH(prof, st, "k32_p", 12.0 * dn, k32_p<<<nb, 256, 0, st>>>(rf, pf, n, dst32));
-          FG_LAUNCH(prof, st, "k32_spmv", 20.0 * dn,
-                    k32_spmv<<<L.grid, L.block, 0, st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0,
-                                                         A.n1, A.n2, L.planes, L.tiles, dst32,
-                                                         partials));
+          if (vec4)
+            FG_LAUNCH(prof, st, "k32_spmv_v4", 20.0 * dn,
+                      k32_spmv_v4<<<L4.grid, L4.block, 0, st>>>(
+                          op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1, A.n2, L4.planes,
+                          L4.tiles, dst32, partials));
+          else
+            FG_LAUNCH(prof, st, "k32_spmv", 20.0 * dn,
+                      k32_spmv<<<L.grid, L.block, 0, st>>>(op32.a0, op32.a1, op32.a2, pf, wf,
+                                                           A.n0, A.n1, A.n2, L.planes, L.tiles,
+                                                           dst32, partials));
           FG_LAUNCH(prof, st, "k32_update", 24.0 * dn,
                     k32_update<<<nb, 256, 0, st>>>(xf, rf, pf, wf, n, dst32, partials));
         }
