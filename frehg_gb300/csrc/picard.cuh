@@ -123,8 +123,8 @@ __global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restri
     const CellSoil s = soil_of(a.soil, c, col);
     const double hc = a.h_new[c];
     const double wcn = a.w_old[c];
-    const double th = vg_theta(s, hc);
-    const double C = vg_capacity(s, hc);
+    const double th = a.wch[c];  // theta(h^m) and C(h^m) from k_constit
+    const double C = a.cap[c];
     const PicRow r = pic_row(a, s, c, col, i, j, k);
     dg[c] = V * (C + s.Ss * wcn / s.ths) + dt * r.tsum;
     a0[c] = -dt * r.tx;

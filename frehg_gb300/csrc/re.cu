@@ -29,6 +29,7 @@ struct frehg_re {
   double* W[2] = {nullptr, nullptr};
   double* kr = nullptr;
   double* wch = nullptr;
+  double* cap = nullptr;
   double* qx = nullptr;
   double* qy = nullptr;
   double* qz = nullptr;
@@ -63,6 +64,7 @@ frehg_re::~frehg_re() {
   }
   cudaFree(kr);
   cudaFree(wch);
+  cudaFree(cap);
   cudaFree(qx);
   cudaFree(qy);
   cudaFree(qz);
@@ -177,6 +179,7 @@ static ReArgs make_args(frehg_re* re) {
   a.w_new = re->W[1 - re->cur];
   a.kr = re->kr;
   a.wch = re->wch;
+  a.cap = re->cap;
   a.qx = re->qx;
   a.qy = re->qy;
   a.qz = re->qz;
@@ -283,11 +286,12 @@ static int pca_step(frehg_re* re) {
   const double n = (double)re->n, sb = soil_bytes(re);
   FG_LAUNCH(prof, st, "k_step_begin", 0.0, k_step_begin<<<1, 1, 0, st>>>(re->sc));
   // computeKFace inputs at h^n
-  FG_LAUNCH(prof, st, "k_kr", (16.0 + sb) * n, k_kr<<<nb, 256, 0, st>>>(a, a.h_old, re->kr));
+  FG_LAUNCH(prof, st, "k_kr", (24.0 + sb) * n,
+            (k_constit<false, true><<<nb, 256, 0, st>>>(a, a.h_old, re->kr, nullptr, re->cap)));
   // groundwaterMatCoeff + groundwaterRhs + assembly
   const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
   re->A.scaled = false;
-  FG_LAUNCH(prof, st, "k_assemble", (64.0 + sb) * n,
+  FG_LAUNCH(prof, st, "k_assemble", (72.0 + sb) * n,
             k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
                                                    re->A.b, L.planes, L.tiles));
   FG_CUDA(cudaGetLastError());
@@ -370,7 +374,8 @@ static int picard_step(frehg_re* re) {
     bool converged = false;
     int fail = FREHG_OK;
     for (its = 0; its < re->p.picard_max_it; ++its) {
-      FG_LAUNCH(prof, st, "k_kr", (16.0 + sb) * n, k_kr<<<nb, 256, 0, st>>>(a, a.h_new, re->kr));
+      FG_LAUNCH(prof, st, "k_kr", (32.0 + sb) * n,
+                (k_constit<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch, re->cap)));
       re->A.scaled = false;
       FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
                 k_pic_assemble<<<nb, 256, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
@@ -493,6 +498,7 @@ int frehg_re_create(int nx, int ny, int nz, const frehg_re_params* p, frehg_re**
   }
   ALLOC(re->kr, n * sizeof(double));
   ALLOC(re->wch, n * sizeof(double));
+  ALLOC(re->cap, n * sizeof(double));
   ALLOC(re->qx, n * sizeof(double));
   ALLOC(re->qy, n * sizeof(double));
   ALLOC(re->qz, n * sizeof(double));

@@ -68,6 +68,7 @@ struct ReArgs {
   double* w_new;
   double* kr;
   double* wch;
+  double* cap;
   double* qx;
   double* qy;
   double* qz;
@@ -137,13 +138,18 @@ __device__ __forceinline__ bool cell_sat(const ReArgs& a, size_t c, size_t col, 
 // savePreviousStepFields' scalar part: the dt this step applies (ReSolver.cpp:932)
 __global__ void k_step_begin(ReScalars* sc) { sc->dt_used = sc->dt; }
 
-// kr at the given head
-__global__ void k_kr(ReArgs a, const double* __restrict__ h, double* __restrict__ kr) {
+// kr (and optionally theta and C) at the given head, from one set of transcendentals
+template <bool THETA, bool CAP>
+__global__ void k_constit(ReArgs a, const double* __restrict__ h, double* __restrict__ kr,
+                          double* __restrict__ th, double* __restrict__ cap) {
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
        c += (size_t)gridDim.x * blockDim.x) {
     const size_t col = c % a.ncol;
     const CellSoil s = soil_of(a.soil, c, col);
-    kr[c] = vg_kr(s, h[c]);
+    const Constit r = vg_constit<THETA, CAP>(s, h[c]);
+    kr[c] = r.kr;
+    if (THETA) th[c] = r.theta;
+    if (CAP) cap[c] = r.cap;
   }
 }
 
@@ -170,7 +176,7 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
     const CellSoil s = soil_of(a.soil, c, col);
     const double hc = a.h_old[c];
     const double krc = a.kr[c];
-    const double ch = vg_capacity(s, hc);
+    const double ch = a.cap[c];
     const double wcn = a.w_old[c];
     const bool sat_c = a.full3d ? true : (wcn >= s.ths);
     // ghost conductivity of this cell: K(h ghost) = K(h_c) once ghosts exist, K(0) = Ks before
@@ -279,9 +285,9 @@ __global__ void k_post(ReArgs a) {
        c += (size_t)gridDim.x * blockDim.x) {
     const size_t col = c % a.ncol;
     const CellSoil so = soil_of(a.soil, c, col);
-    const double h = a.h_new[c];
-    a.kr[c] = vg_kr(so, h);
-    a.wch[c] = vg_theta(so, h);
+    const Constit r = vg_constit<true, false>(so, a.h_new[c]);
+    a.kr[c] = r.kr;
+    a.wch[c] = r.theta;
   }
 }
 

@@ -143,6 +143,63 @@ __device__ __forceinline__ double vg_kr(const CellSoil& s, double h) {
   return kr;
 }
 
+// kr, theta and C at one head from one set of transcendental calls (VG, not MVG).  With
+// L = ln|alpha h|, t = e^{nL} = |alpha h|^n, u = ln(1 + t):
+//   se = (1+t)^-m = e^{-mu},  se^{1/m} = 1/(1+t),  1 - se^{1/m} = t/(1+t),
+//   (1 - se^{1/m})^m = e^{m(nL - u)},  kr = e^{-mu/2} (1 - e^{m(nL-u)})^2,
+//   C = alpha n m (ths - thr) |alpha h|^{n-1} (1+t)^{-(m+1)} = alpha n m (ths-thr) e^{(n-1)L - (m+1)u}.
+// The same relations as the reference's pow() forms (VanGenuchten.hpp:31-111), evaluated with
+// 2 logarithms and 3-4 exponentials instead of 11 pow() calls; 1 - e^{x} is formed as -expm1(x)
+// so no digits cancel when the soil is dry.  The caps and the saturated branches are the
+// reference's.  MVG and the exponential model use the reference forms above.
+struct Constit {
+  double kr, theta, cap;
+};
+
+template <bool WANT_THETA, bool WANT_CAP>
+__device__ __forceinline__ Constit vg_constit(const CellSoil& s, double h) {
+  Constit r;
+  if (!s.use_vg || s.use_mvg) {
+    r.kr = vg_kr(s, h);
+    r.theta = WANT_THETA ? vg_theta(s, h) : 0.0;
+    r.cap = WANT_CAP ? vg_capacity(s, h) : 0.0;
+    return r;
+  }
+  const double mm = s.m;
+  const double ah = fabs(s.alpha * h);
+  const double L = log(ah);
+  const double nL = s.n * L;
+  const double t = exp(nL);
+  const double u = log1p(t);
+  const double mu = mm * u;
+  // kr
+  const double one_minus = -expm1(mm * (nL - u));
+  double kr = exp(-0.5 * mu) * (one_minus * one_minus);
+  if (kr > 1.0) kr = 1.0;
+  if (h > 0.0) kr = 1.0;
+  r.kr = kr;
+  if (WANT_THETA) {
+    double wc;
+    if (h > s.aev)
+      wc = s.ths;
+    else
+      wc = s.thr + (s.ths - s.thr) * exp(-mu);
+    if (wc > s.ths) wc = s.ths;
+    if (wc < s.thr) wc = s.thr;
+    r.theta = wc;
+  } else {
+    r.theta = 0.0;
+  }
+  if (WANT_CAP) {
+    double c = s.alpha * s.n * mm * (s.ths - s.thr) * exp((s.n - 1.0) * L - (mm + 1.0) * u);
+    if (h > 0.0) c = 0.0;
+    r.cap = c;
+  } else {
+    r.cap = 0.0;
+  }
+  return r;
+}
+
 // dKdwc (VanGenuchten.hpp:114-136)
 __device__ __forceinline__ double vg_dKdwc(const CellSoil& s, double wc, double Ks) {
   double theta = wc;
