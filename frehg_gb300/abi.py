@@ -238,6 +238,17 @@ SIGNATURES = {
     "frehg_cg_converged_reason": (C.c_int, [_VP, _PI]),
     "frehg_cg_solve_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _VP,
                                          _VP, C.POINTER(SolverConfig), _VP, _PI, _PD]),
+    "frehg_unet_create": (C.c_int, [C.c_uint64, C.POINTER(_VP)]),
+    "frehg_unet_destroy": (C.c_int, [_VP]),
+    "frehg_unet_num_params": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
+    "frehg_unet_get_params": (C.c_int, [_VP, C.POINTER(C.c_float)]),
+    "frehg_unet_set_params": (C.c_int, [_VP, C.POINTER(C.c_float)]),
+    "frehg_unet_set_input_scaling": (C.c_int, [_VP, C.c_float, C.c_float, C.c_float]),
+    "frehg_unet_forward": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _VP]),
+    "frehg_unet_loss_grad": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _PD,
+                                       C.POINTER(C.c_float), _VP]),
+    "frehg_unet_adam_step": (C.c_int, [_VP, C.c_float, C.c_float, C.c_float, C.c_float, _VP]),
+    "frehg_unet_flops": (C.c_int, [C.c_int, C.c_int, C.c_int, _PD]),
     "frehg_build_arch": (C.c_int, []),
 }
 

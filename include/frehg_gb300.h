@@ -256,6 +256,35 @@ int frehg_cg_iteration_count(const frehg_cg* cg, int* its);   /* getIterationCou
 int frehg_cg_residual_norm(const frehg_cg* cg, double* rnorm); /* getResidualNorm   */
 int frehg_cg_converged_reason(const frehg_cg* cg, int* reason); /* KSPConvergedReason */
 
+/* ------------------------------------------------------------------------------------------ */
+/* Learned preconditioner (not in reference): 3-level 3D U-Net (16/32/64 channels, 3x3x3 conv,  */
+/* BF16 weights and activations on the tensor cores, FP32 accumulation) with its own forward,   */
+/* backward and Adam kernels.  Inputs are FP32 device arrays of nx*ny*nz cells (i fastest);     */
+/* nx, ny, nz must be divisible by 4.                                                          */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct frehg_unet frehg_unet;
+int frehg_unet_create(uint64_t seed, frehg_unet** out);
+int frehg_unet_destroy(frehg_unet* net);
+int frehg_unet_num_params(const frehg_unet* net, int64_t* n);
+/* FP32 master parameters to / from host memory (layout: per convolution W[27][cout][cin] then
+ * b[cout], for c1a c1b c2a c2b c3a c3b d2a d2b d1a d1b; then the output w[16], b). */
+int frehg_unet_get_params(frehg_unet* net, float* host);
+int frehg_unet_set_params(frehg_unet* net, const float* host);
+/* input channel scaling: ln K -> (ln K - mean) * scale; capacity -> C * cap_scale */
+int frehg_unet_set_input_scaling(frehg_unet* net, float lnk_mean, float lnk_scale, float cap_scale);
+/* y = rms(r) * NN(r / rms(r), ln K, C) */
+int frehg_unet_forward(frehg_unet* net, int nx, int ny, int nz, const float* r, const float* lnk,
+                       const float* cap, float* y, void* stream);
+/* loss = mean((NN(r / rms r) - target / rms r)^2) and the parameter gradients (kept in the
+ * network for frehg_unet_adam_step; copied to grad_host when it is not NULL). */
+int frehg_unet_loss_grad(frehg_unet* net, int nx, int ny, int nz, const float* r,
+                         const float* lnk, const float* cap, const float* target, double* loss,
+                         float* grad_host, void* stream);
+int frehg_unet_adam_step(frehg_unet* net, float lr, float beta1, float beta2, float eps,
+                         void* stream);
+/* floating-point operations of one forward application on an nx*ny*nz grid */
+int frehg_unet_flops(int nx, int ny, int nz, double* flops);
+
 /* Allocation-free CG solve.  No counterpart in the reference: it exists for callers that may
  * not allocate GPU memory themselves (a component under a host framework that owns the device
  * memory budget, or a time-critical loop that cannot take cudaMalloc's synchronisation).  The

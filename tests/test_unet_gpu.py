@@ -1,0 +1,92 @@
+"""The U-Net kernels on the GPU against the numpy statement (oracle/unet_ref.py): forward output,
+loss and every parameter gradient, with BF16 rounding emulated at the GPU's storage points.
+Also: Adam steps lower the loss, and the FLOP count of one application."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import unet_ref as U
+
+pytestmark = pytest.mark.gpu
+
+
+def net_with(lib, params):
+    h = C.c_void_p()
+    assert lib.frehg_unet_create(1, C.byref(h)) == 0
+    n = C.c_int64()
+    lib.frehg_unet_num_params(h, C.byref(n))
+    assert n.value == params.size
+    p32 = np.ascontiguousarray(params, dtype=np.float32)
+    assert lib.frehg_unet_set_params(h, p32.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    return h
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (4, 12, 16)])
+def test_forward_and_gradients_match_reference(gpu_lib, shape):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    r = rng.standard_normal(shape).astype(np.float32)
+    lnk = rng.standard_normal(shape).astype(np.float32)
+    cap = rng.uniform(0, 1, shape).astype(np.float32)
+    tgt = rng.standard_normal(shape).astype(np.float32)
+    params = U.init_params(5)
+    h = net_with(gpu_lib, params)
+    nz, ny, nx = shape
+    tr, tk, tc, tt = dev(torch, r), dev(torch, lnk), dev(torch, cap), dev(torch, tgt)
+    y = torch.empty_like(tr)
+    assert gpu_lib.frehg_unet_forward(h, nx, ny, nz, tr.data_ptr(), tk.data_ptr(), tc.data_ptr(),
+                                      y.data_ptr(), None) == 0
+    yref, _, rms = U.forward(params, r, lnk, cap)
+    yg = y.cpu().numpy()
+    assert np.abs(yg - yref * rms).max() <= 2e-2 * np.abs(yref * rms).max()
+    loss = C.c_double()
+    g = np.zeros(params.size, dtype=np.float32)
+    assert gpu_lib.frehg_unet_loss_grad(h, nx, ny, nz, tr.data_ptr(), tk.data_ptr(),
+                                        tc.data_ptr(), tt.data_ptr(), C.byref(loss),
+                                        g.ctypes.data_as(C.POINTER(C.c_float)), None) == 0
+    lref, gref = U.loss_grad(params, r, lnk, cap, tgt)
+    assert abs(loss.value - lref) <= 1e-3 * abs(lref)
+    woff, boff, ooff, ntot = U.layout()
+    cos = float(g @ gref / (np.linalg.norm(g) * np.linalg.norm(gref)))
+    assert cos > 0.999, cos
+    for l in range(10):
+        a = g[woff[l]:boff[l]]
+        b = gref[woff[l]:boff[l]]
+        assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b) + 1e-12, l
+    gpu_lib.frehg_unet_destroy(h)
+
+
+def test_adam_lowers_the_loss(gpu_lib):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(2)
+    shape = (8, 16, 16)
+    r = rng.standard_normal(shape).astype(np.float32)
+    lnk = np.zeros(shape, np.float32)
+    cap = np.zeros(shape, np.float32)
+    tgt = (0.5 * r + 0.1).astype(np.float32)
+    h = C.c_void_p()
+    assert gpu_lib.frehg_unet_create(3, C.byref(h)) == 0
+    tr, tk, tc, tt = dev(torch, r), dev(torch, lnk), dev(torch, cap), dev(torch, tgt)
+    losses = []
+    for it in range(60):
+        loss = C.c_double()
+        assert gpu_lib.frehg_unet_loss_grad(h, 16, 16, 8, tr.data_ptr(), tk.data_ptr(),
+                                            tc.data_ptr(), tt.data_ptr(), C.byref(loss), None,
+                                            None) == 0
+        losses.append(loss.value)
+        assert gpu_lib.frehg_unet_adam_step(h, 1e-3, 0.9, 0.999, 1e-8, None) == 0
+    assert losses[-1] < 0.5 * losses[0], losses[::10]
+    gpu_lib.frehg_unet_destroy(h)
+
+
+def test_flop_count(gpu_lib):
+    f = C.c_double()
+    assert gpu_lib.frehg_unet_flops(256, 256, 128, C.byref(f)) == 0
+    n = 256 * 256 * 128
+    per_cell = f.value / n
+    assert 1.0e5 < per_cell < 2.0e5
