@@ -164,6 +164,7 @@ class ReCounters(C.Structure):
         ("last_residual_norm", C.c_double),
         ("kernel_launches", C.c_int64),
         ("ir_sweeps", C.c_int64),
+        ("fcg_fallbacks", C.c_int64),
         ("elastic_volume", C.c_double),
     ]
 
@@ -249,6 +250,8 @@ SIGNATURES = {
                                        C.POINTER(C.c_float), _VP]),
     "frehg_unet_adam_step": (C.c_int, [_VP, C.c_float, C.c_float, C.c_float, C.c_float, _VP]),
     "frehg_unet_flops": (C.c_int, [C.c_int, C.c_int, C.c_int, _PD]),
+    "frehg_re_attach_unet": (C.c_int, [_VP, _VP]),
+    "frehg_re_training_pairs": (C.c_int, [_VP, C.c_int, _PI, _VP, _VP, _VP, _VP]),
     "frehg_build_arch": (C.c_int, []),
 }
 

@@ -134,11 +134,25 @@ enum {
 };
 
 struct CgResult {
+  int fallback = 0;   // the learned preconditioner was dropped for Jacobi during this solve
   int its = 0;
   int reason = 0;
   double rnorm = 0.0;
   int inner_its = 0;  // mixed precision: total fp32 iterations
   int ir_its = 0;     // mixed precision: refinement sweeps
+};
+
+// Learned preconditioner context of a solve (the network and its per-cell input fields).
+}  // namespace fg
+struct frehg_unet;
+namespace fg {
+int unet_apply(frehg_unet* net, int nx, int ny, int nz, const float* r, const float* lnk,
+               const float* cap, float* z, cudaStream_t st);
+struct NetPrecond {
+  frehg_unet* net = nullptr;
+  const float* lnk = nullptr;
+  const float* cap = nullptr;
+  int max_inner = 0;  // fall back to Jacobi CG beyond this many inner iterations (0 = never)
 };
 
 // Jacobi-preconditioned CG in FP64 (3 kernels per iteration, CUDA-graph chunks), with an
@@ -175,6 +189,8 @@ class KrylovSolver {
   const void* g64_key = nullptr;
   const void* g64_key2 = nullptr;
   Profiler* prof = nullptr;  // owner's profiler (launch counts, optional event timing)
+  NetPrecond net;            // learned preconditioner (FCG inner solves when set)
+  float* zf = nullptr;
   const void* g32_key = nullptr;
   cudaStream_t g_stream = nullptr;
   size_t g_n = 0;

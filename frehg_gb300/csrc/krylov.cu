@@ -369,6 +369,7 @@ KrylovSolver::~KrylovSolver() {
   cudaFree(rres);
   cudaFree(dst32);
   cudaFreeHost(hst32);
+  cudaFree(zf);
   op32.release();
 }
 

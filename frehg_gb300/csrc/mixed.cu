@@ -408,6 +408,55 @@ __global__ void k_zero64(double* __restrict__ x, size_t n) {
     x[c] = 0.0;
 }
 
+// ---- flexible CG (FCG(1), Notay 2000) with a nonlinear preconditioner z = M(r) ----------
+//   beta = -(z . A p_prev) / (p_prev . A p_prev);  p = z + beta p_prev;  alpha = (p . r)/(p . A p)
+// k_fcg_beta forms beta from z . w_prev (w_prev = A p_prev still holds the previous SpMV);
+// k_fcg_p forms p and p . r, stored as st->beta so that k32_spmv* yields alpha = (p.r)/(p.Ap).
+__global__ void k_fcg_beta(const float* __restrict__ z, const float* __restrict__ w, size_t n,
+                           CgDevState* st, double* partials) {
+  if (st->status) return;
+  Kahan32 acc;
+  if (st->iter > 0)
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x)
+      acc.add(z[c] * w[c]);
+  double loc[1] = {acc.value()};
+  double tot[1];
+  if (!grid_sum<1>(loc, partials, &st->arrive[3], tot)) return;
+  if (flat_tid() == 0) st->bcoef = st->iter > 0 ? -tot[0] / st->dpi : 0.0;
+}
+
+__global__ void k_fcg_p(const float* __restrict__ z, float* __restrict__ p,
+                        const float* __restrict__ r, size_t n, CgDevState* st, double* partials) {
+  if (st->status) return;
+  const float bc = (float)st->bcoef;
+  const bool first = st->iter == 0;
+  Kahan32 acc;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const float pv = first ? z[c] : fmaf(bc, p[c], z[c]);
+    p[c] = pv;
+    acc.add(pv * r[c]);
+  }
+  double loc[1] = {acc.value()};
+  double tot[1];
+  if (!grid_sum<1>(loc, partials, &st->arrive[4], tot)) return;
+  if (flat_tid() == 0) st->beta = tot[0];
+}
+
+// z += r: the network supplies the correction on top of the (unit-diagonal) Jacobi step
+__global__ void k_add_f32(float* __restrict__ z, const float* __restrict__ r, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x)
+    z[c] += r[c];
+}
+
+__global__ void k_cast_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x)
+    b[c] = (float)a[c];
+}
+
 // ------------------------------------------------------------------------------------------
 
 int KrylovSolver::ensure32(size_t n) {
@@ -500,6 +549,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
 
   const int max_sweeps = 60;
   int inner_total = 0, sweeps = 0;
+  bool fcg_fallback = false;
   const bool dbg = getenv("FREHG_DEBUG_IR") != nullptr;
   for (;;) {
     FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
@@ -514,10 +564,50 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     if (prof && prof->on) FG_TRY(prof->flush());
     if (hst->status != 0) break;
     if (sweeps >= max_sweeps) break;
-    // inner FP32 solve
+    // inner FP32 solve: flexible CG with the learned preconditioner, or Jacobi CG
     FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
-    for (int q = 0; q < cfg.max_it / chunk + 2 && hst32->status == 0; ++q) {
+    const bool use_net = net.net != nullptr && !fcg_fallback;
+    if (use_net) {
+      if (!zf) {
+        FG_CUDA(cudaMalloc(&zf, cap32 * sizeof(float)));
+      }
+      const int check = 4;
+      for (int it = 0; it < cfg.max_it && hst32->status == 0; ++it) {
+        FG_TRY(unet_apply(net.net, A.n0, A.n1, A.n2, rf, net.lnk, net.cap, zf, st));
+        FG_LAUNCH(prof, st, "k_add_f32", 12.0 * dn, k_add_f32<<<nb, 256, 0, st>>>(zf, rf, n));
+        FG_LAUNCH(prof, st, "k_fcg_beta", 8.0 * dn,
+                  k_fcg_beta<<<nb, 256, 0, st>>>(zf, wf, n, dst32, partials));
+        FG_LAUNCH(prof, st, "k_fcg_p", 16.0 * dn,
+                  k_fcg_p<<<nb, 256, 0, st>>>(zf, pf, rf, n, dst32, partials));
+        if (vec4)
+          FG_LAUNCH(prof, st, "k32_spmv_v4", 20.0 * dn,
+                    k32_spmv_v4<<<L4.grid, L4.block, 0, st>>>(op32.a0, op32.a1, op32.a2, pf, wf,
+                                                              A.n0, A.n1, A.n2, L4.planes,
+                                                              L4.tiles, dst32, partials));
+        else
+          FG_LAUNCH(prof, st, "k32_spmv", 20.0 * dn,
+                    k32_spmv<<<L.grid, L.block, 0, st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0,
+                                                         A.n1, A.n2, L.planes, L.tiles, dst32,
+                                                         partials));
+        FG_LAUNCH(prof, st, "k32_update", 24.0 * dn,
+                  k32_update<<<nb, 256, 0, st>>>(xf, rf, pf, wf, n, dst32, partials));
+        FG_CUDA(cudaGetLastError());
+        if ((it + 1) % check == 0) {
+          FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+          FG_CUDA(cudaStreamSynchronize(st));
+          if (prof && prof->on) FG_TRY(prof->flush());
+          if (net.max_inner > 0 && inner_total + hst32->its > net.max_inner) {
+            fcg_fallback = true;  // too slow: Jacobi CG from here on (the iterate is kept)
+            break;
+          }
+        }
+      }
+      FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaStreamSynchronize(st));
+      if (prof && prof->on) FG_TRY(prof->flush());
+    }
+    for (int q = 0; !use_net && q < cfg.max_it / chunk + 2 && hst32->status == 0; ++q) {
       if (prof && prof->on) {
         for (int it = 0; it < chunk; ++it) {
           FG_LAUNCH(prof, st, "k32_p", 12.0 * dn, k32_p<<<nb, 256, 0, st>>>(rf, pf, n, dst32));
@@ -559,6 +649,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   res->its = inner_total;
   res->inner_its = inner_total;
   res->ir_its = sweeps;
+  res->fallback = fcg_fallback ? 1 : 0;
   res->rnorm = hst->ir_rnorm;
   res->reason = hst->status;
   if (hst->status <= 0) {

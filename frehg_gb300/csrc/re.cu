@@ -4,6 +4,7 @@
 #include "internal.h"
 #include "re_kernels.cuh"
 #include "picard.cuh"
+#include "krylov_kernels.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -51,6 +52,11 @@ struct frehg_re {
   // operator + Krylov
   Stencil64 A;
   KrylovSolver ksp;
+  // learned preconditioner
+  frehg_unet* net = nullptr;
+  float* lnk_f = nullptr;  // network input fields of the current system
+  float* cap_f = nullptr;
+  int plain_its_ref = 0;   // inner iterations of the last Jacobi solve (fallback threshold)
   // counters / profiling
   frehg_re_counters cnt;
   Profiler prof;
@@ -79,6 +85,8 @@ frehg_re::~frehg_re() {
   cudaFree(cid);
   cudaFree(fKs);
   cudaFree(falpha);
+  cudaFree(lnk_f);
+  cudaFree(cap_f);
   A.release();
   if (own_stream) cudaStreamDestroy(own_stream);
 }
@@ -270,6 +278,55 @@ __global__ void k_volume(ReArgs a, const double* __restrict__ w, double* out) {
 
 static int nblocks(size_t n) { return reduction_blocks(n, 256, 4); }
 
+namespace {
+// network input fields: ln of the vertical conductivity and the moisture capacity
+__global__ void k_net_fields(ReArgs a, float* __restrict__ lnk, float* __restrict__ cap) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const CellSoil s = soil_of(a.soil, c, c % a.ncol);
+    const double K = s.Ksz * a.kr[c];
+    lnk[c] = (float)log(K > 1e-300 ? K : 1e-300);
+    cap[c] = (float)a.cap[c];
+  }
+}
+// one training pair: r~_k and e~_k = x~* - x~_k (FP32)
+__global__ void k_pair(const double* __restrict__ xstar, const double* __restrict__ x,
+                       const double* __restrict__ r, float* __restrict__ rout,
+                       float* __restrict__ eout, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    rout[c] = (float)r[c];
+    eout[c] = (float)(xstar[c] - x[c]);
+  }
+}
+}  // namespace
+
+// Krylov solve of the assembled system with the handle's configuration; the learned
+// preconditioner (pc_type "unet") runs flexible CG inside the mixed-precision refinement,
+// after one Jacobi solve has set the fallback threshold (2x its inner iterations).
+static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
+  cudaStream_t st = re->stream;
+  frehg_solver_config cfg = re->cfg;
+  const bool learned = !strcmp(cfg.pc_type, "unet");
+  re->ksp.net = NetPrecond();
+  if (learned) {
+    cfg.precision = 1;
+    if (re->net && re->plain_its_ref > 0) {
+      ReArgs a = make_args(re);
+      k_net_fields<<<nblocks(re->n), 256, 0, st>>>(a, re->lnk_f, re->cap_f);
+      FG_CUDA(cudaGetLastError());
+      re->ksp.net.net = re->net;
+      re->ksp.net.lnk = re->lnk_f;
+      re->ksp.net.cap = re->cap_f;
+      re->ksp.net.max_inner = 2 * re->plain_its_ref;
+    }
+  }
+  const int rc = re->ksp.solve(re->A, x_out, cfg, st, res);
+  if (learned && rc == FREHG_OK && (!re->ksp.net.net || res->fallback)) re->plain_its_ref = res->its;
+  if (res->fallback) re->cnt.fcg_fallbacks += 1;
+  return rc;
+}
+
 // bytes one cell's soil lookup reads (per-cell Ks / alpha fields, class ids)
 static double soil_bytes(const frehg_re* re) {
   return (re->fKs ? 8.0 : 0.0) + (re->falpha ? 8.0 : 0.0) + (re->cid && re->cid3d ? 1.0 : 0.0);
@@ -297,7 +354,7 @@ static int pca_step(frehg_re* re) {
   FG_CUDA(cudaGetLastError());
   // LinearSolver::solve
   CgResult res;
-  const int rc = re->ksp.solve(re->A, a.h_new, re->cfg, st, &res);
+  const int rc = solve_system(re, a.h_new, &res);
   re->cnt.last_ksp_iterations = res.its;
   re->cnt.last_residual_norm = res.rnorm;
   re->cnt.ksp_iterations += res.its;
@@ -382,7 +439,7 @@ static int picard_step(frehg_re* re) {
                                                    re->A.b));
       FG_CUDA(cudaGetLastError());
       CgResult res;
-      const int rc = re->ksp.solve(re->A, re->scratch, re->cfg, st, &res);
+      const int rc = solve_system(re, re->scratch, &res);
       re->cnt.last_ksp_iterations = res.its;
       re->cnt.last_residual_norm = res.rnorm;
       re->cnt.ksp_iterations += res.its;
@@ -618,8 +675,8 @@ int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg) {
     set_error("ksp_type '%s' is not available (cg, fcg)", cfg->ksp_type);
     return FREHG_ERR_UNSUPPORTED;
   }
-  if (strcmp(cfg->pc_type, "jacobi") != 0) {
-    set_error("pc_type '%s' is not available on the GPU path (jacobi)", cfg->pc_type);
+  if (strcmp(cfg->pc_type, "jacobi") != 0 && strcmp(cfg->pc_type, "unet") != 0) {
+    set_error("pc_type '%s' is not available on the GPU path (jacobi, unet)", cfg->pc_type);
     return FREHG_ERR_UNSUPPORTED;
   }
   FG_ARG(cfg->rtol > 0 && cfg->max_it > 0, "rtol and max_it must be positive");
@@ -888,6 +945,87 @@ int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c) {
   c->kernel_launches = re->prof.launches;
   FG_TRY(read_scalars(re));
   c->elastic_volume = re->sc_host->vol_elastic;
+  return FREHG_OK;
+}
+
+int frehg_re_attach_unet(frehg_re* re, frehg_unet* net) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_ARG(re->nx % 4 == 0 && re->ny % 4 == 0 && re->nz % 4 == 0,
+         "the learned preconditioner needs nx, ny, nz divisible by 4");
+  re->net = net;
+  if (net && !re->lnk_f) {
+    FG_CUDA(cudaMalloc(&re->lnk_f, re->n * sizeof(float)));
+    FG_CUDA(cudaMalloc(&re->cap_f, re->n * sizeof(float)));
+  }
+  re->plain_its_ref = 0;
+  return FREHG_OK;
+}
+
+int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, float* r_out,
+                            float* e_out, float* lnk_out, float* cap_out) {
+  clear_error();
+  FG_ARG(re && iters && r_out && e_out && lnk_out && cap_out && npairs > 0, "bad argument");
+  FG_ARG(re->finalized && re->attached, "training pairs need an initialised, attached solver");
+  FG_ARG(re->p.scheme == 0, "training pairs are drawn from the PCA head solve");
+  int kmax = 0;
+  for (int q = 0; q < npairs; ++q) {
+    FG_ARG(iters[q] >= 0 && (q == 0 || iters[q] > iters[q - 1]),
+           "iteration numbers must be increasing");
+    kmax = iters[q];
+  }
+  cudaStream_t st = re->stream;
+  ReArgs a = make_args(re);
+  const int nb = nblocks(re->n);
+  const size_t n = re->n;
+  // the next step's system at the current state (nothing advances)
+  k_step_begin<<<1, 1, 0, st>>>(re->sc);
+  k_constit<false, true><<<nb, 256, 0, st>>>(a, a.h_old, re->kr, nullptr, re->cap);
+  const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
+  re->A.scaled = false;
+  k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b,
+                                         L.planes, L.tiles);
+  k_net_fields<<<nb, 256, 0, st>>>(a, lnk_out, cap_out);
+  FG_CUDA(cudaGetLastError());
+  // x~* of the scaled system, FP64 Jacobi-PCG to the handle's rtol
+  frehg_solver_config cfg = re->cfg;
+  cfg.precision = 0;
+  CgResult res;
+  KrylovSolver& K = re->ksp;
+  K.net = NetPrecond();
+  FG_TRY(K.solve(re->A, re->scratch, cfg, st, &res));
+  double* xstar = nullptr;
+  FG_CUDA(cudaMalloc(&xstar, n * sizeof(double)));
+  FG_CUDA(cudaMemcpyAsync(xstar, K.x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  // rerun the iteration and record (r~_k, x~* - x~_k)
+  CgDevState init;
+  memset(&init, 0, sizeof(init));
+  init.rtol = 0.0;
+  init.atol = 0.0;
+  init.divtol = 0.0;
+  init.max_it = kmax + 1;
+  FG_CUDA(cudaMemcpyAsync(K.dst, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+  const int nbk = reduction_blocks(n, 256, 4);
+  k_cg_init<<<nbk, 256, 0, st>>>(re->A.s, re->A.b, K.x, K.r, n, K.dst, K.partials);
+  int q = 0;
+  for (int it = 0; it <= kmax && q < npairs; ++it) {
+    if (it == iters[q]) {
+      k_pair<<<nb, 256, 0, st>>>(xstar, K.x, K.r, r_out + (size_t)q * n, e_out + (size_t)q * n, n);
+      ++q;
+    }
+    if (it == kmax) break;
+    k_cg_p<<<nbk, 256, 0, st>>>(K.r, K.p, n, K.dst);
+    k_cg_spmv<<<L.grid, L.block, 0, st>>>(re->A.a0, re->A.a1, re->A.a2, K.p, K.w, re->nx, re->ny,
+                                          re->nz, L.planes, L.tiles, K.dst, K.partials);
+    k_cg_update<<<nbk, 256, 0, st>>>(K.x, K.r, K.p, K.w, re->A.s, n, K.dst, K.partials);
+  }
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaStreamSynchronize(st));
+  cudaFree(xstar);
+  if (q < npairs) {
+    set_error("training pairs: the iteration stopped before iteration %d", iters[q]);
+    return FREHG_ERR_STATE;
+  }
   return FREHG_OK;
 }
 

@@ -188,6 +188,7 @@ typedef struct frehg_re_counters {
   double last_residual_norm;
   int64_t kernel_launches;   /* kernels this handle launched (graph nodes included)      */
   int64_t ir_sweeps;         /* mixed precision: FP64 refinement sweeps (not in reference)  */
+  int64_t fcg_fallbacks;     /* learned preconditioner dropped for Jacobi (not in reference) */
   double elastic_volume;     /* Picard: cumulative specific-storage volume [m^3]            */
 } frehg_re_counters;
 int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c);
@@ -284,6 +285,19 @@ int frehg_unet_adam_step(frehg_unet* net, float lr, float beta1, float beta2, fl
                          void* stream);
 /* floating-point operations of one forward application on an nx*ny*nz grid */
 int frehg_unet_flops(int nx, int ny, int nz, double* flops);
+
+/* Attach a network to an RE handle: with pc_type "unet" the head solves run flexible CG
+ * preconditioned by it inside the FP64 refinement loop (FP32 Krylov).  The first solve after
+ * attaching runs Jacobi CG and sets the fallback threshold: a solve whose FCG iterations
+ * exceed twice that count continues with Jacobi CG.  net = NULL detaches. */
+int frehg_re_attach_unet(frehg_re* re, frehg_unet* net);
+/* Training pairs from the plain solver: assembles the next PCA step's system at the current
+ * state (nothing advances), solves it with FP64 Jacobi-PCG, re-runs the iteration from zero and
+ * at each iteration number iters[q] (increasing) stores the scaled residual r~ and error
+ * x~* - x~ as FP32 into r_out + q*n, e_out + q*n; ln K (vertical) and C into lnk_out, cap_out.
+ * Device pointers, n = nx*ny*nz. */
+int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, float* r_out,
+                            float* e_out, float* lnk_out, float* cap_out);
 
 /* Allocation-free CG solve.  No counterpart in the reference: it exists for callers that may
  * not allocate GPU memory themselves (a component under a host framework that owns the device
