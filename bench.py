@@ -40,6 +40,8 @@ def parse():
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
     ap.add_argument("--scheme", default="pca", choices=["pca", "picard"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--pc", default="jacobi", choices=["jacobi", "line"],
+                    help="inner preconditioner of the mixed solve")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-window", type=int, default=128,
                     help="columns per side of the CPU sample window")
@@ -64,6 +66,10 @@ def workload(args, nx=None, ny=None):
     else:
         kw = {} if nx is None else dict(nx=nx, ny=ny)
         w = W.config1(args.scheme, precision=prec, **kw)
+    if args.pc != "jacobi":
+        if prec != 1:
+            raise SystemExit("--pc line needs --precision mixed")
+        w.solver.pc_type = args.pc.encode()
     return w
 
 

@@ -191,6 +191,11 @@ class KrylovSolver {
   Profiler* prof = nullptr;  // owner's profiler (launch counts, optional event timing)
   NetPrecond net;            // learned preconditioner (FCG inner solves when set)
   float* zf = nullptr;
+  // vertical-line preconditioner (FP32 factors and sweep scratch)
+  int ensure_line(size_t n);
+  size_t cap_line = 0;
+  float *lkf = nullptr, *dinvf = nullptr, *uf = nullptr;
+  int g32_line = 0;
   const void* g32_key = nullptr;
   cudaStream_t g_stream = nullptr;
   size_t g_n = 0;

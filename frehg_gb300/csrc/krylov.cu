@@ -370,6 +370,9 @@ KrylovSolver::~KrylovSolver() {
   cudaFree(dst32);
   cudaFreeHost(hst32);
   cudaFree(zf);
+  cudaFree(lkf);
+  cudaFree(dinvf);
+  cudaFree(uf);
   op32.release();
 }
 
@@ -432,6 +435,10 @@ int KrylovSolver::solve(Stencil64& A, double* x_out, const frehg_solver_config& 
   FG_TRY(ensure(A.n));
   FG_TRY(scale(A, st));
   if (cfg.precision == 1) return solve_mixed(A, x_out, cfg, st, res);
+  if (strcmp(cfg.pc_type, "jacobi") != 0) {
+    set_error("pc_type '%s' needs the mixed-precision solve (precision 1)", cfg.pc_type);
+    return FREHG_ERR_UNSUPPORTED;
+  }
   return solve64(A, x_out, cfg, st, res);
 }
 

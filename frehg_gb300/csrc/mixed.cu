@@ -13,6 +13,7 @@
 // residual, so the inner precision changes the iteration count, not the accuracy.
 #include "internal.h"
 #include "krylov_kernels.cuh"
+#include "line.cuh"
 #include "reduce.cuh"
 
 #include <cmath>
@@ -21,18 +22,6 @@
 #include <cstring>
 
 namespace fg {
-
-// per-thread compensated FP32 sum (Kahan)
-struct Kahan32 {
-  float s = 0.0f, c = 0.0f;
-  __device__ __forceinline__ void add(float x) {
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
 
 // r~ = s b - A~ x~ (FP64, kept in rres); e = 0; sums of r~^2 (scale of the inner system),
 // (r~/s)^2 for the true residual and b^2 for ||b||.  The last block runs the refinement test.
@@ -487,6 +476,19 @@ int KrylovSolver::ensure32(size_t n) {
   return FREHG_OK;
 }
 
+int KrylovSolver::ensure_line(size_t n) {
+  if (lkf && n <= cap_line) return FREHG_OK;
+  cudaFree(lkf);
+  cudaFree(dinvf);
+  cudaFree(uf);
+  lkf = dinvf = uf = nullptr;
+  FG_CUDA(cudaMalloc(&lkf, n * sizeof(float)));
+  FG_CUDA(cudaMalloc(&dinvf, n * sizeof(float)));
+  FG_CUDA(cudaMalloc(&uf, n * sizeof(float)));
+  cap_line = n;
+  return FREHG_OK;
+}
+
 int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_config& cfg,
                               cudaStream_t st, CgResult* res) {
   const size_t n = A.n;
@@ -500,6 +502,16 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
             k_to_f32<<<nb, 256, 0, st>>>(A.a0, A.a1, A.a2, op32.a0, op32.a1, op32.a2, n));
   FG_LAUNCH(prof, st, "k_zero64", 8.0 * dn, k_zero64<<<nb, 256, 0, st>>>(x, n));
   FG_CUDA(cudaGetLastError());
+  // inner preconditioner: Jacobi (unit diagonal, z = r) or vertical lines
+  const bool line = !strcmp(cfg.pc_type, "line");
+  const int ncol = A.n0 * A.n1, nzl = A.n2;
+  const int lb = (int)std::min<long>((ncol + 127) / 128, kMaxRedBlocks);
+  if (line) {
+    FG_TRY(ensure_line(n));
+    FG_LAUNCH(prof, st, "k_line_factor", 16.0 * dn,
+              k_line_factor<<<lb, 128, 0, st>>>(A.a2, lkf, dinvf, ncol, nzl));
+    FG_CUDA(cudaGetLastError());
+  }
   CgDevState ir0, in0;
   memset(&ir0, 0, sizeof(ir0));
   memset(&in0, 0, sizeof(in0));
@@ -509,8 +521,17 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
 
   const int chunk = 32;
+  const long shape_key = (long)A.n0 * 1000003L + A.n1;
   const bool rebuild = !g32 || g32_key != (const void*)op32.a0 || g_stream32 != st || g_n32 != n ||
-                       g32_shape != (long)A.n0 * 1000003L + A.n1;
+                       g32_shape != shape_key || g32_line != (line ? 1 : 0);
+  auto spmv32 = [&](cudaStream_t s) {
+    if (vec4)
+      k32_spmv_v4<<<L4.grid, L4.block, 0, s>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1,
+                                                A.n2, L4.planes, L4.tiles, dst32, partials);
+    else
+      k32_spmv<<<L.grid, L.block, 0, s>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1, A.n2,
+                                          L.planes, L.tiles, dst32, partials);
+  };
   if (!(prof && prof->on) && rebuild) {
     if (g32) cudaGraphExecDestroy(g32);
     g32 = nullptr;
@@ -519,15 +540,16 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     cudaGraph_t graph;
     FG_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
     for (int q = 0; q < chunk; ++q) {
-      k32_p<<<nb, 256, 0, cap_st>>>(rf, pf, n, dst32);
-      if (vec4)
-        k32_spmv_v4<<<L4.grid, L4.block, 0, cap_st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0,
-                                                       A.n1, A.n2, L4.planes, L4.tiles, dst32,
-                                                       partials);
-      else
-        k32_spmv<<<L.grid, L.block, 0, cap_st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1,
-                                                 A.n2, L.planes, L.tiles, dst32, partials);
-      k32_update<<<nb, 256, 0, cap_st>>>(xf, rf, pf, wf, n, dst32, partials);
+      if (line) {
+        spmv32(cap_st);
+        k32_line_fwd<true><<<lb, 128, 0, cap_st>>>(xf, rf, pf, wf, lkf, dinvf, uf, ncol, nzl,
+                                                   dst32, partials);
+        k32_line_bwd<<<lb, 128, 0, cap_st>>>(uf, lkf, pf, ncol, nzl, dst32);
+      } else {
+        k32_p<<<nb, 256, 0, cap_st>>>(rf, pf, n, dst32);
+        spmv32(cap_st);
+        k32_update<<<nb, 256, 0, cap_st>>>(xf, rf, pf, wf, n, dst32, partials);
+      }
     }
     cudaError_t e = cudaStreamEndCapture(cap_st, &graph);
     cudaStreamDestroy(cap_st);
@@ -544,7 +566,8 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     g32_key = op32.a0;
     g_stream32 = st;
     g_n32 = n;
-    g32_shape = (long)A.n0 * 1000003L + A.n1;
+    g32_shape = shape_key;
+    g32_line = line ? 1 : 0;
   }
 
   const int max_sweeps = 60;
@@ -575,21 +598,16 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       const int check = 4;
       for (int it = 0; it < cfg.max_it && hst32->status == 0; ++it) {
         FG_TRY(unet_apply(net.net, A.n0, A.n1, A.n2, rf, net.lnk, net.cap, zf, st));
-        FG_LAUNCH(prof, st, "k_add_f32", 12.0 * dn, k_add_f32<<<nb, 256, 0, st>>>(zf, rf, n));
+        if (line)
+          FG_LAUNCH(prof, st, "k32_line_apply", 32.0 * dn,
+                    k32_line_apply<<<lb, 128, 0, st>>>(rf, lkf, dinvf, uf, zf, ncol, nzl, 1));
+        else
+          FG_LAUNCH(prof, st, "k_add_f32", 12.0 * dn, k_add_f32<<<nb, 256, 0, st>>>(zf, rf, n));
         FG_LAUNCH(prof, st, "k_fcg_beta", 8.0 * dn,
                   k_fcg_beta<<<nb, 256, 0, st>>>(zf, wf, n, dst32, partials));
         FG_LAUNCH(prof, st, "k_fcg_p", 16.0 * dn,
                   k_fcg_p<<<nb, 256, 0, st>>>(zf, pf, rf, n, dst32, partials));
-        if (vec4)
-          FG_LAUNCH(prof, st, "k32_spmv_v4", 20.0 * dn,
-                    k32_spmv_v4<<<L4.grid, L4.block, 0, st>>>(op32.a0, op32.a1, op32.a2, pf, wf,
-                                                              A.n0, A.n1, A.n2, L4.planes,
-                                                              L4.tiles, dst32, partials));
-        else
-          FG_LAUNCH(prof, st, "k32_spmv", 20.0 * dn,
-                    k32_spmv<<<L.grid, L.block, 0, st>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0,
-                                                         A.n1, A.n2, L.planes, L.tiles, dst32,
-                                                         partials));
+        FG_LAUNCH(prof, st, vec4 ? "k32_spmv_v4" : "k32_spmv", 20.0 * dn, spmv32(st));
         FG_LAUNCH(prof, st, "k32_update", 24.0 * dn,
                   k32_update<<<nb, 256, 0, st>>>(xf, rf, pf, wf, n, dst32, partials));
         FG_CUDA(cudaGetLastError());
@@ -607,22 +625,32 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       FG_CUDA(cudaStreamSynchronize(st));
       if (prof && prof->on) FG_TRY(prof->flush());
     }
+    if (!use_net && line) {
+      // z0 = M^-1 r0, r0.z0 and p0 = z0
+      FG_LAUNCH(prof, st, "k32_line_fwd0", 16.0 * dn,
+                (k32_line_fwd<false><<<lb, 128, 0, st>>>(xf, rf, pf, wf, lkf, dinvf, uf, ncol,
+                                                         nzl, dst32, partials)));
+      FG_LAUNCH(prof, st, "k32_line_bwd", 12.0 * dn,
+                k32_line_bwd<<<lb, 128, 0, st>>>(uf, lkf, pf, ncol, nzl, dst32));
+      FG_CUDA(cudaGetLastError());
+    }
     for (int q = 0; !use_net && q < cfg.max_it / chunk + 2 && hst32->status == 0; ++q) {
       if (prof && prof->on) {
         for (int it = 0; it < chunk; ++it) {
-          FG_LAUNCH(prof, st, "k32_p", 12.0 * dn, k32_p<<<nb, 256, 0, st>>>(rf, pf, n, dst32));
-          if (vec4)
-            FG_LAUNCH(prof, st, "k32_spmv_v4", 20.0 * dn,
-                      k32_spmv_v4<<<L4.grid, L4.block, 0, st>>>(
-                          op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1, A.n2, L4.planes,
-                          L4.tiles, dst32, partials));
-          else
-            FG_LAUNCH(prof, st, "k32_spmv", 20.0 * dn,
-                      k32_spmv<<<L.grid, L.block, 0, st>>>(op32.a0, op32.a1, op32.a2, pf, wf,
-                                                           A.n0, A.n1, A.n2, L.planes, L.tiles,
-                                                           dst32, partials));
-          FG_LAUNCH(prof, st, "k32_update", 24.0 * dn,
-                    k32_update<<<nb, 256, 0, st>>>(xf, rf, pf, wf, n, dst32, partials));
+          if (line) {
+            FG_LAUNCH(prof, st, vec4 ? "k32_spmv_v4" : "k32_spmv", 20.0 * dn, spmv32(st));
+            FG_LAUNCH(prof, st, "k32_line_fwd", 36.0 * dn,
+                      (k32_line_fwd<true><<<lb, 128, 0, st>>>(xf, rf, pf, wf, lkf, dinvf, uf,
+                                                              ncol, nzl, dst32, partials)));
+            FG_LAUNCH(prof, st, "k32_line_bwd", 16.0 * dn,
+                      k32_line_bwd<<<lb, 128, 0, st>>>(uf, lkf, pf, ncol, nzl, dst32));
+          } else {
+            FG_LAUNCH(prof, st, "k32_p", 12.0 * dn,
+                      k32_p<<<nb, 256, 0, st>>>(rf, pf, n, dst32));
+            FG_LAUNCH(prof, st, vec4 ? "k32_spmv_v4" : "k32_spmv", 20.0 * dn, spmv32(st));
+            FG_LAUNCH(prof, st, "k32_update", 24.0 * dn,
+                      k32_update<<<nb, 256, 0, st>>>(xf, rf, pf, wf, n, dst32, partials));
+          }
         }
         FG_CUDA(cudaGetLastError());
       } else {

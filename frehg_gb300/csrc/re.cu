@@ -301,16 +301,20 @@ __global__ void k_pair(const double* __restrict__ xstar, const double* __restric
 }
 }  // namespace
 
-// Krylov solve of the assembled system with the handle's configuration; the learned
-// preconditioner (pc_type "unet") runs flexible CG inside the mixed-precision refinement,
-// after one Jacobi solve has set the fallback threshold (2x its inner iterations).
+// Krylov solve of the assembled system with the handle's configuration.  The learned
+// preconditioners run flexible CG inside the mixed-precision refinement with
+// z = M(r) + NN(r, ln K, C): M = I for pc_type "unet" (unit-diagonal Jacobi step, Jacobi-PCG
+// fallback), M = the vertical-line solve for "unet-line" (line-PCG fallback).  The first solve
+// runs the fallback method and sets the threshold (2x its inner iterations) beyond which a
+// solve switches to it.
 static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
   cudaStream_t st = re->stream;
   frehg_solver_config cfg = re->cfg;
-  const bool learned = !strcmp(cfg.pc_type, "unet");
+  const bool learned = !strncmp(cfg.pc_type, "unet", 4);
   re->ksp.net = NetPrecond();
   if (learned) {
     cfg.precision = 1;
+    strcpy(cfg.pc_type, strcmp(re->cfg.pc_type, "unet-line") ? "jacobi" : "line");
     if (re->net && re->plain_its_ref > 0) {
       ReArgs a = make_args(re);
       k_net_fields<<<nblocks(re->n), 256, 0, st>>>(a, re->lnk_f, re->cap_f);
@@ -675,12 +679,20 @@ int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg) {
     set_error("ksp_type '%s' is not available (cg, fcg)", cfg->ksp_type);
     return FREHG_ERR_UNSUPPORTED;
   }
-  if (strcmp(cfg->pc_type, "jacobi") != 0 && strcmp(cfg->pc_type, "unet") != 0) {
-    set_error("pc_type '%s' is not available on the GPU path (jacobi, unet)", cfg->pc_type);
+  const char* pcs[] = {"jacobi", "line", "unet", "unet-line"};
+  bool known = false;
+  for (const char* q : pcs) known = known || !strcmp(cfg->pc_type, q);
+  if (!known) {
+    set_error("pc_type '%s' is not available on the GPU path (jacobi, line, unet, unet-line)",
+              cfg->pc_type);
     return FREHG_ERR_UNSUPPORTED;
   }
   FG_ARG(cfg->rtol > 0 && cfg->max_it > 0, "rtol and max_it must be positive");
   FG_ARG(cfg->precision == 0 || cfg->precision == 1, "precision must be 0 or 1");
+  if (!strcmp(cfg->pc_type, "line") && cfg->precision != 1) {
+    set_error("pc_type 'line' runs in the FP32 inner solve: it needs precision 1 (mixed)");
+    return FREHG_ERR_UNSUPPORTED;
+  }
   re->cfg = *cfg;
   re->attached = true;
   return FREHG_OK;

@@ -51,3 +51,35 @@ def test_mixed_seam_true_residual(gpu_lib):
             if p:
                 ax[r] += coef[r, q] * x[r + o]
     assert np.linalg.norm(b - ax) <= 1.5e-11 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("shape", [(32, 24, 32), (30, 14, 27)])
+@pytest.mark.parametrize("scheme", ["pca", "picard"])
+def test_line_preconditioner(gpu_lib, scheme, shape):
+    """Vertical-line PCG inside the refinement: same heads as FP64 Jacobi-PCG (1e-8 m) with
+    fewer inner iterations.  (30, 14, 27): axis 0 not a multiple of 4 (scalar SpMV) and a
+    column length that is not a multiple of the sweep's load batch."""
+    nx, ny, nz = shape
+    w64 = W.config1(scheme, nx=nx, ny=ny, nz=nz, steps=6)
+    wj = W.config1(scheme, nx=nx, ny=ny, nz=nz, steps=6, precision=1)
+    wl = W.config1(scheme, nx=nx, ny=ny, nz=nz, steps=6, precision=1)
+    for w in (wj, wl):
+        w.solver.ir_rtol = 1e-12
+    wl.solver.pc_type = b"line"
+    a, j, l = make(w64), make(wj), make(wl)
+    for s in range(w64.steps):
+        for g in (a, j, l):
+            g.advance_step()
+        dh = np.abs(a.interior("h") - l.interior("h")).max()
+        assert dh <= 1e-8, f"step {s}: line-PCG vs fp64 head error {dh:.3e}"
+    its_j, its_l = j.counters().ksp_iterations, l.counters().ksp_iterations
+    print(f"\n  {scheme} {shape}: inner iterations jacobi {its_j}  line {its_l}")
+    assert its_l < its_j
+
+
+def test_line_needs_mixed(gpu_lib):
+    from frehg_gb300.abi import FrehgError
+    w = W.config1("pca", nx=8, ny=8, nz=8, steps=1)
+    w.solver.pc_type = b"line"
+    with pytest.raises(FrehgError, match="precision"):
+        make(w)
