@@ -1,13 +1,20 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 Richards-equation step: cells*steps/s.
 
-Default workload: the 256x256x128 heterogeneous infiltration (ln Ks GRF sigma 1, correlated
-ln alpha, hydrostatic start, 20 mm/h rain, bottom head fixed, dt 60 s), plain FP64 with CG +
-Jacobi at rtol 1e-12, run with the reference's PCA step.  A "step" is one Richards time step
-over the whole grid.  Inputs are seeded and synthetic; the working set (~1 GB) is larger than
-L2, so no flush is needed between steps.
+Default workload: the combined configuration, 768x768x96 cells (56.6M) of three-layer soil
+(sand / loam / clay at seeded interface depths, in-layer ln Ks GRF sigma 1.5), dry start
+h = -5 m, 50 mm/h rain for 1800 s then none, free-drainage bottom, mixed-form modified Picard
+(|dh|_inf < 1e-6 m) with a Picard-count time step in [10, 120] s.  A "step" is one time step
+over the whole grid, all its Picard iterations included.  The timed arm is the learned +
+mixed-precision solver (FP32 flexible CG with z = M_line^-1 r + NN(r) inside FP64 iterative
+refinement to a true relative residual of 1e-12, network time policy and iteration fallback);
+the same steps are then run with the plain FP64 Jacobi-PCG path (rtol 1e-12) for the
+comparison and the head error between the two.  Inputs are seeded and synthetic; the working
+set (> 10 GB) is far larger than L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--config c0..c4] [--scheme pca|picard] [--precision fp64|mixed]
+                    [--pc jacobi|line|unet|unet-line]
 
 --impl reference times the CPU restatement of the reference path (oracle/, OpenMP on every
 host core) on a bounded window of the same workload; under torchrun only rank 0 runs it.
@@ -15,6 +22,7 @@ host core) on a bounded window of the same workload; under torchrun only rank 0 
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import math
 import os
@@ -30,53 +38,87 @@ sys.path.insert(0, ROOT)
 METRIC = "Richards cells·steps/s at 1e-8 m head error: learned+mixed vs plain FP64 PCG"
 UNIT = "cells·steps/s"
 
+# per-configuration defaults: scheme, precision, inner preconditioner, timed steps,
+# oracle window (columns per side) for the CPU legs
+DEFAULTS = {
+    "c0": dict(scheme="picard", precision="fp64", pc="jacobi", steps=120, window=40),
+    "c1": dict(scheme="picard", precision="fp64", pc="jacobi", steps=20, window=64),
+    "c2": dict(scheme="picard", precision="mixed", pc="jacobi", steps=10, window=64),
+    "c3": dict(scheme="picard", precision="mixed", pc="unet-line", steps=10, window=64),
+    "c4": dict(scheme="picard", precision="mixed", pc="unet-line", steps=20, window=64),
+}
+
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
-    ap.add_argument("--scheme", default="pca", choices=["pca", "picard"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--pc", default="jacobi", choices=["jacobi", "line"],
-                    help="inner preconditioner of the mixed solve")
+    ap.add_argument("--config", default="c4", choices=sorted(DEFAULTS))
+    ap.add_argument("--scheme", default=None, choices=["pca", "picard"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
+    ap.add_argument("--pc", default=None, choices=["jacobi", "line", "unet", "unet-line"])
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the plain FP64 arm (comparison and head error)")
+    ap.add_argument("--unet-weights", default=None, help="trained network (.npz, learned.py)")
+    ap.add_argument("--train-steps", type=int, default=300)
+    ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--ref-window", type=int, default=128,
-                    help="columns per side of the CPU sample window")
+    ap.add_argument("--ref-window", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-steps", type=int, default=2)
+    ap.add_argument("--profile-steps", type=int, default=1)
     ap.add_argument("--nx", type=int, default=None, help="window of the workload (smaller case)")
     ap.add_argument("--ny", type=int, default=None)
-    return ap.parse_args()
+    a = ap.parse_args()
+    d = DEFAULTS[a.config]
+    a.scheme = a.scheme or d["scheme"]
+    a.precision = a.precision or d["precision"]
+    a.pc = a.pc or (d["pc"] if a.precision == "mixed" else "jacobi")
+    a.steps = a.steps or d["steps"]
+    a.ref_window = a.ref_window or d["window"]
+    if a.pc != "jacobi" and a.precision != "mixed":
+        ap.error(f"--pc {a.pc} runs in the mixed-precision solve (--precision mixed)")
+    return a
 
 
-def workload(args, nx=None, ny=None):
+def workload(args, nx=None, ny=None, precision=None, pc=None):
+    """The configuration's workload (optionally a window of nx x ny columns) with the solver
+    selected by precision / pc (default: the command line's)."""
     from frehg_gb300 import workloads as W
-    prec = 1 if args.precision == "mixed" else 0
+    prec = 1 if (precision or args.precision) == "mixed" else 0
+    pc = pc or args.pc
     if nx is None and args.nx:
         nx, ny = args.nx, args.ny or args.nx
+    kw = {} if nx is None else dict(nx=nx, ny=ny)
     if args.config == "c0":
-        kw = {} if nx is None else dict(nx=nx, ny=ny)
         w = W.config0(args.scheme, **kw)
-    elif args.config == "c2":
-        kw = {} if nx is None else dict(nx=nx, ny=ny)
-        w = W.config2(args.scheme, **kw)
-    else:
-        kw = {} if nx is None else dict(nx=nx, ny=ny)
+    elif args.config == "c1":
         w = W.config1(args.scheme, precision=prec, **kw)
-    if args.pc != "jacobi":
-        if prec != 1:
-            raise SystemExit("--pc line needs --precision mixed")
-        w.solver.pc_type = args.pc.encode()
+    elif args.config == "c2":
+        w = W.config2(args.scheme, **kw)
+    elif args.config == "c3":
+        w = W.config3(args.scheme, precision=prec, pc=pc if prec else "jacobi", **kw)
+    else:
+        w = W.config4(precision=prec, pc=pc if prec else "jacobi", **kw)
+    w.solver.precision = prec
+    w.solver.pc_type = (pc if prec else "jacobi").encode()
+    if prec:
+        w.solver.ir_rtol = 1e-12
     return w
 
 
-def window(w_full, args, side):
-    """A bounded sample of the workload: the same generator on side x side columns."""
-    side = min(side, w_full.nx, w_full.ny)
-    return workload(args, nx=side, ny=side)
+FULL_COLUMNS = {"c0": 40, "c1": 256, "c2": 512, "c3": 256, "c4": 768}
+
+
+def window(args, side, **kw):
+    """A bounded sample of the workload: the same generator on side x side columns.  Returns
+    the full workload's name and the window."""
+    full = args.nx or FULL_COLUMNS[args.config]
+    fully = args.ny or full
+    side = min(side, full, fully)
+    w = workload(args, nx=side, ny=side, **kw)
+    return w.name.replace(f"{side}x{side}x", f"{full}x{fully}x", 1), w
 
 
 def dist_env():
@@ -160,12 +202,16 @@ def ncu_traffic(kernel):
     return d.get(kernel)
 
 
-def cpu_rate(args, w_full, seconds, max_steps=None):
-    """Time the oracle (CPU restatement of the reference PCA step, OpenMP on every host core) on a
+def scheme_name(args):
+    return "mixed-form Picard" if args.scheme == "picard" else "PCA (ReSolver::advanceStep)"
+
+
+def cpu_rate(args, seconds, max_steps=None):
+    """Time the oracle (FP64 CPU restatement of the step, OpenMP on every host core) on a
     bounded window of the workload; returns (cells*steps/s, threads, sample description)."""
     from oracle import oracle
     oracle.build()
-    w = window(w_full, args, args.ref_window)
+    full_name, w = window(args, args.ref_window, precision="fp64", pc="jacobi")
     o = oracle.OracleRe(w.nx, w.ny, w.nz, w.params)
     w.apply(o)
     threads = oracle.num_threads()
@@ -178,24 +224,27 @@ def cpu_rate(args, w_full, seconds, max_steps=None):
         if el >= seconds or (max_steps and steps >= max_steps):
             break
     rate = w.cells * steps / el
-    sample = (f"first {steps} PCA steps of the workload's generator on a {w.nx}x{w.ny}x{w.nz} "
-              f"window ({w.cells} cells), {el:.1f} s, {threads} OpenMP threads")
+    sample = (f"first {steps} {scheme_name(args)} steps of {full_name}'s generator on a "
+              f"{w.nx}x{w.ny}x{w.nz} window ({w.cells} cells), {el:.1f} s, {threads} OpenMP "
+              f"threads, FP64 CG+Jacobi rtol 1e-12")
     return rate, threads, sample
 
 
 def run_reference(args):
+    """The reference's CPU path: the oracle restatement, all host threads, per-step samples of
+    a bounded window of the same workload."""
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-    w_full = workload(args)
     from oracle import oracle
     oracle.build()
-    w = window(w_full, args, args.ref_window)
+    full_name, w = window(args, args.ref_window, precision="fp64", pc="jacobi")
     o = oracle.OracleRe(w.nx, w.ny, w.nz, w.params)
     w.apply(o)
     for _ in range(args.warmup):
         o.advance_step()
+    o = oracle.OracleRe(w.nx, w.ny, w.nz, w.params)
     w.apply(o)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -203,14 +252,15 @@ def run_reference(args):
     el = time.perf_counter() - t0
     value = w.cells * args.steps / el
     threads = oracle.num_threads()
-    sample = (f"{args.steps} PCA steps on a {w.nx}x{w.ny}x{w.nz} window of the workload "
-              f"({w.cells} cells), {threads} OpenMP threads, CPU restatement of ReSolver::advanceStep")
+    sample = (f"first {args.steps} {scheme_name(args)} steps of {full_name}'s generator on a "
+              f"{w.nx}x{w.ny}x{w.nz} window ({w.cells} cells), {threads} OpenMP threads, CPU "
+              f"restatement of the reference path (FP64, CG+Jacobi rtol 1e-12)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded GRF soil fields)",
-        "config": {"workload": w_full.name, "sample_window": f"{w.nx}x{w.ny}x{w.nz}",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded soil fields)",
+        "config": {"workload": full_name, "sample_window": f"{w.nx}x{w.ny}x{w.nz}",
                    "scheme": args.scheme, "precision": "fp64", "solver": "cg+jacobi rtol 1e-12"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
@@ -218,6 +268,73 @@ def run_reference(args):
     }
     print(json.dumps(line))
     return 0
+
+
+def trained_net(args):
+    """The network of the learned arm: loaded from --unet-weights, or trained here (outside the
+    timed region) on pairs from plain solves of seeded three-layer soils at 64x64x32."""
+    from frehg_gb300 import learned as Lr
+    net = Lr.UNet(0)
+    if args.unet_weights:
+        net.load(args.unet_weights)
+        return net, {"weights": os.path.basename(args.unet_weights)}
+    t0 = time.perf_counter()
+    seeds = list(range(100, 100 + args.train_seeds))
+    data = Lr.generate_pairs(seeds, 64, 64, 32, snapshots=(0, 2), iters=(0, 2, 5, 10, 20, 40),
+                             pc=args.pc)
+    t1 = time.perf_counter()
+    losses = Lr.train(net, data, steps=args.train_steps, lr=1e-3)
+    t2 = time.perf_counter()
+    k = max(1, len(losses) // 10)
+    info = {"pairs": int(data["r"].shape[0]), "pair_shape": "64x64x32", "seeds": len(seeds),
+            "adam_steps": args.train_steps, "lr": 1e-3, "pairs_s": round(t1 - t0, 2),
+            "train_s": round(t2 - t1, 2),
+            "loss_first": float(sum(losses[:k]) / k), "loss_last": float(sum(losses[-k:]) / k),
+            "note": "bounded training budget for the benchmark run"}
+    del data
+    return net, info
+
+
+def time_arm(args, w, net, stream, barrier, steps, warmup):
+    """W warm-up steps, reset, K timed steps (CUDA events on the library's stream).  Returns the
+    solver, elapsed ms and the counter deltas of the timed steps."""
+    import torch
+    from frehg_gb300.abi import check
+    from frehg_gb300.re_solver import Grid, ReSolver
+    s = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
+    s.set_stream(stream.cuda_stream)
+
+    def reset():
+        s.set_params(w.params)
+        w.apply(s)
+        if net is not None:
+            check(s._lib.frehg_re_attach_unet(s._h, net.handle), "attach_unet")
+
+    reset()
+    for _ in range(warmup):
+        s.advance_step()
+    reset()
+    c0 = s.counters()
+    v0 = s.water_volume()
+    top0, bot0 = s.boundary_volumes()
+    el0 = s.elastic_volume()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        s.advance_step()
+    e1.record(stream)
+    stream.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    c1 = s.counters()
+    d = {f: getattr(c1, f) - getattr(c0, f) for f in
+         ("ksp_iterations", "picard_iterations", "kernel_launches", "ir_sweeps", "fcg_fallbacks",
+          "net_solves", "net_skipped", "net_ms", "plain_ms")}
+    top, bot = s.boundary_volumes()
+    mass = (s.water_volume() - v0) + (s.elastic_volume() - el0) - ((top - top0) + (bot - bot0))
+    d["mass_error_rel"] = abs(mass) / v0
+    return s, ms, d, reset
 
 
 def run_gpu(args):
@@ -237,24 +354,20 @@ def run_gpu(args):
             pg.barrier()
         torch.cuda.synchronize()
 
+    def max_over_ranks(v):
+        if not pg:
+            return v
+        t = torch.tensor([v], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
     from frehg_gb300 import build as B
     B.build()
-    from frehg_gb300.re_solver import Grid, ReSolver
 
+    learned = args.pc.startswith("unet")
+    net, net_info = trained_net(args) if learned else (None, None)
     w = workload(args)
-    s = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
     stream = torch.cuda.Stream()
-    s.set_stream(stream.cuda_stream)
-
-    def reset():
-        s.set_params(w.params)
-        w.apply(s)
-
-    reset()
-    for _ in range(args.warmup):
-        s.advance_step()
-    reset()
-    c0 = s.counters()
     bus = None
     try:
         bus = torch.cuda.get_device_properties(local).pci_bus_id
@@ -262,33 +375,21 @@ def run_gpu(args):
         pass
     clocks = Clocks(bus)
     clocks.start()
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        s.advance_step()
-    e1.record(stream)
-    stream.synchronize()
-    barrier()
-    ms = e0.elapsed_time(e1)
+    s, ms, cnt, reset = time_arm(args, w, net, stream, barrier, args.steps, args.warmup)
     clk = clocks.stop()
-    c1 = s.counters()
-    ms_max = ms
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = max_over_ranks(ms)
     value = w.cells * args.steps * world / (ms_max / 1000.0)
-    ksp_its = c1.ksp_iterations - c0.ksp_iterations
-    launches = c1.kernel_launches - c0.kernel_launches
+    h_fast = s.interior("h").copy()
 
-    # end to end through the public API: per step H2D of the top-flux forcing from pinned host
-    # memory, the step, D2H of the head and water-content fields into pinned host memory
+    # end to end through the public API: per step H2D of the top forcing (rain or qtop per
+    # column) from pinned host memory, the step, D2H of the head and water-content fields
     reset()
-    q_host = torch.full((w.ny * w.nx,), float(w.params.qtop), dtype=torch.float64).pin_memory()
+    qv = w.params.rain_rate if w.params.rain_rate != 0.0 else w.params.qtop
+    q_host = torch.full((w.ny * w.nx,), float(qv), dtype=torch.float64).pin_memory()
     h_host = torch.empty((w.nz, w.ny, w.nx), dtype=torch.float64).pin_memory()
     wc_host = torch.empty((w.nz, w.ny, w.nx), dtype=torch.float64).pin_memory()
     qn, hn, wn = q_host.numpy(), h_host.numpy(), wc_host.numpy()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     t0 = time.perf_counter()
     e0.record(stream)
@@ -300,12 +401,7 @@ def run_gpu(args):
     e1.record(stream)
     stream.synchronize()
     barrier()
-    e2e_wall = time.perf_counter() - t0
-    e2e_ms = max(e0.elapsed_time(e1), 1000.0 * e2e_wall)
-    if pg:
-        t = torch.tensor([e2e_ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0)))
     e2e_value = w.cells * args.steps * world / (e2e_ms / 1000.0)
 
     # per-kernel durations from CUDA events on the launching stream (profiling pass)
@@ -316,6 +412,7 @@ def run_gpu(args):
     stats = s.kernel_stats() if args.profile_steps > 0 else [
         {"name": "none", "launches": 1, "total_ms": 1.0, "bytes_per_launch": 0.0}]
     s.set_profiling(0)
+    del s
     tot = sum(st["total_ms"] for st in stats) or 1.0
     dom = max(stats, key=lambda st: st["total_ms"])
     per_launch_ms = dom["total_ms"] / dom["launches"]
@@ -332,33 +429,71 @@ def run_gpu(args):
                                  "share": round(st["total_ms"] / tot, 4),
                                  "GBps": round(st["bytes_per_launch"] * st["launches"] /
                                                (st["total_ms"] / 1000.0) / 1e9, 1)
-                                 if st["total_ms"] > 0 else None}
+                                 if st["total_ms"] > 0 else 0.0}
                     for st in stats},
     }
+
+    # the plain FP64 GPU path on the same inputs and steps: throughput and head error
+    comparison = None
+    if not args.no_compare and (args.precision != "fp64" or args.pc != "jacobi"):
+        torch.cuda.empty_cache()
+        from frehg_gb300.abi import SolverConfig
+        w64 = dataclasses.replace(w, solver=SolverConfig("cg", "jacobi", rtol=w.solver.rtol,
+                                                          max_it=w.solver.max_it))
+        s64, ms64, cnt64, _ = time_arm(args, w64, None, stream, barrier, args.steps, 0)
+        ms64 = max_over_ranks(ms64)
+        h64 = s64.interior("h")
+        del s64
+        dh = np.abs(h_fast - h64)
+        v64 = w.cells * args.steps * world / (ms64 / 1000.0)
+        comparison = {
+            "plain_fp64": {"value": v64, "ms_per_step": ms64 / args.steps,
+                           "cg_iterations": cnt64["ksp_iterations"],
+                           "picard_iterations": cnt64["picard_iterations"],
+                           "mass_error_rel": cnt64["mass_error_rel"]},
+            "speedup": value / v64,
+            "head_error_vs_plain_fp64_m": {"max": float(dh.max()),
+                                           "l2_rms": float(np.sqrt(np.mean(dh * dh))),
+                                           "after_steps": args.steps},
+        }
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        del s
         torch.cuda.empty_cache()
-        rate, threads, sample = cpu_rate(args, w, args.cpu_seconds)
+        rate, threads, sample = cpu_rate(args, args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    solver = (f"cg+jacobi rtol 1e-12 (fp64)" if args.precision == "fp64" else
+              f"fp32 {'fcg' if learned else 'pcg'} + {args.pc} under fp64 refinement to "
+              f"true relative residual 1e-12")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded GRF soil fields, hydrostatic start)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64+f32" + ("+bf16" if learned else ""),
+        "data": "synthetic (seeded soil fields)",
         "config": {"workload": w.name, "cells": w.cells, "scheme": args.scheme,
-                   "precision": args.precision, "solver": "cg+jacobi rtol 1e-12",
+                   "precision": args.precision, "pc": args.pc, "solver": solver,
                    "parallelism": f"replicas x{world}",
-                   "l2": "working set ~1 GB > 129 MB L2 (no flush needed)",
-                   "cg_iterations": ksp_its, "cg_iterations_per_step": ksp_its / args.steps},
+                   "l2": "working set > 1 GB, larger than the 129 MB L2 (no flush needed)",
+                   "picard_iterations": cnt["picard_iterations"],
+                   "cg_iterations": cnt["ksp_iterations"], "ir_sweeps": cnt["ir_sweeps"],
+                   "mass_error_rel": cnt["mass_error_rel"]},
+        "comparison": comparison,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(q_host.numel() * 8),
                 "d2h_bytes_per_step": int(h_host.numel() * 8 + wc_host.numel() * 8)},
         "roofline": roofline,
         "cpu_baseline": cpu,
-        "gpu_launches": int(launches),
+        "gpu_launches": int(cnt["kernel_launches"]),
         "clocks": clk,
     }
+    if learned:
+        line["config"]["learned"] = dict(net_info, net_solves=cnt["net_solves"],
+                                         net_skipped=cnt["net_skipped"],
+                                         fcg_fallbacks=cnt["fcg_fallbacks"],
+                                         net_solve_ms=round(cnt["net_ms"], 2),
+                                         plain_solve_ms=round(cnt["plain_ms"], 2),
+                                         policy="probe every 32 solves, keep if <= 1.0x plain time")
     if rank == 0:
         print(json.dumps(line))
     if pg:

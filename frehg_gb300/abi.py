@@ -99,6 +99,7 @@ class ReParams(C.Structure):
         ("rain_until", C.c_double),
         ("picard_dt_adapt", C.c_int32),
         ("pad_", C.c_int32),
+        ("picard_dh_max", C.c_double),
     ]
 
     def __init__(self, **kw):
@@ -112,6 +113,7 @@ class ReParams(C.Structure):
         self.htop = self.hbot = self.qtop = self.qbot = 0.0
         self.scheme, self.face_mean, self.picard_max_it, self.picard_tol = 0, 0, 50, 1.0e-6
         self.rain_rate, self.rain_until, self.picard_dt_adapt = 0.0, 0.0, 0
+        self.picard_dh_max = 0.0
         for k, v in kw.items():
             if k == "bc_type":
                 self.bc_type[:] = list(v)
@@ -166,6 +168,10 @@ class ReCounters(C.Structure):
         ("ir_sweeps", C.c_int64),
         ("fcg_fallbacks", C.c_int64),
         ("elastic_volume", C.c_double),
+        ("net_solves", C.c_int64),
+        ("net_skipped", C.c_int64),
+        ("net_ms", C.c_double),
+        ("plain_ms", C.c_double),
     ]
 
 
@@ -248,10 +254,12 @@ SIGNATURES = {
     "frehg_unet_forward": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _VP]),
     "frehg_unet_loss_grad": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _PD,
                                        C.POINTER(C.c_float), _VP]),
+    "frehg_unet_set_loss_weight": (C.c_int, [_VP, C.c_float]),
     "frehg_unet_adam_step": (C.c_int, [_VP, C.c_float, C.c_float, C.c_float, C.c_float, _VP]),
     "frehg_unet_flops": (C.c_int, [C.c_int, C.c_int, C.c_int, _PD]),
     "frehg_re_attach_unet": (C.c_int, [_VP, _VP]),
-    "frehg_re_training_pairs": (C.c_int, [_VP, C.c_int, _PI, _VP, _VP, _VP, _VP]),
+    "frehg_re_set_learned_policy": (C.c_int, [_VP, C.c_int, C.c_double]),
+    "frehg_re_training_pairs": (C.c_int, [_VP, C.c_int, _PI, C.c_int, _VP, _VP, _VP, _VP]),
     "frehg_build_arch": (C.c_int, []),
 }
 

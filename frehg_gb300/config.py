@@ -315,6 +315,7 @@ def re_params(cfg, scheme):
     p.picard_tol = float(get(cfg, "groundwater.picard_tol", 1e-6))
     p.picard_max_it = int(get(cfg, "groundwater.picard_max_it", 50))
     p.picard_dt_adapt = int(bool(get(cfg, "groundwater.picard_dt_adapt", False)))
+    p.picard_dh_max = float(get(cfg, "groundwater.picard_dh_max", 0.0))
     p.rain_rate = float(get(cfg, "groundwater.rain.rate", 0.0))
     p.rain_until = float(get(cfg, "groundwater.rain.until", 0.0))
     return p

@@ -1,5 +1,8 @@
 // Mixed-form modified Picard step on the device (not in reference: the reference only has the
-// PCA scheme).  The same scheme as the oracle's FP64 statement (Celia, Bouloutas & Zarba 1990):
+// PCA scheme).  A rain pulse (rain_rate) enters through the top face up to what the face
+// admits with the surface held at h = 0 (Dirichlet branch for that iterate, the excess runs
+// off); a fixed qtop is forced as in the PCA step.  Optionally the head change of one
+// iteration is limited to +-picard_dh_max.  The same scheme as the oracle's FP64 statement (Celia, Bouloutas & Zarba 1990):
 //   per iterate h^m, with K and C frozen at h^m,
 //   [V(C + Ss th^n/ths) + dt sum T] d_c - dt sum_nb T d_nb = -Rdt_c,
 //   Rdt_c = V(th(h^m) - th^n) + V Ss (th^n/ths)(h^m - h^n) - dt Q_c(h^m)   (FP64 residual),
@@ -19,8 +22,10 @@ __device__ __forceinline__ double pic_mean(int harmonic, double a, double b) {
 }
 
 __device__ __forceinline__ double pic_qtop(const ReArgs& a, size_t col) {
-  if (a.rain_rate != 0.0) return a.sc->time < a.rain_until ? a.rain_rate : 0.0;
-  return a.has_qtop ? a.qtop_field[col] : a.qtop;
+  // rain pulse: the per-column top flux field, when set, distributes it over the columns
+  const double q = a.has_qtop ? a.qtop_field[col] : (a.rain_rate != 0.0 ? a.rain_rate : a.qtop);
+  if (a.rain_rate != 0.0) return a.sc->time < a.rain_until ? q : 0.0;
+  return q;
 }
 
 // Net inflow Q_c of cell (i,j,k) at the current iterate (a.h_new) with the frozen cell
@@ -80,7 +85,17 @@ __device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, si
     r.q += r.top;
     r.tsum += t;
   } else if (a.bc5 == 2) {
-    r.top = -pic_qtop(a, col) * Az;
+    const double qin = -pic_qtop(a, col) * Az;
+    const double tD = s.Ksz * Az / (0.5 * dz);
+    const double fD = tD * (0.0 - hc) + Az * s.Ksz;
+    if (a.rain_rate != 0.0 && qin > 0.0 && fD < qin) {
+      // rain beyond what the face admits with the surface at h = 0: the top face is a
+      // Dirichlet h = 0 face for this iterate and the excess runs off (no ponding)
+      r.top = fD;
+      r.tsum += tD;
+    } else {
+      r.top = qin;
+    }
     r.q += r.top;
   }
   // face below
@@ -135,12 +150,14 @@ __global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restri
   }
 }
 
-// h^{m+1} = h^m + d and |d|_inf
+// h^{m+1} = h^m + d (d limited to +-picard_dh_max when set) and |d|_inf
 __global__ void k_pic_update(ReArgs a, const double* __restrict__ d) {
   double m = 0.0;
+  const double lim = a.picard_dh_max;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
        c += (size_t)gridDim.x * blockDim.x) {
-    const double dc = d[c];
+    double dc = d[c];
+    if (lim > 0.0) dc = fmin(fmax(dc, -lim), lim);
     a.h_new[c] += dc;
     m = fmax(m, fabs(dc));
   }

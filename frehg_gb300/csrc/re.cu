@@ -7,6 +7,7 @@
 #include "krylov_kernels.cuh"
 
 #include <cmath>
+#include <chrono>
 #include <cstring>
 #include <vector>
 
@@ -56,7 +57,15 @@ struct frehg_re {
   frehg_unet* net = nullptr;
   float* lnk_f = nullptr;  // network input fields of the current system
   float* cap_f = nullptr;
-  int plain_its_ref = 0;   // inner iterations of the last Jacobi solve (fallback threshold)
+  int plain_its_ref = 0;   // inner iterations of the last network-free solve (fallback bound)
+  // time policy of the learned preconditioner
+  int probe_every = 32;      // a probe solve applies the network every probe_every solves
+  double max_ratio = 1.0;    // network kept while its solve time <= max_ratio * plain time
+  bool net_on = false;       // outcome of the last probe
+  bool probe_pending = true; // the next solve with a network-free reference probes
+  long solves_since_probe = 0;
+  bool probe_now = false;
+  double last_plain_ms = 0.0;
   // counters / profiling
   frehg_re_counters cnt;
   Profiler prof;
@@ -176,11 +185,13 @@ static ReArgs make_args(frehg_re* re) {
   a.face_mean = re->p.face_mean;
   a.rain_rate = re->p.rain_rate;
   a.rain_until = re->p.rain_until;
+  a.picard_dh_max = re->p.picard_dh_max;
   a.soil.cls = re->cls;
   a.soil.cid = re->cid;
   a.soil.cid3d = re->cid3d;
   a.soil.Ks = re->fKs;
   a.soil.alpha = re->falpha;
+  a.soil.continuous_theta = re->p.scheme == 1;
   a.h_old = re->H[re->cur];
   a.w_old = re->W[re->cur];
   a.h_new = re->H[1 - re->cur];
@@ -289,14 +300,51 @@ __global__ void k_net_fields(ReArgs a, float* __restrict__ lnk, float* __restric
     cap[c] = (float)a.cap[c];
   }
 }
-// one training pair: r~_k and e~_k = x~* - x~_k (FP32)
+// z = M^-1 r in FP64, M the vertical-line (column tridiagonal) part of the scaled operator,
+// factorised on the fly as in the FP32 inner solve's line preconditioner (training targets of
+// the learned correction over the line solve; u is scratch).
+__global__ void k_line_apply64(const double* __restrict__ a2, const double* __restrict__ r,
+                               double* __restrict__ u, double* __restrict__ z, int ncol,
+                               int nz) {
+  const size_t sk = (size_t)ncol;
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
+       col += gridDim.x * blockDim.x) {
+    size_t c = (size_t)col;
+    double d = 1.0, y = r[c];
+    u[c] = y;
+    z[c] = 0.0;  // holds l_k until the backward sweep overwrites it
+    for (int k = 1; k < nz; ++k) {
+      c += sk;
+      const double a = a2[c - sk];
+      const double l = a / d;
+      d = 1.0 - l * a;
+      if (!(d > 0.0)) d = 1.0;
+      y = r[c] - l * y;
+      u[c] = y / d;
+      z[c] = l;
+    }
+    // u_0 = y_0 / d_0 with d_0 = 1 already holds
+    double zz = 0.0, lnext = 0.0;
+    for (int k = nz - 1; k >= 0; --k) {
+      const double lk = z[c];
+      zz = u[c] - lnext * zz;
+      lnext = lk;
+      z[c] = zz;
+      c -= (k > 0) ? sk : 0;
+    }
+  }
+}
+
+// one training pair: r~_k and the target e~_k - sub_k with e~_k = x~* - x~_k (sub = 0, r~ or
+// the line solve of r~), FP32
 __global__ void k_pair(const double* __restrict__ xstar, const double* __restrict__ x,
-                       const double* __restrict__ r, float* __restrict__ rout,
-                       float* __restrict__ eout, size_t n) {
+                       const double* __restrict__ r, const double* __restrict__ sub,
+                       float* __restrict__ rout, float* __restrict__ eout, size_t n) {
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
        c += (size_t)gridDim.x * blockDim.x) {
     rout[c] = (float)r[c];
-    eout[c] = (float)(xstar[c] - x[c]);
+    const double e = xstar[c] - x[c];
+    eout[c] = (float)(sub ? e - sub[c] : e);
   }
 }
 }  // namespace
@@ -312,10 +360,19 @@ static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
   frehg_solver_config cfg = re->cfg;
   const bool learned = !strncmp(cfg.pc_type, "unet", 4);
   re->ksp.net = NetPrecond();
+  bool use_net = false;
   if (learned) {
     cfg.precision = 1;
     strcpy(cfg.pc_type, strcmp(re->cfg.pc_type, "unet-line") ? "jacobi" : "line");
+    bool probe = false;
     if (re->net && re->plain_its_ref > 0) {
+      // time policy: probe the network every probe_every solves (always with probe_every 0)
+      probe = re->probe_every <= 0 || re->probe_pending ||
+              re->solves_since_probe >= re->probe_every;
+      use_net = probe || re->net_on;
+    }
+    re->probe_now = probe;
+    if (use_net) {
       ReArgs a = make_args(re);
       k_net_fields<<<nblocks(re->n), 256, 0, st>>>(a, re->lnk_f, re->cap_f);
       FG_CUDA(cudaGetLastError());
@@ -323,10 +380,31 @@ static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
       re->ksp.net.lnk = re->lnk_f;
       re->ksp.net.cap = re->cap_f;
       re->ksp.net.max_inner = 2 * re->plain_its_ref;
+    } else if (re->net && re->plain_its_ref > 0) {
+      re->cnt.net_skipped += 1;
     }
   }
+  const auto t0 = std::chrono::steady_clock::now();
   const int rc = re->ksp.solve(re->A, x_out, cfg, st, res);
-  if (learned && rc == FREHG_OK && (!re->ksp.net.net || res->fallback)) re->plain_its_ref = res->its;
+  const double ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (learned && rc == FREHG_OK) {
+    if (use_net) {
+      re->cnt.net_solves += 1;
+      re->cnt.net_ms += ms;
+      if (re->probe_now) {
+        re->net_on = re->probe_every <= 0 || re->last_plain_ms <= 0.0 ||
+                     ms <= re->max_ratio * re->last_plain_ms;
+        re->probe_pending = false;
+        re->solves_since_probe = 0;
+      }
+    } else {
+      re->last_plain_ms = ms;
+    }
+    ++re->solves_since_probe;
+    if (!use_net || res->fallback) re->plain_its_ref = res->its;
+  }
+  if (!use_net) re->cnt.plain_ms += ms;
   if (res->fallback) re->cnt.fcg_fallbacks += 1;
   return rc;
 }
@@ -467,7 +545,10 @@ static int picard_step(frehg_re* re) {
       }
     }
     if (converged) break;
-    if (!re->p.picard_dt_adapt || dt <= re->p.dt_min) {
+    // a failed step is retried at half the time step, down to an emergency floor of
+    // dt_min / 16 below the controller's range
+    const double dt_floor = re->p.dt_min / 16.0;
+    if (!re->p.picard_dt_adapt || dt <= dt_floor) {
       if (fail == FREHG_OK) {
         set_error("Picard iteration did not reach |dh| < %g in %d iterations (dt %g)",
                   re->p.picard_tol, re->p.picard_max_it, dt);
@@ -476,17 +557,19 @@ static int picard_step(frehg_re* re) {
       re->cnt.last_picard_iterations = its;
       return fail;
     }
-    dt = fmax(0.5 * dt, re->p.dt_min);  // retry the step with half the time step
+    dt = fmax(0.5 * dt, dt_floor);
   }
   FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n, k_pic_final<<<nb, 256, 0, st>>>(a));
   FG_CUDA(cudaGetLastError());
   re->cnt.last_picard_iterations = its;
   if (re->p.picard_dt_adapt) {
+    // Picard-count controller: grow after <= 3 iterations, shrink after >= 8, within
+    // [dt_min, dt_max] (a dt below dt_min after a retry only grows back)
     double nd = dt;
     if (its <= 3)
       nd = fmin(dt * 1.25, re->p.dt_max);
     else if (its >= 8)
-      nd = fmax(dt * 0.7, re->p.dt_min);
+      nd = fmax(dt * 0.7, fmin(dt, re->p.dt_min));
     FG_CUDA(cudaMemcpyAsync(&re->sc->dt, &nd, sizeof(double), cudaMemcpyHostToDevice, st));
     re->p.dt = nd;
   }
@@ -971,13 +1054,31 @@ int frehg_re_attach_unet(frehg_re* re, frehg_unet* net) {
     FG_CUDA(cudaMalloc(&re->cap_f, re->n * sizeof(float)));
   }
   re->plain_its_ref = 0;
+  re->net_on = false;
+  re->probe_pending = true;
+  re->solves_since_probe = 0;
+  re->last_plain_ms = 0.0;
   return FREHG_OK;
 }
 
-int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, float* r_out,
-                            float* e_out, float* lnk_out, float* cap_out) {
+int frehg_re_set_learned_policy(frehg_re* re, int probe_every, double max_ratio) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_ARG(probe_every >= 0 && max_ratio > 0.0, "probe_every >= 0 and max_ratio > 0 required");
+  re->probe_every = probe_every;
+  re->max_ratio = max_ratio;
+  re->net_on = false;
+  re->probe_pending = true;
+  re->solves_since_probe = 0;
+  return FREHG_OK;
+}
+
+int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, int target,
+                            float* r_out, float* e_out, float* lnk_out, float* cap_out) {
   clear_error();
   FG_ARG(re && iters && r_out && e_out && lnk_out && cap_out && npairs > 0, "bad argument");
+  FG_ARG(target >= 0 && target <= 2, "target must be 0 (error), 1 (error - r) or 2 "
+         "(error - line solve of r)");
   FG_ARG(re->finalized && re->attached, "training pairs need an initialised, attached solver");
   FG_ARG(re->p.scheme == 0, "training pairs are drawn from the PCA head solve");
   int kmax = 0;
@@ -1008,6 +1109,12 @@ int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, float* r
   FG_TRY(K.solve(re->A, re->scratch, cfg, st, &res));
   double* xstar = nullptr;
   FG_CUDA(cudaMalloc(&xstar, n * sizeof(double)));
+  double *zl = nullptr, *ul = nullptr;
+  if (target == 2) {
+    FG_CUDA(cudaMalloc(&zl, n * sizeof(double)));
+    FG_CUDA(cudaMalloc(&ul, n * sizeof(double)));
+  }
+  const int ncol = re->nx * re->ny;
   FG_CUDA(cudaMemcpyAsync(xstar, K.x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
   // rerun the iteration and record (r~_k, x~* - x~_k)
   CgDevState init;
@@ -1022,7 +1129,13 @@ int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, float* r
   int q = 0;
   for (int it = 0; it <= kmax && q < npairs; ++it) {
     if (it == iters[q]) {
-      k_pair<<<nb, 256, 0, st>>>(xstar, K.x, K.r, r_out + (size_t)q * n, e_out + (size_t)q * n, n);
+      const double* sub = target == 1 ? K.r : nullptr;
+      if (target == 2) {
+        k_line_apply64<<<(ncol + 127) / 128, 128, 0, st>>>(re->A.a2, K.r, ul, zl, ncol, re->nz);
+        sub = zl;
+      }
+      k_pair<<<nb, 256, 0, st>>>(xstar, K.x, K.r, sub, r_out + (size_t)q * n,
+                                 e_out + (size_t)q * n, n);
       ++q;
     }
     if (it == kmax) break;
@@ -1034,6 +1147,8 @@ int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, float* r
   FG_CUDA(cudaGetLastError());
   FG_CUDA(cudaStreamSynchronize(st));
   cudaFree(xstar);
+  cudaFree(zl);
+  cudaFree(ul);
   if (q < npairs) {
     set_error("training pairs: the iteration stopped before iteration %d", iters[q]);
     return FREHG_ERR_STATE;

@@ -60,7 +60,8 @@ struct ReArgs {
   int bc4, bc5;
   int full3d, ghosts_valid, adaptive, use_corrector, has_qtop;
   int face_mean;                   // Picard: 0 arithmetic, 1 harmonic
-  double rain_rate, rain_until;    // Picard: time-varying top flux
+  double rain_rate, rain_until;    // Picard: rain pulse on the top face (no ponding)
+  double picard_dh_max;            // Picard: per-iteration head change limit (0 = none)
   SoilView soil;
   const double* h_old;  // h^n (and hn)
   const double* w_old;  // wc^n (and wcn)

@@ -321,8 +321,9 @@ __global__ void k_out(const bf16* __restrict__ d1, const float* __restrict__ wo,
 // loss = mean((y - t)^2); gy = 2 (y - t) / n; plus the output-layer gradients and dL/dd1
 __global__ void k_out_bwd(const bf16* __restrict__ d1, const float* __restrict__ wo,
                           const float* __restrict__ y, const float* __restrict__ tgt,
-                          const float* __restrict__ tscale, size_t n, bf16* __restrict__ gd1,
-                          float* __restrict__ gwo, double* __restrict__ loss) {
+                          const float* __restrict__ tscale, size_t n, float weight,
+                          bf16* __restrict__ gd1, float* __restrict__ gwo,
+                          double* __restrict__ loss) {
   const float ts = *tscale;
   float lw[17];
 #pragma unroll
@@ -332,8 +333,8 @@ __global__ void k_out_bwd(const bf16* __restrict__ d1, const float* __restrict__
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n;
        p += (size_t)gridDim.x * blockDim.x) {
     const float e = y[p] - tgt[p] * ts;
-    ls += (double)e * e;
-    const float gy = 2.0f * e * inv_n;
+    ls += (double)weight * e * e;
+    const float gy = 2.0f * weight * e * inv_n;
     uint32_t* o = reinterpret_cast<uint32_t*>(gd1 + p * 16);
 #pragma unroll
     for (int c = 0; c < 16; c += 2) {
@@ -450,6 +451,7 @@ struct frehg_unet {
   bf16* wt = nullptr;   // mirrored/transposed BF16 weights (data gradient)
   int adam_t = 0;
   float kmean = 0.f, kscale = 1.f, cscale = 1.f;
+  float loss_weight = 1.f;  // multiplies the loss and its gradients
   // activations
   int nx = 0, ny = 0, nz = 0;
   size_t cap1 = 0;
@@ -595,7 +597,8 @@ int backward(frehg_unet* net, const float* target, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(net->loss, 0, sizeof(double), st));
   // normalised target: t * (1/rms r); y holds the unscaled network output
   k_out_bwd<<<blocks_for(n1), 256, 0, st>>>(net->d1, M + net->ooff, net->y, target, net->scal,
-                                            n1, net->g_d1, G + net->ooff, net->loss);
+                                            n1, net->loss_weight, net->g_d1, G + net->ooff,
+                                            net->loss);
   auto relu_b = [&](bf16* g, int gs, int go, const bf16* a, int as, int ao, int c, size_t n) {
     k_relu_bwd<<<blocks_for(n * c), 256, 0, st>>>(g, gs, go, a, as, ao, c, n);
   };
@@ -793,6 +796,13 @@ int frehg_unet_loss_grad(frehg_unet* net, int nx, int ny, int nz, const float* r
   if (grad_host)
     FG_CUDA(cudaMemcpyAsync(grad_host, net->grad, net->nparam * 4, cudaMemcpyDeviceToHost, st));
   FG_CUDA(cudaStreamSynchronize(st));
+  return FREHG_OK;
+}
+
+int frehg_unet_set_loss_weight(frehg_unet* net, float weight) {
+  clear_error();
+  FG_ARG(net && weight > 0.f, "positive weight required");
+  net->loss_weight = weight;
   return FREHG_OK;
 }
 

@@ -35,6 +35,11 @@ struct SoilView {
   const double* Ks = nullptr;
   const double* alpha = nullptr;
   int cid3d = 0;
+  // Picard scheme: van Genuchten theta(h) without the air-entry switch (theta = theta_s only
+  // for h > 0).  The reference's switch (VanGenuchten.hpp:38-41) is a jump in theta of up to
+  // 0.008 (sand) at h = air_entry that a Picard iteration cannot converge across; K and C of
+  // the VG branch already switch at h = 0.
+  int continuous_theta = 0;
 };
 
 __device__ __forceinline__ CellSoil soil_of(const SoilView& v, size_t cell, size_t col) {
@@ -46,7 +51,7 @@ __device__ __forceinline__ CellSoil soil_of(const SoilView& v, size_t cell, size
   s.ths = k.ths;
   s.thr = k.thr;
   s.Ss = k.Ss;
-  s.aev = k.aev;
+  s.aev = (v.continuous_theta && !k.use_mvg) ? 0.0 : k.aev;
   s.m = k.m;
   s.inv_m = k.inv_m;
   s.inv_n = k.inv_n;

@@ -7,8 +7,10 @@ training set are torch tensors (plumbing).
 Training data are (residual, error) pairs the plain solver produces: for seeded three-layer
 soils (sand / loam / clay, in-layer ln Ks GRF sigma 1.5) at 128x128x64, the PCA head system of
 several time levels is solved with FP64 Jacobi-PCG, then the iteration is re-run and at chosen
-iteration numbers k the scaled residual r~_k and error x~* - x~_k are stored together with
-ln K and the moisture capacity C of the state.
+iteration numbers k the scaled residual r~_k and a target are stored together with ln K and the
+moisture capacity C of the state.  The preconditioner is z = M r~ + NN(r~), so the target is the
+part of the error x~* - x~_k that M r~ misses: e~ - r~ for M = I ("unet", the unit-diagonal
+Jacobi step) or e~ - M_line^-1 r~ ("unet-line", the vertical-line solve).
 """
 from __future__ import annotations
 
@@ -74,6 +76,9 @@ class UNet:
                                              C.byref(loss), None, stream), "unet_loss_grad")
         return loss.value
 
+    def set_loss_weight(self, w):
+        check(self._lib.frehg_unet_set_loss_weight(self._h, float(w)), "unet_loss_weight")
+
     def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, stream=None):
         check(self._lib.frehg_unet_adam_step(self._h, lr, b1, b2, eps, stream), "unet_adam")
 
@@ -84,26 +89,22 @@ class UNet:
         return f.value
 
 
+TARGETS = {"unet": 1, "unet-line": 2}
+
+
 def layered_workload(nx, ny, nz, seed, dt=60.0):
-    """three-layer heterogeneous soil (the learned-preconditioner configuration's generator)"""
+    """three-layer heterogeneous soil (the learned-preconditioner configuration's generator;
+    training seeds are 100 + i, the benchmark's own soil uses seed 5)"""
     from . import workloads as W
-    w = W.config1("pca", nx=nx, ny=ny, nz=nz, steps=1)
-    classes, cls, Ks = W.layered_soil(nx, ny, nz, seed_layers=1000 + seed, seed_k=2000 + seed)
-    w.classes, w.class_index, w.Ks, w.alpha = classes, cls.ravel(), Ks, None
+    w = W.config3("pca", nx=nx, ny=ny, nz=nz, steps=1, seed=seed, precision=0)
     w.params.dt = dt
-    # water table at the same relative depth as the 6.4 m deep benchmark column (4 m)
-    depth = nz * w.params.dz
-    table = 0.625 * depth
-    w.h0 = np.broadcast_to(W.hydrostatic_head(nz, w.params.dz, table)[:, None, None],
-                           (nz, ny, nx)).copy()
-    w.params.hbot = depth - table
-    w.name = f"layered-{nx}x{ny}x{nz}-seed{seed}"
     return w
 
 
 def generate_pairs(seeds, nx=128, ny=128, nz=64, snapshots=(0, 3, 6, 9), iters=PAIR_ITERS,
-                   device="cuda"):
-    """(residual, error) pairs from plain solves; returns a dict of torch tensors on the GPU."""
+                   pc="unet-line", device="cuda"):
+    """(residual, target) pairs from plain solves; returns a dict of torch tensors on the GPU
+    (r, t = target, lnk, cap, snap = the snapshot index of each pair)."""
     import torch
     from .re_solver import Grid, ReSolver
     lib = load_library()
@@ -126,15 +127,16 @@ def generate_pairs(seeds, nx=128, ny=128, nz=64, snapshots=(0, 3, 6, 9), iters=P
             while done < snap:
                 g.advance_step()
                 done += 1
-            check(lib.frehg_re_training_pairs(g._h, len(iters), it_arr, R[q].data_ptr(),
-                                              E[q].data_ptr(), LNK[s].data_ptr(),
-                                              CAP[s].data_ptr()), "training_pairs")
+            check(lib.frehg_re_training_pairs(g._h, len(iters), it_arr, TARGETS[pc],
+                                              R[q].data_ptr(), E[q].data_ptr(),
+                                              LNK[s].data_ptr(), CAP[s].data_ptr()),
+                  "training_pairs")
             snap_of += [s] * len(iters)
             q += len(iters)
             s += 1
         del g
     torch.cuda.synchronize()
-    return dict(r=R, e=E, lnk=LNK, cap=CAP, snap=np.array(snap_of), shape=(nx, ny, nz))
+    return dict(r=R, t=E, lnk=LNK, cap=CAP, snap=np.array(snap_of), shape=(nx, ny, nz), pc=pc)
 
 
 def input_scaling(data):
@@ -146,19 +148,31 @@ def input_scaling(data):
     return kmean, (1.0 / kstd if kstd > 0 else 1.0), (1.0 / cstd if cstd > 0 else 1.0)
 
 
-def correction_targets(data):
-    """The preconditioner is z = r~ + NN(r~) (Jacobi step on the unit-diagonal operator plus a
-    learned correction), so the network is trained on e~ - r~."""
-    data["t"] = data["e"] - data["r"]
-    return data
+def pair_weights(data):
+    """1 / mean((t / rms r)^2) per pair: the loss of every pair becomes its relative error, so
+    pairs whose error is large next to their residual (late iterations, smooth residuals) do not
+    drown the others"""
+    if "w" not in data:
+        r2 = (data["r"].double() ** 2).mean(dim=1)
+        t2 = (data["t"].double() ** 2).mean(dim=1)
+        data["w"] = (r2 / t2.clamp_min(1e-300)).cpu().numpy()
+    return data["w"]
+
+
+def pair_loss(net: UNet, data, q):
+    """relative loss of pair q (no parameter update)"""
+    nx, ny, nz = data["shape"]
+    s = int(data["snap"][q])
+    net.set_loss_weight(pair_weights(data)[q])
+    return net.loss_grad(nx, ny, nz, data["r"][q].data_ptr(), data["lnk"][s].data_ptr(),
+                         data["cap"][s].data_ptr(), data["t"][q].data_ptr())
 
 
 def train(net: UNet, data, steps=5000, lr=1e-3, seed=0, log_every=0):
-    """Adam on randomly drawn pairs (target e~ - r~); returns the loss history"""
-    if "t" not in data:
-        correction_targets(data)
+    """Adam on randomly drawn pairs with the relative per-pair loss; returns the loss history"""
     nx, ny, nz = data["shape"]
     net.set_scaling(*input_scaling(data))
+    wts = pair_weights(data)
     rng = np.random.default_rng(seed)
     npair = data["r"].shape[0]
     losses = []
@@ -166,6 +180,7 @@ def train(net: UNet, data, steps=5000, lr=1e-3, seed=0, log_every=0):
     for it in range(steps):
         q = int(rng.integers(npair))
         s = int(data["snap"][q])
+        net.set_loss_weight(wts[q])
         loss = net.loss_grad(nx, ny, nz, data["r"][q].data_ptr(), data["lnk"][s].data_ptr(),
                              data["cap"][s].data_ptr(), data["t"][q].data_ptr())
         net.adam(lr)

@@ -145,6 +145,52 @@ def layered_soil(nx, ny, nz, seed_layers, seed_k, sigma=1.5, corr=(4.0, 8.0, 8.0
     return classes, cls, Ks
 
 
+def config3(scheme="pca", nx=256, ny=256, nz=128, steps=60, seed=5, precision=1,
+            pc="unet-line", rtol=1e-12, ir_rtol=1e-12) -> Workload:
+    """256x256x128 three-layer soil (sand / loam / clay at seeded interface depths, in-layer
+    ln Ks GRF sigma 1.5, 8x8x4 cells) under config 1's forcing: hydrostatic start with the
+    water table at 0.625 of the depth (4 m at 6.4 m), 20 mm/h rain on top, bottom head fixed,
+    dt = 60 s.  The learned preconditioner's configuration (FCG under FP64 refinement)."""
+    w = config1(scheme, nx=nx, ny=ny, nz=nz, steps=steps, rtol=rtol, precision=precision)
+    classes, cls, Ks = layered_soil(nx, ny, nz, seed_layers=seed, seed_k=1000 + seed)
+    w.classes, w.class_index, w.Ks, w.alpha = classes, cls.ravel(), Ks, None
+    depth = nz * w.params.dz
+    table = 0.625 * depth
+    w.h0 = np.broadcast_to(hydrostatic_head(nz, w.params.dz, table)[:, None, None],
+                           (nz, ny, nx)).copy()
+    w.params.hbot = depth - table
+    w.solver.pc_type = pc.encode() if precision == 1 else b"jacobi"
+    w.solver.ir_rtol = ir_rtol
+    w.name = f"c3-{scheme}-{nx}x{ny}x{nz}-seed{seed}"
+    return w
+
+
+def config4(nx=768, ny=768, nz=96, steps=200, seeds=(6, 7), precision=1, pc="unet-line",
+            rtol=1e-12, ir_rtol=1e-12) -> Workload:
+    """768x768x96 three-layer soil (config 3's generator, new seeds), dry start h = -5 m,
+    50 mm/h rain for the first 1800 s then none (the surface does not pond: rain beyond what
+    the top face admits at h = 0 runs off), free-drainage bottom, lateral no-flux, mixed-form
+    Picard (|dh|_inf < 1e-6 m, at most 1 m head change per iteration) with the time step driven
+    by the Picard count between 10 and 120 s, 200 steps."""
+    dz = 0.05
+    classes, cls, Ks = layered_soil(nx, ny, nz, seed_layers=seeds[0], seed_k=seeds[1])
+    p = ReParams(soil=soil(LOAM), dx=1.0, dy=1.0, dz=dz, botz=-nz * dz, dt=10.0, dt_min=10.0,
+                 dt_max=120.0, adaptive_dt=0, use_corrector=1, use_full3d=1,
+                 bc_type=[0, 0, 0, 0, 3, 2], qtop=0.0)
+    p.scheme = 1
+    p.picard_tol = 1.0e-6
+    p.picard_max_it = 50
+    p.picard_dt_adapt = 1
+    p.picard_dh_max = 1.0
+    p.rain_rate = -50.0e-3 / 3600.0
+    p.rain_until = 1800.0
+    solver = SolverConfig("cg", pc if precision == 1 else "jacobi", rtol=rtol, max_it=20000,
+                          precision=precision, ir_rtol=ir_rtol)
+    return Workload(f"c4-picard-{nx}x{ny}x{nz}", nx, ny, nz, p, solver, steps,
+                    h0=np.full((nz, ny, nx), -5.0), classes=classes, class_index=cls.ravel(),
+                    Ks=Ks)
+
+
 def small_box(nx=4, ny=4, nz=8, steps=40, full3d=True, Ks=1.0e-5) -> Workload:
     """tests/re/test_re_3d.cpp's closed heterogeneous box (dx=2, dy=1, dz=0.05, dt=5, Ss=0)."""
     s = SoilParams(alpha=2.0, n=1.6, theta_s=0.45, theta_r=0.05, Ks_x=Ks, Ks_y=Ks, Ks_z=Ks,

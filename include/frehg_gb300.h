@@ -95,10 +95,15 @@ typedef struct frehg_re_params {
   int32_t face_mean;      /* 0 = arithmetic 0.5(Kp+Km) (reference), 1 = harmonic              */
   int32_t picard_max_it;  /* default 50                                                      */
   double picard_tol;      /* |dh|_inf stopping test [m], default 1e-6                        */
-  double rain_rate;       /* time-varying top flux: qtop = rain_rate while t < rain_until    */
-  double rain_until;      /* [s]; rain_rate = 0 disables (default)                           */
+  double rain_rate;       /* rain on the top face (bc_type[5] = 2) while t < rain_until [m/s,
+                             < 0 downward; a top flux field, when set, replaces it per
+                             column]; the face takes at most what a surface held at h = 0
+                             admits (no ponding, the excess runs off); 0 disables             */
+  double rain_until;      /* [s]                                                             */
   int32_t picard_dt_adapt;/* Picard-count driven dt (1) or fixed (0)                         */
   int32_t pad_;
+  double picard_dh_max;   /* largest head change one Picard iteration applies per cell [m];
+                             0 = unlimited (default)                                         */
 } frehg_re_params;
 
 /* struct SolverConfig (include/frehg2/linear/SolverConfig.hpp:14-20) plus precision keys. */
@@ -190,6 +195,10 @@ typedef struct frehg_re_counters {
   int64_t ir_sweeps;         /* mixed precision: FP64 refinement sweeps (not in reference)  */
   int64_t fcg_fallbacks;     /* learned preconditioner dropped for Jacobi (not in reference) */
   double elastic_volume;     /* Picard: cumulative specific-storage volume [m^3]            */
+  int64_t net_solves;        /* solves that applied the network (not in reference)          */
+  int64_t net_skipped;       /* solves the time policy ran without it (not in reference)    */
+  double net_ms;             /* host time of the solves that applied the network [ms]       */
+  double plain_ms;           /* host time of the solves without the network [ms]            */
 } frehg_re_counters;
 int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c);
 
@@ -281,23 +290,36 @@ int frehg_unet_forward(frehg_unet* net, int nx, int ny, int nz, const float* r, 
 int frehg_unet_loss_grad(frehg_unet* net, int nx, int ny, int nz, const float* r,
                          const float* lnk, const float* cap, const float* target, double* loss,
                          float* grad_host, void* stream);
+/* weight w multiplies the loss of frehg_unet_loss_grad and its gradients (default 1); training
+ * sets w = 1 / mean((target / rms r)^2) per pair so that every pair's relative error counts
+ * alike */
+int frehg_unet_set_loss_weight(frehg_unet* net, float weight);
 int frehg_unet_adam_step(frehg_unet* net, float lr, float beta1, float beta2, float eps,
                          void* stream);
 /* floating-point operations of one forward application on an nx*ny*nz grid */
 int frehg_unet_flops(int nx, int ny, int nz, double* flops);
 
-/* Attach a network to an RE handle: with pc_type "unet" the head solves run flexible CG
- * preconditioned by it inside the FP64 refinement loop (FP32 Krylov).  The first solve after
- * attaching runs Jacobi CG and sets the fallback threshold: a solve whose FCG iterations
- * exceed twice that count continues with Jacobi CG.  net = NULL detaches. */
+/* Attach a network to an RE handle.  With pc_type "unet" ("unet-line") the head solves run
+ * flexible CG inside the FP64 refinement loop (FP32 Krylov) with z = M r + NN(r, ln K, C),
+ * M = I (the unit-diagonal Jacobi step) or the vertical-line solve.  The first solve after
+ * attaching runs the network-free method (Jacobi- or line-PCG) and sets the fallback
+ * threshold: a solve whose FCG iterations exceed twice that count continues without the
+ * network.  net = NULL detaches. */
 int frehg_re_attach_unet(frehg_re* re, frehg_unet* net);
+/* Time policy of the learned preconditioner: every probe_every-th solve applies the network;
+ * if that solve took longer than max_ratio times the last network-free solve, the solves up to
+ * the next probe run without it, otherwise the network stays on.  probe_every = 0 applies the
+ * network on every solve (no time policy).  Defaults: 32, 1.0. */
+int frehg_re_set_learned_policy(frehg_re* re, int probe_every, double max_ratio);
 /* Training pairs from the plain solver: assembles the next PCA step's system at the current
  * state (nothing advances), solves it with FP64 Jacobi-PCG, re-runs the iteration from zero and
- * at each iteration number iters[q] (increasing) stores the scaled residual r~ and error
- * x~* - x~ as FP32 into r_out + q*n, e_out + q*n; ln K (vertical) and C into lnk_out, cap_out.
+ * at each iteration number iters[q] (increasing) stores the scaled residual r~ and a target
+ * as FP32 into r_out + q*n, t_out + q*n; ln K (vertical) and C into lnk_out, cap_out.
+ * target: 0 = the error x~* - x~, 1 = error - r~ (correction over the Jacobi step),
+ * 2 = error - M^-1 r~ with M the vertical-line tridiagonal part of the scaled operator.
  * Device pointers, n = nx*ny*nz. */
-int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, float* r_out,
-                            float* e_out, float* lnk_out, float* cap_out);
+int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, int target,
+                            float* r_out, float* t_out, float* lnk_out, float* cap_out);
 
 /* Allocation-free CG solve.  No counterpart in the reference: it exists for callers that may
  * not allocate GPU memory themselves (a component under a host framework that owns the device

@@ -207,22 +207,26 @@ static inline long IN(const or_re* s, int i, int j, int k) {
 /* ReSolver::soilAt (ReSolver.cpp:87-96): class of the clamped cell, plus the per-cell Ks /
  * alpha overrides (not in reference). */
 static inline frehg_soil_params soil_at(const or_re* s, int i, int j, int k) {
-  if (!s->cls && !s->fKs && !s->falpha) return s->p.soil;
-  const int ci = i < 0 ? 0 : (i >= s->nx ? s->nx - 1 : i);
-  const int cj = j < 0 ? 0 : (j >= s->ny ? s->ny - 1 : j);
-  const int ck = k < 0 ? 0 : (k >= s->nz ? s->nz - 1 : k);
   frehg_soil_params r = s->p.soil;
-  if (s->cls) {
-    const long id = s->cls3d ? IN(s, ci, cj, ck) : (long)ci + (long)cj * s->nx;
-    r = s->classes[s->cls[id]];
+  if (s->cls || s->fKs || s->falpha) {
+    const int ci = i < 0 ? 0 : (i >= s->nx ? s->nx - 1 : i);
+    const int cj = j < 0 ? 0 : (j >= s->ny ? s->ny - 1 : j);
+    const int ck = k < 0 ? 0 : (k >= s->nz ? s->nz - 1 : k);
+    if (s->cls) {
+      const long id = s->cls3d ? IN(s, ci, cj, ck) : (long)ci + (long)cj * s->nx;
+      r = s->classes[s->cls[id]];
+    }
+    if (s->fKs) {
+      const double K = s->fKs[IN(s, ci, cj, ck)];
+      r.Ks_x = K;
+      r.Ks_y = K;
+      r.Ks_z = K;
+    }
+    if (s->falpha) r.alpha = s->falpha[IN(s, ci, cj, ck)];
   }
-  if (s->fKs) {
-    const double K = s->fKs[IN(s, ci, cj, ck)];
-    r.Ks_x = K;
-    r.Ks_y = K;
-    r.Ks_z = K;
-  }
-  if (s->falpha) r.alpha = s->falpha[IN(s, ci, cj, ck)];
+  /* Picard (not in reference): VG theta(h) without the air-entry switch, i.e. theta = theta_s
+   * only for h > 0, so theta(h) is continuous like the VG K(h) and C(h) */
+  if (s->p.scheme == 1 && !r.use_mvg) r.air_entry = 0.0;
   return r;
 }
 

@@ -77,3 +77,30 @@ def test_mass_balance_closes(gpu_lib):
     el = g.elastic_volume()
     err = abs((v1 - v0) + el - (top + bot)) / v0
     assert err < 1e-12, err
+
+
+def test_config4_window(gpu_lib, oracle_mod):
+    """The combined configuration's physics on a 14x10x96 window: three soil classes with an
+    in-class Ks field, dry start, rain limited by the h = 0 surface (no ponding), 1 m
+    head-change limit per Picard iteration, free-drainage bottom, Picard-count dt.  The rain
+    stops at 300 s here, so the 40 steps (dt >= 10 s) cover its end; the water budget closes."""
+    w = W.config4(nx=14, ny=10, nz=96, steps=40, precision=0)
+    w.params.rain_until = 300.0
+    g, o = pair(w, oracle_mod)
+    v0 = g.water_volume()
+    run_compare(g, o, w.steps)
+    top, bot = g.boundary_volumes()
+    assert top > 0.0
+    err = abs((g.water_volume() - v0) + g.elastic_volume() - (top + bot)) / v0
+    assert err < 1e-12, err
+
+
+def test_picard_head_change_limit(gpu_lib, oracle_mod):
+    """With a 0.05 m per-iteration limit the ponded-top infiltration needs more Picard
+    iterations but GPU and oracle agree iteration for iteration."""
+    w = W.config0("picard", nx=6, ny=5, nz=30, steps=4)
+    w.params.picard_dh_max = 0.05
+    w.params.picard_max_it = 200
+    g, o = pair(w, oracle_mod)
+    run_compare(g, o, w.steps)
+    assert g.counters().last_picard_iterations > 3
