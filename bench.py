@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--scheme", default=None, choices=["pca", "picard"])
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
     ap.add_argument("--pc", default=None, choices=["jacobi", "line", "unet", "unet-line"])
+    ap.add_argument("--inner-rtol", type=float, default=None,
+                    help="relative reduction of each FP32 inner solve (mixed precision)")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain FP64 arm (comparison and head error)")
     ap.add_argument("--unet-weights", default=None, help="trained network (.npz, learned.py)")
@@ -105,6 +107,8 @@ def workload(args, nx=None, ny=None, precision=None, pc=None):
     w.solver.pc_type = (pc if prec else "jacobi").encode()
     if prec:
         w.solver.ir_rtol = 1e-12
+        if args.inner_rtol:
+            w.solver.inner_rtol = args.inner_rtol
     return w
 
 

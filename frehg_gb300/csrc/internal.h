@@ -193,6 +193,8 @@ class KrylovSolver {
   float* zf = nullptr;
   // vertical-line preconditioner (FP32 factors and sweep scratch)
   int ensure_line(size_t n);
+  // scaling of the operator for the mixed path (sq = D^1/2 into r, FP32 copy, line factors)
+  int prep_mixed(Stencil64& A, cudaStream_t st, bool line);
   size_t cap_line = 0;
   float *lkf = nullptr, *dinvf = nullptr, *uf = nullptr;
   int g32_line = 0;

@@ -80,7 +80,7 @@ __global__ void k_diag_rsqrt(double* __restrict__ s, size_t n) {
        c += (size_t)gridDim.x * blockDim.x) {
     double d = s[c];
     if (d == 0.0) d = 1.0;  // PCJacobi replaces a zero diagonal entry by 1
-    s[c] = 1.0 / sqrt(d);   // NaN for d < 0: the solve then stops with DIVERGED_NANORINF
+    s[c] = rsqrt(d);        // NaN for d < 0: the solve then stops with DIVERGED_NANORINF
   }
 }
 
@@ -433,8 +433,11 @@ int KrylovSolver::run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int
 int KrylovSolver::solve(Stencil64& A, double* x_out, const frehg_solver_config& cfg,
                         cudaStream_t st, CgResult* res) {
   FG_TRY(ensure(A.n));
+  if (cfg.precision == 1) {
+    FG_TRY(prep_mixed(A, st, !strcmp(cfg.pc_type, "line")));
+    return solve_mixed(A, x_out, cfg, st, res);
+  }
   FG_TRY(scale(A, st));
-  if (cfg.precision == 1) return solve_mixed(A, x_out, cfg, st, res);
   if (strcmp(cfg.pc_type, "jacobi") != 0) {
     set_error("pc_type '%s' needs the mixed-precision solve (precision 1)", cfg.pc_type);
     return FREHG_ERR_UNSUPPORTED;

@@ -24,12 +24,13 @@
 namespace fg {
 
 // r~ = s b - A~ x~ (FP64, kept in rres); e = 0; sums of r~^2 (scale of the inner system),
-// (r~/s)^2 for the true residual and b^2 for ||b||.  The last block runs the refinement test.
+// (r~/s)^2 = (sq r~)^2 for the true residual (sq = D^1/2) and b^2 for ||b||.  The last block
+// runs the refinement test.
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
-    const double* __restrict__ s, const double* __restrict__ b, const double* __restrict__ x,
-    double* __restrict__ rres, float* __restrict__ ef, int n0, int n1, int n2, int planes,
-    int tiles, CgDevState* ir, double* partials, double ir_rtol) {
+    const double* __restrict__ s, const double* __restrict__ sq, const double* __restrict__ b,
+    const double* __restrict__ x, double* __restrict__ rres, float* __restrict__ ef, int n0,
+    int n1, int n2, int planes, int tiles, CgDevState* ir, double* partials, double ir_rtol) {
   if (ir->status) return;
   const int t0 = (n0 + 31) / 32;
   double v[3] = {0.0, 0.0, 0.0};
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(256) k_ir_residual(
       rres[c] = r;
       ef[c] = 0.0f;
       v[0] = fma(r, r, v[0]);
-      const double ru = r / sc;
+      const double ru = r * sq[c];  // r~ / s = D^1/2 r~
       v[1] = fma(ru, ru, v[1]);
       v[2] = fma(bc, bc, v[2]);
     }
@@ -476,6 +477,102 @@ int KrylovSolver::ensure32(size_t n) {
   return FREHG_OK;
 }
 
+// Scaling of a fresh operator for the mixed path in two passes: s = D^-1/2 with sq = D^1/2
+// (the true-residual norm multiplies by it), then one pass per column that scales the
+// couplings in place (FP64, for the refinement residual), writes their FP32 copies and, with
+// the line preconditioner, the column factors (FP64 recurrence, one division per cell).
+__global__ void k_diag_rsqrt_sq(double* __restrict__ s, double* __restrict__ sq, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    double d = s[c];
+    if (d == 0.0) d = 1.0;  // PCJacobi replaces a zero diagonal entry by 1
+    const double r = rsqrt(d);
+    s[c] = r;
+    sq[c] = d * r;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
+                                                     double* __restrict__ a1,
+                                                     double* __restrict__ a2,
+                                                     const double* __restrict__ s,
+                                                     float* __restrict__ f0,
+                                                     float* __restrict__ f1,
+                                                     float* __restrict__ f2,
+                                                     float* __restrict__ lk,
+                                                     float* __restrict__ dinv, int n0, int n1,
+                                                     int n2, int line) {
+  const int ncol = n0 * n1;
+  const size_t sk = (size_t)ncol;
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
+       col += gridDim.x * blockDim.x) {
+    const int i0 = col % n0, i1 = col / n0;
+    double inv_d = 1.0, aprev = 0.0;
+    size_t c = (size_t)col;
+    for (int k = 0; k < n2; ++k, c += sk) {
+      const double sc = s[c];
+      const double v0 = (i0 + 1 < n0) ? a0[c] * sc * s[c + 1] : 0.0;
+      const double v1 = (i1 + 1 < n1) ? a1[c] * sc * s[c + n0] : 0.0;
+      const double v2 = (k + 1 < n2) ? a2[c] * sc * s[c + sk] : 0.0;
+      a0[c] = v0;
+      a1[c] = v1;
+      a2[c] = v2;
+      f0[c] = (float)v0;
+      f1[c] = (float)v1;
+      f2[c] = (float)v2;
+      if (line) {
+        double l = 0.0;
+        if (k > 0) {
+          l = aprev * inv_d;
+          double d = 1.0 - l * aprev;
+          if (!(d > 0.0)) d = 1.0;  // not SPD: that row falls back to the Jacobi step
+          inv_d = 1.0 / d;
+        }
+        lk[c] = (float)l;
+        dinv[c] = (float)inv_d;
+        aprev = v2;
+      }
+    }
+  }
+}
+
+// sq = 1 / s for an operator scaled earlier (s already holds D^-1/2)
+__global__ void k_inv64(const double* __restrict__ s, double* __restrict__ sq, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+       c += (size_t)gridDim.x * blockDim.x)
+    sq[c] = 1.0 / s[c];
+}
+
+int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line) {
+  const size_t n = A.n;
+  FG_TRY(ensure32(n));
+  if (line) FG_TRY(ensure_line(n));
+  const int nb = reduction_blocks(n, 256, 4);
+  const double dn = (double)n;
+  const int ncol = A.n0 * A.n1;
+  const int lb = (int)std::min<long>((ncol + 127) / 128, kMaxRedBlocks);
+  if (!A.scaled) {
+    FG_LAUNCH(prof, st, "k_diag_rsqrt_sq", 24.0 * dn,
+              k_diag_rsqrt_sq<<<nb, 256, 0, st>>>(A.s, r, n));
+    FG_LAUNCH(prof, st, "k_scale_mixed", (56.0 + 12.0 + (line ? 8.0 : 0.0)) * dn,
+              k_scale_mixed<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, op32.a0, op32.a1,
+                                                op32.a2, lkf, dinvf, A.n0, A.n1, A.n2,
+                                                line ? 1 : 0));
+    FG_CUDA(cudaGetLastError());
+    A.scaled = true;
+    return FREHG_OK;
+  }
+  // an operator scaled by an earlier solve: derive sq, the FP32 copy and the factors from it
+  FG_LAUNCH(prof, st, "k_inv64", 16.0 * dn, k_inv64<<<nb, 256, 0, st>>>(A.s, r, n));
+  FG_LAUNCH(prof, st, "k_to_f32", 36.0 * dn,
+            k_to_f32<<<nb, 256, 0, st>>>(A.a0, A.a1, A.a2, op32.a0, op32.a1, op32.a2, n));
+  if (line)
+    FG_LAUNCH(prof, st, "k_line_factor", 16.0 * dn,
+              k_line_factor<<<lb, 128, 0, st>>>(A.a2, lkf, dinvf, ncol, A.n2));
+  FG_CUDA(cudaGetLastError());
+  return FREHG_OK;
+}
+
 int KrylovSolver::ensure_line(size_t n) {
   if (lkf && n <= cap_line) return FREHG_OK;
   cudaFree(lkf);
@@ -498,20 +595,12 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
   const bool vec4 = (A.n0 % 4) == 0 && getenv("FREHG_NO_VEC4") == nullptr;
   const StencilLaunch L4 = launch_v4(A.n0, A.n1, A.n2);
-  FG_LAUNCH(prof, st, "k_to_f32", 36.0 * dn,
-            k_to_f32<<<nb, 256, 0, st>>>(A.a0, A.a1, A.a2, op32.a0, op32.a1, op32.a2, n));
   FG_LAUNCH(prof, st, "k_zero64", 8.0 * dn, k_zero64<<<nb, 256, 0, st>>>(x, n));
   FG_CUDA(cudaGetLastError());
   // inner preconditioner: Jacobi (unit diagonal, z = r) or vertical lines
   const bool line = !strcmp(cfg.pc_type, "line");
   const int ncol = A.n0 * A.n1, nzl = A.n2;
   const int lb = (int)std::min<long>((ncol + 127) / 128, kMaxRedBlocks);
-  if (line) {
-    FG_TRY(ensure_line(n));
-    FG_LAUNCH(prof, st, "k_line_factor", 16.0 * dn,
-              k_line_factor<<<lb, 128, 0, st>>>(A.a2, lkf, dinvf, ncol, nzl));
-    FG_CUDA(cudaGetLastError());
-  }
   CgDevState ir0, in0;
   memset(&ir0, 0, sizeof(ir0));
   memset(&in0, 0, sizeof(in0));
@@ -577,8 +666,8 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   for (;;) {
     FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
               k_ir_residual<<<L.grid, L.block, 0, st>>>(
-                  A.a0, A.a1, A.a2, A.s, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes, L.tiles,
-                  dst, partials, cfg.ir_rtol));
+                  A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                  L.tiles, dst, partials, cfg.ir_rtol));
     FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
               k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials, cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());

@@ -38,8 +38,8 @@ struct PicRow {
 __device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, size_t c,
                                           size_t col, int i, int j, int k) {
   const int hm = a.face_mean;
-  const double dx = a.dx, dy = a.dy, dz = a.dz;
-  const double Ax = dy * dz, Ay = dx * dz, Az = dx * dy;
+  const double dz = a.dz;
+  const double Az = a.dx * a.dy;
   const double hc = a.h_new[c];
   const double krc = a.kr[c];
   const double Kxc = s.Ksx * krc, Kyc = s.Ksy * krc, Kzc = s.Ksz * krc;
@@ -47,26 +47,26 @@ __device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, si
   double t;
   if (i > 0) {
     const CellSoil sm = soil_of(a.soil, c - 1, col - 1);
-    t = pic_mean(hm, sm.Ksx * a.kr[c - 1], Kxc) * Ax / dx;
+    t = pic_mean(hm, sm.Ksx * a.kr[c - 1], Kxc) * a.cx;
     r.q += t * (a.h_new[c - 1] - hc);
     r.tsum += t;
   }
   if (i + 1 < a.nx) {
     const CellSoil sp = soil_of(a.soil, c + 1, col + 1);
-    t = pic_mean(hm, Kxc, sp.Ksx * a.kr[c + 1]) * Ax / dx;
+    t = pic_mean(hm, Kxc, sp.Ksx * a.kr[c + 1]) * a.cx;
     r.q += t * (a.h_new[c + 1] - hc);
     r.tsum += t;
     r.tx = t;
   }
   if (j > 0) {
     const CellSoil sm = soil_of(a.soil, c - a.nx, col - a.nx);
-    t = pic_mean(hm, sm.Ksy * a.kr[c - a.nx], Kyc) * Ay / dy;
+    t = pic_mean(hm, sm.Ksy * a.kr[c - a.nx], Kyc) * a.cy;
     r.q += t * (a.h_new[c - a.nx] - hc);
     r.tsum += t;
   }
   if (j + 1 < a.ny) {
     const CellSoil sp = soil_of(a.soil, c + a.nx, col + a.nx);
-    t = pic_mean(hm, Kyc, sp.Ksy * a.kr[c + a.nx]) * Ay / dy;
+    t = pic_mean(hm, Kyc, sp.Ksy * a.kr[c + a.nx]) * a.cy;
     r.q += t * (a.h_new[c + a.nx] - hc);
     r.tsum += t;
     r.ty = t;
@@ -75,18 +75,18 @@ __device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, si
   if (k > 0) {
     const CellSoil sm = soil_of(a.soil, c - a.ncol, col);
     const double kf = pic_mean(hm, sm.Ksz * a.kr[c - a.ncol], Kzc);
-    t = kf * Az / dz;
+    t = kf * a.cz;
     r.q += t * (a.h_new[c - a.ncol] - hc) + Az * kf;
     r.tsum += t;
   } else if (a.bc5 == 1) {
     const double kf = s.Ksz;
-    t = kf * Az / (0.5 * dz);
+    t = kf * (2.0 * a.cz);
     r.top = t * (a.htop - hc) + Az * kf;
     r.q += r.top;
     r.tsum += t;
   } else if (a.bc5 == 2) {
     const double qin = -pic_qtop(a, col) * Az;
-    const double tD = s.Ksz * Az / (0.5 * dz);
+    const double tD = s.Ksz * (2.0 * a.cz);
     const double fD = tD * (0.0 - hc) + Az * s.Ksz;
     if (a.rain_rate != 0.0 && qin > 0.0 && fD < qin) {
       // rain beyond what the face admits with the surface at h = 0: the top face is a
@@ -102,14 +102,14 @@ __device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, si
   if (k + 1 < a.nz) {
     const CellSoil sp = soil_of(a.soil, c + a.ncol, col);
     const double kf = pic_mean(hm, Kzc, sp.Ksz * a.kr[c + a.ncol]);
-    t = kf * Az / dz;
+    t = kf * a.cz;
     r.q += t * (a.h_new[c + a.ncol] - hc) - Az * kf;
     r.tsum += t;
     r.tz = t;
   } else if (a.bc4 == 1) {
     const double kb = s.Ksz * vg_kr(s, a.hbot);
     const double kf = pic_mean(hm, Kzc, kb);
-    t = kf * Az / (0.5 * dz);
+    t = kf * (2.0 * a.cz);
     r.bot = t * (a.hbot - hc) - Az * kf;
     r.q += r.bot;
     r.tsum += t;
@@ -124,29 +124,37 @@ __device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, si
 }
 
 // Linearised system of one Picard iteration (diagonal into dg, +x/+y/+z couplings, rhs).
+// Launched on (32 x 8)-column tiles marching through `planes` levels (no index divisions).
 __global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restrict__ dg,
                                                       double* __restrict__ a0,
                                                       double* __restrict__ a1,
                                                       double* __restrict__ a2,
-                                                      double* __restrict__ bvec) {
+                                                      double* __restrict__ bvec, int planes,
+                                                      int tiles) {
   const double dt = a.sc->dt_used;
   const double V = a.dx * a.dy * a.dz;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
-       c += (size_t)gridDim.x * blockDim.x) {
-    const size_t col = c % a.ncol;
-    const int k = (int)(c / a.ncol), i = (int)(col % a.nx), j = (int)(col / a.nx);
+  const int t0 = (a.nx + 31) / 32;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+  const int i = (tile % t0) * 32 + threadIdx.x;
+  const int j = (tile / t0) * 8 + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) continue;
+  const size_t col = (size_t)i + (size_t)a.nx * j;
+  const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
+  for (int k = kb; k < ke; ++k) {
+    const size_t c = col + a.ncol * k;
     const CellSoil s = soil_of(a.soil, c, col);
     const double hc = a.h_new[c];
     const double wcn = a.w_old[c];
     const double th = a.wch[c];  // theta(h^m) and C(h^m) from k_constit
     const double C = a.cap[c];
     const PicRow r = pic_row(a, s, c, col, i, j, k);
-    dg[c] = V * (C + s.Ss * wcn / s.ths) + dt * r.tsum;
+    dg[c] = V * (C + s.Ss * wcn * s.inv_ths) + dt * r.tsum;
     a0[c] = -dt * r.tx;
     a1[c] = -dt * r.ty;
     a2[c] = -dt * r.tz;
-    const double rdt = V * (th - wcn) + V * s.Ss * (wcn / s.ths) * (hc - a.h_old[c]) - dt * r.q;
+    const double rdt = V * (th - wcn) + V * s.Ss * (wcn * s.inv_ths) * (hc - a.h_old[c]) - dt * r.q;
     bvec[c] = -rdt;
+  }
   }
 }
 
@@ -167,22 +175,29 @@ __global__ void k_pic_update(ReArgs a, const double* __restrict__ d) {
 }
 
 // conservative water-content update + boundary / elastic volumes + time
-__global__ void k_pic_final(ReArgs a) {
+__global__ void __launch_bounds__(256) k_pic_final(ReArgs a, int planes, int tiles) {
   const double dt = a.sc->dt_used;
   const double V = a.dx * a.dy * a.dz;
+  const double inv_V = 1.0 / V;
   double v[3] = {0.0, 0.0, 0.0};
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
-       c += (size_t)gridDim.x * blockDim.x) {
-    const size_t col = c % a.ncol;
-    const int k = (int)(c / a.ncol), i = (int)(col % a.nx), j = (int)(col / a.nx);
+  const int t0 = (a.nx + 31) / 32;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+  const int i = (tile % t0) * 32 + threadIdx.x;
+  const int j = (tile / t0) * 8 + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) continue;
+  const size_t col = (size_t)i + (size_t)a.nx * j;
+  const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
+  for (int k = kb; k < ke; ++k) {
+    const size_t c = col + a.ncol * k;
     const CellSoil s = soil_of(a.soil, c, col);
     const double wcn = a.w_old[c];
     const PicRow r = pic_row(a, s, c, col, i, j, k);
-    const double el = V * s.Ss * (wcn / s.ths) * (a.h_new[c] - a.h_old[c]);
-    a.w_new[c] = wcn + (dt * r.q - el) / V;
+    const double el = V * s.Ss * (wcn * s.inv_ths) * (a.h_new[c] - a.h_old[c]);
+    a.w_new[c] = wcn + (dt * r.q - el) * inv_V;
     v[0] += r.top * dt;
     v[1] += r.bot * dt;
     v[2] += el;
+  }
   }
   double tot[3];
   if (grid_sum<3>(v, a.partials, &a.sc->arrive[0], tot) && flat_tid() == 0) {

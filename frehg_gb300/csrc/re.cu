@@ -66,6 +66,7 @@ struct frehg_re {
   long solves_since_probe = 0;
   bool probe_now = false;
   double last_plain_ms = 0.0;
+  double apply_ms = -1.0;    // host time of one network application at this grid (once)
   // counters / profiling
   frehg_re_counters cnt;
   Profiler prof;
@@ -114,6 +115,7 @@ static SoilClass make_class(const frehg_soil_params& s) {
   k.m = 1.0 - 1.0 / s.n;
   k.inv_m = 1.0 / k.m;
   k.inv_n = 1.0 / s.n;
+  k.inv_ths = 1.0 / s.theta_s;
   k.use_vg = s.use_vg;
   k.use_mvg = s.use_mvg;
   return k;
@@ -186,6 +188,20 @@ static ReArgs make_args(frehg_re* re) {
   a.rain_rate = re->p.rain_rate;
   a.rain_until = re->p.rain_until;
   a.picard_dh_max = re->p.picard_dh_max;
+  // geometric factors, so that the kernels multiply instead of dividing in FP64
+  {
+    const double dx = re->p.dx, dy = re->p.dy, dz = re->p.dz;
+    a.inv_dx = 1.0 / dx;
+    a.inv_dy = 1.0 / dy;
+    a.inv_dz = 1.0 / dz;
+    a.cx = dy * dz / dx;
+    a.cy = dx * dz / dy;
+    a.cz = dx * dy / dz;
+    a.v_dz = dx * dy * dz / dz;
+    a.inv_Ax = 1.0 / (dy * dz);
+    a.inv_Ay = 1.0 / (dx * dz);
+    a.inv_Az = 1.0 / (dx * dy);
+  }
   a.soil.cls = re->cls;
   a.soil.cid = re->cid;
   a.soil.cid3d = re->cid3d;
@@ -349,6 +365,26 @@ __global__ void k_pair(const double* __restrict__ xstar, const double* __restric
 }
 }  // namespace
 
+// Host time of one network application on this grid (second of two calls: the first sizes
+// the activation buffers).  The input is the ln K field; the cost does not depend on values.
+static int time_network(frehg_re* re) {
+  cudaStream_t st = re->stream;
+  ReArgs a = make_args(re);
+  k_net_fields<<<nblocks(re->n), 256, 0, st>>>(a, re->lnk_f, re->cap_f);
+  FG_CUDA(cudaGetLastError());
+  float* z = reinterpret_cast<float*>(re->scratch);  // n doubles hold n floats
+  double ms = 0.0;
+  for (int q = 0; q < 2; ++q) {
+    FG_CUDA(cudaStreamSynchronize(st));
+    const auto t0 = std::chrono::steady_clock::now();
+    FG_TRY(unet_apply(re->net, re->nx, re->ny, re->nz, re->lnk_f, re->lnk_f, re->cap_f, z, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  re->apply_ms = ms;
+  return FREHG_OK;
+}
+
 // Krylov solve of the assembled system with the handle's configuration.  The learned
 // preconditioners run flexible CG inside the mixed-precision refinement with
 // z = M(r) + NN(r, ln K, C): M = I for pc_type "unet" (unit-diagonal Jacobi step, Jacobi-PCG
@@ -369,6 +405,17 @@ static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
       // time policy: probe the network every probe_every solves (always with probe_every 0)
       probe = re->probe_every <= 0 || re->probe_pending ||
               re->solves_since_probe >= re->probe_every;
+      if (probe && re->probe_every > 0) {
+        // a solve applies the network at least once: when one application alone takes longer
+        // than max_ratio times the whole network-free solve, no probe can pay
+        if (re->apply_ms < 0.0) FG_TRY(time_network(re));
+        if (re->apply_ms >= re->max_ratio * re->last_plain_ms) {
+          probe = false;
+          re->net_on = false;
+          re->probe_pending = false;
+          re->solves_since_probe = 0;
+        }
+      }
       use_net = probe || re->net_on;
     }
     re->probe_now = probe;
@@ -475,7 +522,7 @@ static int pca_step(frehg_re* re) {
   re->cnt.realloc_sweeps += sweeps;
   // apply reallocation, clampWaterContent, adaptiveTimeStep
   FG_LAUNCH(prof, st, "k_finalize", (25.0 + sb) * n,
-            k_finalize<<<nb, 256, 0, st>>>(a, top_sat));
+            k_finalize<<<L.grid, L.block, 0, st>>>(a, top_sat, L.planes, L.tiles));
   FG_CUDA(cudaGetLastError());
   if (prof->on) {
     FG_CUDA(cudaStreamSynchronize(st));
@@ -504,6 +551,7 @@ static int picard_step(frehg_re* re) {
   FG_TRY(read_scalars(re));
   double dt = re->sc_host->dt;
   ReArgs a = make_args(re);
+  const StencilLaunch PL = stencil_launch(re->nx, re->ny, re->nz);
   int its = 0;
   for (;;) {
     FG_CUDA(cudaMemcpyAsync(&re->sc->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st));
@@ -517,8 +565,9 @@ static int picard_step(frehg_re* re) {
                 (k_constit<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch, re->cap)));
       re->A.scaled = false;
       FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
-                k_pic_assemble<<<nb, 256, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
-                                                   re->A.b));
+                k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
+                                                             re->A.a2, re->A.b, PL.planes,
+                                                             PL.tiles));
       FG_CUDA(cudaGetLastError());
       CgResult res;
       const int rc = solve_system(re, re->scratch, &res);
@@ -559,7 +608,8 @@ static int picard_step(frehg_re* re) {
     }
     dt = fmax(0.5 * dt, dt_floor);
   }
-  FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n, k_pic_final<<<nb, 256, 0, st>>>(a));
+  FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n,
+            k_pic_final<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
   FG_CUDA(cudaGetLastError());
   re->cnt.last_picard_iterations = its;
   if (re->p.picard_dt_adapt) {
@@ -1058,6 +1108,7 @@ int frehg_re_attach_unet(frehg_re* re, frehg_unet* net) {
   re->probe_pending = true;
   re->solves_since_probe = 0;
   re->last_plain_ms = 0.0;
+  re->apply_ms = -1.0;
   return FREHG_OK;
 }
 

@@ -62,6 +62,8 @@ struct ReArgs {
   int face_mean;                   // Picard: 0 arithmetic, 1 harmonic
   double rain_rate, rain_until;    // Picard: rain pulse on the top face (no ponding)
   double picard_dh_max;            // Picard: per-iteration head change limit (0 = none)
+  // geometric factors: 1/dx, 1/dy, 1/dz; Ax/dx, Ay/dy, Az/dz; V/dz; 1/Ax, 1/Ay, 1/Az
+  double inv_dx, inv_dy, inv_dz, cx, cy, cz, v_dz, inv_Ax, inv_Ay, inv_Az;
   SoilView soil;
   const double* h_old;  // h^n (and hn)
   const double* w_old;  // wc^n (and wcn)
@@ -143,9 +145,14 @@ __global__ void k_step_begin(ReScalars* sc) { sc->dt_used = sc->dt; }
 template <bool THETA, bool CAP>
 __global__ void k_constit(ReArgs a, const double* __restrict__ h, double* __restrict__ kr,
                           double* __restrict__ th, double* __restrict__ cap) {
+  // the column index is only needed for a per-column class map; 32-bit when it fits
+  const bool col_map = a.soil.cid && !a.soil.cid3d;
+  const bool small = a.n <= 0xffffffffull;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
        c += (size_t)gridDim.x * blockDim.x) {
-    const size_t col = c % a.ncol;
+    const size_t col = !col_map ? 0
+                       : small  ? (size_t)((uint32_t)c % (uint32_t)a.ncol)
+                                : c % a.ncol;
     const CellSoil s = soil_of(a.soil, c, col);
     const Constit r = vg_constit<THETA, CAP>(s, h[c]);
     kr[c] = r.kr;
@@ -232,18 +239,15 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
         Kzm = face_top(a, s.Ksz, s.Ksz * krc);
       }
     }
-    // groundwaterMatCoeff (ReSolver.cpp:433-468)
-    const double Gxp = -Kxp * dtg * Ax / dx;
-    const double Gxm = -Kxm * dtg * Ax / dx;
-    const double Gyp = -Kyp * dtg * Ay / dy;
-    const double Gym = -Kym * dtg * Ay / dy;
-    const double dzf_p = 0.5 * (dzk + dzk);
-    double Gzp = -Kzp * dtg / (dzk * dzf_p);
-    Gzp *= V;
-    const double dzf_m = (k == 0) ? 0.5 * dzk : 0.5 * (dzk + dzk);
-    double Gzm = -Kzm * dtg / (dzk * dzf_m);
-    Gzm *= V;
-    const double store = ch + s.Ss * wcn / s.ths;
+    // groundwaterMatCoeff (ReSolver.cpp:433-468) with the geometric quotients precomputed:
+    // A/d = a.cx, a.cy; V/(dz*dzf) = Az/dz (2 Az/dz for the half cell above k = 0)
+    const double Gxp = -Kxp * dtg * a.cx;
+    const double Gxm = -Kxm * dtg * a.cx;
+    const double Gyp = -Kyp * dtg * a.cy;
+    const double Gym = -Kym * dtg * a.cy;
+    const double Gzp = -Kzp * dtg * a.cz;
+    const double Gzm = -Kzm * dtg * ((k == 0) ? 2.0 * a.cz : a.cz);
+    const double store = ch + s.Ss * wcn * s.inv_ths;
     double Gct = store;
     Gct *= V;
     Gct -= (Gxp + Gxm + Gyp + Gym);
@@ -253,10 +257,10 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
     } else {
       Gct -= Gzm;
     }
-    // groundwaterRhs (ReSolver.cpp:515-547)
+    // groundwaterRhs (ReSolver.cpp:515-547); V/dz precomputed
     double g = store * hc * V;
-    g -= dtg * V * Kzp / dzk;
-    g += dtg * V * Kzm / dzk;
+    g -= dtg * a.v_dz * Kzp;
+    g += dtg * a.v_dz * Kzm;
     const double hn_ghost = gv ? hc : 0.0;  // lateral hn ghosts are copies (or zero at step 1)
     if (i == a.nx - 1) g -= Gxp * hn_ghost;
     if (i == 0) g -= Gxm * hn_ghost;
@@ -264,12 +268,12 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
     if (j == 0) g -= Gym * hn_ghost;
     if (k == a.nz - 1) {
       if (a.bc4 == 1) g += Gzp * (gv ? a.hbot : 0.0);
-      if (a.bc4 == 2) g += dtg * V * (a.qbot + Kzp) / dzk;
+      if (a.bc4 == 2) g += dtg * a.v_dz * (a.qbot + Kzp);
     }
     if (k == 0 && a.bc5 == 1) g -= Gzm * a.htop;
     if (k == 0 && a.bc5 == 2) {
       const double qcol = a.has_qtop ? a.qtop_field[col] : a.qtop;
-      g += -dtg * V * (qcol + Kzm) / dzk;
+      g += -dtg * a.v_dz * (qcol + Kzm);
     }
     dg[c] = Gct;
     a0[c] = (i + 1 < a.nx) ? Gxp : 0.0;
@@ -282,9 +286,13 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
 
 // kr(h^{n+1}) and theta(h^{n+1}) once the solve has written h^{n+1} (re_solve_unpack).
 __global__ void k_post(ReArgs a) {
+  const bool col_map = a.soil.cid && !a.soil.cid3d;
+  const bool small = a.n <= 0xffffffffull;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
        c += (size_t)gridDim.x * blockDim.x) {
-    const size_t col = c % a.ncol;
+    const size_t col = !col_map ? 0
+                       : small  ? (size_t)((uint32_t)c % (uint32_t)a.ncol)
+                                : c % a.ncol;
     const CellSoil so = soil_of(a.soil, c, col);
     const Constit r = vg_constit<true, false>(so, a.h_new[c]);
     a.kr[c] = r.kr;
@@ -297,7 +305,7 @@ __device__ __forceinline__ double flux_z_inner(const ReArgs& a, double Kc, doubl
                                                double hn) {
   const double faceA = a.dx * a.dy;
   const double kface = 0.5 * (Kc + Kn);
-  return faceA * kface * ((hn - hc) / a.dz - 1.0);
+  return faceA * kface * ((hn - hc) * a.inv_dz - 1.0);
 }
 
 // groundwaterFlux + updateWaterContent + adaptiveTimeStep's dq (ReSolver.cpp:671-786, 891-905)
@@ -362,10 +370,10 @@ __global__ void __launch_bounds__(256) k_correct(ReArgs a, int planes, int tiles
       }
       double qxp = 0.0, qxm = 0.0, qyp = 0.0, qym = 0.0;
       if (a.full3d) {
-        qxp = (dy * dzk) * Kxp * (hxp - hc) / dx;
-        if (i > 0) qxm = (dy * dzk) * Kxm * (hc - hxm) / dx;
-        qyp = (dx * dzk) * Kyp * (hyp - hc) / dy;
-        if (j > 0) qym = (dx * dzk) * Kym * (hc - hym) / dy;
+        qxp = Ax * Kxp * (hxp - hc) * a.inv_dx;
+        if (i > 0) qxm = Ax * Kxm * (hc - hxm) * a.inv_dx;
+        qyp = Ay * Kyp * (hyp - hc) * a.inv_dy;
+        if (j > 0) qym = Ay * Kym * (hc - hym) * a.inv_dy;
       }
       // vertical fluxes (upward positive): qzp through the bottom face, qzm through the top face
       const double Kc = s.Ksz * krc;
@@ -381,7 +389,7 @@ __global__ void __launch_bounds__(256) k_correct(ReArgs a, int planes, int tiles
         const double hg = a.bc4 == 1 ? a.hbot : hc;  // enforceHeadBc bottom ghost
         const double Kg = s.Ksz * vg_kr(s, hg);
         const double kface = 0.5 * (Kc + Kg);
-        qzp = Az * kface * ((hg - hc) / (0.5 * dzk) - 1.0);
+        qzp = Az * kface * ((hg - hc) * (2.0 * a.inv_dz) - 1.0);
       }
       double qzm;
       if (k > 0) {
@@ -392,14 +400,14 @@ __global__ void __launch_bounds__(256) k_correct(ReArgs a, int planes, int tiles
       } else {
         const double kface = a.bc5 == 1 ? s.Ksz : 0.0;
         const double hg = a.bc5 == 1 ? a.htop : hc;
-        qzm = Az * kface * ((hc - hg) / (0.5 * dzk) - 1.0);
+        qzm = Az * kface * ((hc - hg) * (2.0 * a.inv_dz) - 1.0);
       }
       // updateWaterContent
       const double hn = a.h_old[c];
       const double wcn = a.w_old[c];
       double wc;
       if (a.use_corrector) {
-        const double coeff = V * (1.0 + 1.0 * s.Ss * (hc - hn) / s.ths);
+        const double coeff = V * (1.0 + 1.0 * s.Ss * (hc - hn) * s.inv_ths);
         const double dqx = dtg * (qxp - qxm);
         const double dqy = dtg * (qyp - qym);
         const double dqz = dtg * (qzp - qzm);
@@ -419,9 +427,9 @@ __global__ void __launch_bounds__(256) k_correct(ReArgs a, int planes, int tiles
       if (Kyp != 0.0) f |= F_OPEN_YP;
       a.flags[c] = f;
       if (a.adaptive && k > 0) {
-        const double qin = qxp / Ax + qyp / Ay + qzp / Az;
-        const double qou = qxm / Ax + qym / Ay + qzm / Az;
-        const double dq = fabs(qin - qou) * dtq / dzk;
+        const double qin = qxp * a.inv_Ax + qyp * a.inv_Ay + qzp * a.inv_Az;
+        const double qou = qxm * a.inv_Ax + qym * a.inv_Ay + qzm * a.inv_Az;
+        const double dq = fabs(qin - qou) * dtq * a.inv_dz;
         dqmax = fmax(dqmax, dq);
       }
       if (k == 0) vol[0] += -qzm * dtg;
@@ -497,13 +505,18 @@ __global__ void k_realloc_sweep(ReArgs a, int top_sat) {
 
 // Apply the reallocation (ReSolver.cpp:825-833), clampWaterContent (:839-853) and the
 // adaptiveTimeStep Courant bound (:906-910); the last block updates dt (:921-928) and time.
-__global__ void k_finalize(ReArgs a, int top_sat) {
+// Launched on (32 x 8)-column tiles marching through `planes` levels (no index divisions).
+__global__ void __launch_bounds__(256) k_finalize(ReArgs a, int top_sat, int planes, int tiles) {
   double dtco = INFINITY;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
-       c += (size_t)gridDim.x * blockDim.x) {
-    const size_t col = c % a.ncol;
-    const int k = (int)(c / a.ncol);
-    const int i = (int)(col % a.nx), j = (int)(col / a.nx);
+  const int t0 = (a.nx + 31) / 32;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+  const int i = (tile % t0) * 32 + threadIdx.x;
+  const int j = (tile / t0) * 8 + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) continue;
+  const size_t col = (size_t)i + (size_t)a.nx * j;
+  const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
+  for (int k = kb; k < ke; ++k) {
+    const size_t c = col + a.ncol * k;
     const CellSoil s = soil_of(a.soil, c, col);
     const uint8_t f = a.flags[c];
     double wc = a.w_new[c];
@@ -541,6 +554,7 @@ __global__ void k_finalize(ReArgs a, int top_sat) {
       const double dt_co = a.co_max * a.dz / dk;
       if (dt_co < dtco) dtco = dt_co;  // std::min(dt_Comin, dt_Co): NaN is skipped
     }
+  }
   }
   // -max(-x) gives the NaN-skipping min
   double m;

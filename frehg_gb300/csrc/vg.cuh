@@ -16,13 +16,13 @@ namespace fg {
 // reference recomputes per call: m = 1 - 1/n, 1/m, 1/n).
 struct SoilClass {
   double alpha, n, ths, thr, Ksx, Ksy, Ksz, Ss, aev;
-  double m, inv_m, inv_n;
+  double m, inv_m, inv_n, inv_ths;
   int32_t use_vg, use_mvg;
 };
 
 // Soil of one cell after the per-cell overrides (not in reference: continuous Ks / alpha).
 struct CellSoil {
-  double alpha, n, ths, thr, Ss, aev, m, inv_m, inv_n;
+  double alpha, n, ths, thr, Ss, aev, m, inv_m, inv_n, inv_ths;
   double Ksx, Ksy, Ksz;
   int32_t use_vg, use_mvg;
 };
@@ -55,6 +55,7 @@ __device__ __forceinline__ CellSoil soil_of(const SoilView& v, size_t cell, size
   s.m = k.m;
   s.inv_m = k.inv_m;
   s.inv_n = k.inv_n;
+  s.inv_ths = k.inv_ths;
   if (v.Ks) {
     const double K = v.Ks[cell];
     s.Ksx = K;
@@ -94,15 +95,21 @@ __device__ __forceinline__ double vg_theta(const CellSoil& s, double h) {
   return wc;
 }
 
-// headFromWaterContent (VanGenuchten.hpp:50-65)
+// headFromWaterContent (VanGenuchten.hpp:50-65).  The reference's
+// pow(pow(q, 1/m) - 1, 1/n) with q = (wcm - thr)/(theta - thr) is evaluated as
+// exp(log(expm1(log(q)/m)) / n): q^{1/m} - 1 without cancellation near saturation, and
+// exp/log instead of the (costlier, extended-precision) FP64 pow.
 __device__ __forceinline__ double vg_head(const CellSoil& s, double wc) {
   const double eps = 1.0e-7;
   if (s.use_vg) {
     const double wcm_val = vg_wcm(s);
     double theta = wc;
     if (theta - s.thr < eps) theta = s.thr + eps;
-    if (theta < s.ths)
-      return -(1.0 / s.alpha) * pow(pow((wcm_val - s.thr) / (theta - s.thr), s.inv_m) - 1.0, s.inv_n);
+    if (theta < s.ths) {
+      const double q = (wcm_val - s.thr) / (theta - s.thr);
+      const double x = expm1(s.inv_m * log(q));
+      return -(1.0 / s.alpha) * exp(s.inv_n * log(x));
+    }
     return 0.0;
   }
   return log((wc - s.thr) / (s.ths - s.thr)) / 0.1634;
@@ -152,10 +159,10 @@ __device__ __forceinline__ double vg_kr(const CellSoil& s, double h) {
 // L = ln|alpha h|, t = e^{nL} = |alpha h|^n, u = ln(1 + t):
 //   se = (1+t)^-m = e^{-mu},  se^{1/m} = 1/(1+t),  1 - se^{1/m} = t/(1+t),
 //   (1 - se^{1/m})^m = e^{m(nL - u)},  kr = e^{-mu/2} (1 - e^{m(nL-u)})^2,
-//   C = alpha n m (ths - thr) |alpha h|^{n-1} (1+t)^{-(m+1)} = alpha n m (ths-thr) e^{(n-1)L - (m+1)u}.
+//   C = alpha n m (ths - thr) |alpha h|^{n-1} (1+t)^{-(m+1)} = alpha n m (ths-thr) t se / (|alpha h| (1+t)).
 // The same relations as the reference's pow() forms (VanGenuchten.hpp:31-111), evaluated with
-// 2 logarithms and 3-4 exponentials instead of 11 pow() calls; 1 - e^{x} is formed as -expm1(x)
-// so no digits cancel when the soil is dry.  The caps and the saturated branches are the
+// 2 logarithms, 2 exponentials and one expm1 instead of 11 pow() calls (se = e^{-mu/2}
+// squared); 1 - e^{x} is formed as -expm1(x) so no digits cancel when the soil is dry.  The caps and the saturated branches are the
 // reference's.  MVG and the exponential model use the reference forms above.
 struct Constit {
   double kr, theta, cap;
@@ -177,9 +184,10 @@ __device__ __forceinline__ Constit vg_constit(const CellSoil& s, double h) {
   const double t = exp(nL);
   const double u = log1p(t);
   const double mu = mm * u;
-  // kr
+  // kr; se = e^{-mu} = (e^{-mu/2})^2 serves theta
   const double one_minus = -expm1(mm * (nL - u));
-  double kr = exp(-0.5 * mu) * (one_minus * one_minus);
+  const double se_half = exp(-0.5 * mu);
+  double kr = se_half * (one_minus * one_minus);
   if (kr > 1.0) kr = 1.0;
   if (h > 0.0) kr = 1.0;
   r.kr = kr;
@@ -188,7 +196,7 @@ __device__ __forceinline__ Constit vg_constit(const CellSoil& s, double h) {
     if (h > s.aev)
       wc = s.ths;
     else
-      wc = s.thr + (s.ths - s.thr) * exp(-mu);
+      wc = s.thr + (s.ths - s.thr) * (se_half * se_half);
     if (wc > s.ths) wc = s.ths;
     if (wc < s.thr) wc = s.thr;
     r.theta = wc;
@@ -196,7 +204,10 @@ __device__ __forceinline__ Constit vg_constit(const CellSoil& s, double h) {
     r.theta = 0.0;
   }
   if (WANT_CAP) {
-    double c = s.alpha * s.n * mm * (s.ths - s.thr) * exp((s.n - 1.0) * L - (mm + 1.0) * u);
+    // |alpha h|^{n-1} (1+t)^{-(m+1)} = t * se / (|alpha h| (1 + t)): one division, no exp
+    double c = ah > 0.0 ? s.alpha * s.n * mm * (s.ths - s.thr) *
+                              (t * (se_half * se_half) / (ah * (1.0 + t)))
+                        : 0.0;
     if (h > 0.0) c = 0.0;
     r.cap = c;
   } else {

@@ -308,8 +308,10 @@ int frehg_unet_flops(int nx, int ny, int nz, double* flops);
 int frehg_re_attach_unet(frehg_re* re, frehg_unet* net);
 /* Time policy of the learned preconditioner: every probe_every-th solve applies the network;
  * if that solve took longer than max_ratio times the last network-free solve, the solves up to
- * the next probe run without it, otherwise the network stays on.  probe_every = 0 applies the
- * network on every solve (no time policy).  Defaults: 32, 1.0. */
+ * the next probe run without it, otherwise the network stays on.  A probe is skipped (the
+ * network stays off) when one network application, timed once per attach, already takes longer
+ * than max_ratio times the last network-free solve.  probe_every = 0 applies the network on
+ * every solve (no time policy).  Defaults: 32, 1.0. */
 int frehg_re_set_learned_policy(frehg_re* re, int probe_every, double max_ratio);
 /* Training pairs from the plain solver: assembles the next PCA step's system at the current
  * state (nothing advances), solves it with FP64 Jacobi-PCG, re-runs the iteration from zero and
