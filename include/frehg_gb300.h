@@ -109,7 +109,8 @@ typedef struct frehg_re_params {
 /* struct SolverConfig (include/frehg2/linear/SolverConfig.hpp:14-20) plus precision keys. */
 typedef struct frehg_solver_config {
   char ksp_type[16];      /* "cg" (default) or "fcg"                                         */
-  char pc_type[16];       /* "jacobi" (default here), "none", "unet"                         */
+  char pc_type[16];       /* "jacobi" (default here); with precision 1 also "line" (vertical-
+                             line tridiagonal), "unet" / "unet-line" (learned, RE handles)   */
   double rtol;            /* default 1e-8                                                    */
   double atol;            /* default 1e-50                                                   */
   int32_t max_it;         /* default 10000                                                   */

@@ -1,0 +1,195 @@
+// C++ host interface end to end on the GPU (include/frehg_gb300.hpp): the linear-solver seam on
+// a manufactured 3D Laplacian (the reference's PETSc boundary test, tests/linear/
+// test_petsc_linear_solver.cpp:70-102, asks for L2 error < 1e-9), its error behaviour, and the
+// ReSolver interface on the closed heterogeneous box of tests/re/test_re_3d.cpp:210-227 (water
+// volume conserved to 1e-10 relative).  Prints one line per check; exit status 0 when all pass.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "frehg_gb300.hpp"
+
+namespace g = frehg_gb300;
+
+static int failures = 0;
+#define EXPECT(cond, ...)                                  \
+  do {                                                     \
+    if (cond) {                                            \
+      std::printf("ok   ");                                \
+    } else {                                               \
+      std::printf("FAIL ");                                \
+      ++failures;                                          \
+    }                                                      \
+    std::printf(__VA_ARGS__);                              \
+    std::printf("\n");                                     \
+  } while (0)
+
+// 7-point SPD operator: Laplacian with unit spacings on an nx x ny x nz box, zero Dirichlet
+// values outside (diagonal 6 everywhere), rows in owned order row = (j*nx + i)*nz + k.
+static void assemble_laplacian(g::SparseSystem& A, const g::Decomp3D& d) {
+  A.beginAssembly();
+  for (int j = 0; j < d.ny; ++j)
+    for (int i = 0; i < d.nx; ++i)
+      for (int k = 0; k < d.nz; ++k) {
+        const int row = (int)d.globalRow(i, j, k);
+        int cols[7];
+        double vals[7];
+        int n = 0;
+        cols[n] = row;
+        vals[n++] = 6.0;
+        if (i > 0) { cols[n] = (int)d.globalRow(i - 1, j, k); vals[n++] = -1.0; }
+        if (i + 1 < d.nx) { cols[n] = (int)d.globalRow(i + 1, j, k); vals[n++] = -1.0; }
+        if (j > 0) { cols[n] = (int)d.globalRow(i, j - 1, k); vals[n++] = -1.0; }
+        if (j + 1 < d.ny) { cols[n] = (int)d.globalRow(i, j + 1, k); vals[n++] = -1.0; }
+        if (k > 0) { cols[n] = row - 1; vals[n++] = -1.0; }
+        if (k + 1 < d.nz) { cols[n] = row + 1; vals[n++] = -1.0; }
+        A.addRow(row, n, cols, vals);
+      }
+  A.endAssembly();
+}
+
+static std::vector<double> apply_laplacian(const std::vector<double>& x, const g::Decomp3D& d) {
+  std::vector<double> y(x.size(), 0.0);
+  for (int j = 0; j < d.ny; ++j)
+    for (int i = 0; i < d.nx; ++i)
+      for (int k = 0; k < d.nz; ++k) {
+        const long r = d.globalRow(i, j, k);
+        double v = 6.0 * x[r];
+        if (i > 0) v -= x[d.globalRow(i - 1, j, k)];
+        if (i + 1 < d.nx) v -= x[d.globalRow(i + 1, j, k)];
+        if (j > 0) v -= x[d.globalRow(i, j - 1, k)];
+        if (j + 1 < d.ny) v -= x[d.globalRow(i, j + 1, k)];
+        if (k > 0) v -= x[r - 1];
+        if (k + 1 < d.nz) v -= x[r + 1];
+        y[r] = v;
+      }
+  return y;
+}
+
+static void seam(const char* precision) {
+  g::Decomp3D d(12, 10, 8);
+  g::SolverConfig cfg;
+  cfg.rtol = 1e-12;
+  cfg.precision = precision;
+  cfg.ir_rtol = 1e-13;
+  auto ls = g::makeLinearSolver("gb300", cfg);
+  auto A = ls->createSystem(d);
+  A->preallocate(d);
+  assemble_laplacian(*A, d);
+  std::vector<double> xe(d.nOwned());
+  for (int j = 0; j < d.ny; ++j)
+    for (int i = 0; i < d.nx; ++i)
+      for (int k = 0; k < d.nz; ++k)
+        xe[d.globalRow(i, j, k)] = std::sin(0.3 * i + 1.0) * std::cos(0.2 * j) * (1.0 + 0.1 * k);
+  const std::vector<double> b = apply_laplacian(xe, d);
+  std::vector<double> x;
+  ls->setup(*A);
+  ls->solve(*A, b, x);
+  double e2 = 0.0, n2 = 0.0;
+  for (size_t q = 0; q < xe.size(); ++q) {
+    e2 += (x[q] - xe[q]) * (x[q] - xe[q]);
+    n2 += xe[q] * xe[q];
+  }
+  const double rel = std::sqrt(e2 / n2);
+  EXPECT(rel < 1e-9, "seam %s: manufactured Laplacian relative L2 error %.3e (%d iterations)",
+         precision, rel, ls->getIterationCount());
+  // getSolution returns the last solve's x
+  std::vector<double> x2;
+  A->getSolution(x2);
+  double d2 = 0.0;
+  for (size_t q = 0; q < x.size(); ++q) d2 = std::fmax(d2, std::fabs(x2[q] - x[q]));
+  EXPECT(d2 == 0.0, "seam %s: getSolution equals the solve's x", precision);
+}
+
+static void errors() {
+  bool thrown = false;
+  try {
+    g::makeLinearSolver("petsc", g::SolverConfig());
+  } catch (const std::runtime_error&) {
+    thrown = true;
+  }
+  EXPECT(thrown, "makeLinearSolver rejects a backend that is not built");
+  thrown = false;
+  try {
+    g::SolverConfig c;
+    c.pc_type = "sor";
+    g::makeLinearSolver("gb300", c);
+  } catch (const std::invalid_argument&) {
+    thrown = true;
+  }
+  EXPECT(thrown, "pc_type sor is rejected (std::invalid_argument)");
+  thrown = false;
+  try {
+    auto ls = g::makeLinearSolver("gb300", g::SolverConfig());
+    g::Decomp3D d(4, 4, 4);
+    auto A = ls->createSystem(d);
+    A->beginAssembly();
+    const int cols[2] = {0, 9};  // (0,0,0) and a cell that is not a 7-point neighbour
+    const double vals[2] = {6.0, -1.0};
+    A->addRow(0, 2, cols, vals);
+  } catch (const std::invalid_argument&) {
+    thrown = true;
+  }
+  EXPECT(thrown, "addRow rejects a column outside the 7-point stencil");
+}
+
+static void closed_box() {
+  const int nx = 4, ny = 4, nz = 8;
+  g::Grid grid(nx, ny, nz, 2.0, 1.0, 0.05);
+  g::ReSolver re(grid);
+  g::ReParams p;
+  p.dx = 2.0;
+  p.dy = 1.0;
+  p.dz = 0.05;
+  p.botz = -0.05 * nz;
+  p.dt = 5.0;
+  p.adaptive_dt = 0;
+  p.use_corrector = 1;
+  p.use_full3d = 1;
+  for (int q = 0; q < 6; ++q) p.bc_type[q] = 0;
+  p.soil.alpha = 2.0;
+  p.soil.n = 1.6;
+  p.soil.theta_s = 0.45;
+  p.soil.theta_r = 0.05;
+  p.soil.Ks_x = p.soil.Ks_y = p.soil.Ks_z = 1.0e-5;
+  p.soil.Ss = 0.0;
+  re.setParams(p);
+  g::SolverConfig cfg;
+  cfg.rtol = 1e-13;
+  auto ls = g::makeLinearSolver("gb300", cfg);
+  g::Decomp3D dd(nx, ny, nz);
+  re.attachSolver(*ls, dd);
+  re.initializeGeometry();
+  std::vector<double> wc((size_t)nx * ny * nz);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        wc[i + nx * (j + ny * k)] = 0.20 + 0.03 * std::sin(0.9 * i) + 0.02 * std::cos(0.7 * j);
+  re.setInitialWaterContent(wc);
+  re.finalizeInitialState();
+  const double v0 = re.waterVolume();
+  for (int s = 0; s < 40; ++s) re.advanceStep();
+  const double v1 = re.waterVolume();
+  const double rel = std::fabs(v1 - v0) / v0;
+  EXPECT(rel < 1e-10, "ReSolver closed box: water volume drift %.3e relative over 40 steps", rel);
+  const std::vector<double> h = re.fields().h();
+  EXPECT((long)h.size() == grid.nCell(), "fields().h() in the halo layout (%zu values)",
+         h.size());
+  EXPECT(std::isfinite(h[grid.getIndex(1, 2, 3)]) && re.dtUsed() == 5.0,
+         "fields() readable, dtUsed %.1f", re.dtUsed());
+}
+
+int main() {
+  try {
+    seam("fp64");
+    seam("mixed");
+    errors();
+    closed_box();
+  } catch (const std::exception& e) {
+    std::printf("FAIL unexpected exception: %s\n", e.what());
+    return 2;
+  }
+  if (failures == 0) std::printf("ALL OK\n");
+  return failures == 0 ? 0 : 1;
+}
