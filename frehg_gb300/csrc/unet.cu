@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -240,15 +241,19 @@ __global__ void k_pool_bwd_add(const bf16* __restrict__ gout, bf16* __restrict__
 // nearest 2x upsampling of a coarse field (stride c) into a channel slice of a fine buffer
 __global__ void k_up(const bf16* __restrict__ in, bf16* __restrict__ out, int out_stride,
                      int out_off, int c, int nx, int ny, int nz) {
-  const size_t n = (size_t)nx * ny * nz;
-  const int cx = nx / 2, cy = ny / 2;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n * c;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const size_t p = e / c;
-    const int ch = (int)(e % c);
-    const int x = (int)(p % nx), y = (int)((p / nx) % ny), z = (int)(p / ((size_t)nx * ny));
-    const size_t q = (size_t)(x / 2) + (size_t)cx * ((size_t)(y / 2) + (size_t)cy * (z / 2));
-    out[p * out_stride + out_off + ch] = in[q * c + ch];
+  // one thread per fine cell and group of 8 channels (16-byte copies); c, out_stride and
+  // out_off are multiples of 8.  Cell counts of the network's grids stay below 2^32.
+  const uint32_t n = (uint32_t)nx * ny * nz;
+  const uint32_t g = (uint32_t)c / 8;
+  const uint32_t cx = nx / 2, cy = ny / 2;
+  const uint64_t tot = (uint64_t)n * g;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < tot;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = (uint32_t)(e / g), cg = (uint32_t)(e - (uint64_t)p * g);
+    const uint32_t x = p % nx, yz = p / nx, y = yz % ny, z = yz / ny;
+    const uint32_t q = (x >> 1) + cx * ((y >> 1) + cy * (z >> 1));
+    const uint4 v = *reinterpret_cast<const uint4*>(in + (size_t)q * c + 8 * cg);
+    *reinterpret_cast<uint4*>(out + (size_t)p * out_stride + out_off + 8 * cg) = v;
   }
 }
 
@@ -287,11 +292,29 @@ __global__ void k_pack_input(const float* __restrict__ r, const float* __restric
   }
 }
 
-// 1 / rms of r (zero -> 1); one block
-__global__ void k_rms_scale(const float* __restrict__ r, size_t n, float* __restrict__ scale,
-                            float* __restrict__ inv) {
+// 1 / rms of r (zero -> 1) in two deterministic passes: per-block partial sums of r^2, then one
+// block adds the partials in a fixed order.
+constexpr int kRmsBlocks = 1024;
+__global__ void k_rms_partial(const float* __restrict__ r, size_t n, double* __restrict__ part) {
   double s = 0.0;
-  for (size_t p = threadIdx.x; p < n; p += blockDim.x) s += (double)r[p] * r[p];
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n;
+       p += (size_t)gridDim.x * blockDim.x)
+    s += (double)r[p] * r[p];
+  __shared__ double sh[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_rms_scale(const double* __restrict__ part, int nparts, size_t n,
+                            float* __restrict__ scale, float* __restrict__ inv) {
+  double s = 0.0;
+  for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += part[q];
   __shared__ double sh[32];
   s = warp_sum(s);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
@@ -463,6 +486,7 @@ struct frehg_unet {
   bf16 *g_e3 = nullptr, *g_a3 = nullptr, *g_p2 = nullptr;
   float* y = nullptr;
   float* scal = nullptr;  // [0] 1/rms(r), [1] rms(r)
+  double* rms_part = nullptr;  // per-block partial sums of r^2
   double* loss = nullptr;
   std::vector<void*> bufs;
   ~frehg_unet() {
@@ -475,6 +499,7 @@ struct frehg_unet {
     cudaFree(wb);
     cudaFree(wt);
     cudaFree(scal);
+    cudaFree(rms_part);
     cudaFree(loss);
   }
 };
@@ -561,7 +586,11 @@ int forward(frehg_unet* net, const float* r, const float* lnk, const float* cap,
   const size_t n1 = (size_t)nx * ny * nz, n2 = n1 / 8, n3 = n1 / 64;
   const float* M = net->master;
   const bf16* W = net->wb;
-  k_rms_scale<<<1, 1024, 0, st>>>(r, n1, net->scal, net->scal + 1);
+  {
+    const int nb = (int)std::min<size_t>((n1 + 255) / 256, (size_t)kRmsBlocks);
+    k_rms_partial<<<nb, 256, 0, st>>>(r, n1, net->rms_part);
+    k_rms_scale<<<1, 256, 0, st>>>(net->rms_part, nb, n1, net->scal, net->scal + 1);
+  }
   k_pack_input<<<blocks_for(n1), 256, 0, st>>>(r, lnk, cap, net->scal, net->kmean, net->kscale,
                                                net->cscale, net->x0, n1);
   conv<16, 16>(net->x0, 16, 0, W + net->wboff[0], M + net->boff[0], net->a1, 16, 0, nx, ny, nz, true, st);
@@ -715,6 +744,7 @@ int frehg_unet_create(uint64_t seed, frehg_unet** out) {
       cudaMalloc(&net->m, off * 4) || cudaMalloc(&net->v, off * 4) ||
       cudaMalloc(&net->frozen, off) || cudaMalloc(&net->wb, boff * 2) ||
       cudaMalloc(&net->wt, boff * 2) || cudaMalloc(&net->scal, 2 * sizeof(float)) ||
+      cudaMalloc(&net->rms_part, kRmsBlocks * sizeof(double)) ||
       cudaMalloc(&net->loss, sizeof(double)))
     return fail("device allocation");
   cudaMemcpy(net->master, h.data(), off * 4, cudaMemcpyHostToDevice);
