@@ -63,7 +63,10 @@ def parse():
                     help="relative reduction of each FP32 inner solve (mixed precision)")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain FP64 arm (comparison and head error)")
-    ap.add_argument("--unet-weights", default=None, help="trained network (.npz, learned.py)")
+    ap.add_argument("--unet-weights", default=None,
+                    help="trained network (.npz written by python -m frehg_gb300.learned); "
+                         "default: the committed layered-soil network when it exists, else "
+                         "a bounded training run before the timed steps")
     ap.add_argument("--train-steps", type=int, default=300)
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -198,12 +201,14 @@ def measured_peaks():
 
 
 def ncu_traffic(kernel):
-    """DRAM bytes per cell of `kernel` from the committed ncu summary (profiles/), or None."""
+    """(DRAM bytes per cell, limiter) of `kernel` from the committed ncu summary (profiles/)"""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p):
-        return None
-    d = json.load(open(p))
-    return d.get(kernel)
+        return None, None
+    v = json.load(open(p)).get(kernel)
+    if isinstance(v, dict):
+        return v.get("dram_bytes_per_cell"), v.get("limiter")
+    return v, None
 
 
 def scheme_name(args):
@@ -279,9 +284,17 @@ def trained_net(args):
     timed region) on pairs from plain solves of seeded three-layer soils at 64x64x32."""
     from frehg_gb300 import learned as Lr
     net = Lr.UNet(0)
-    if args.unet_weights:
-        net.load(args.unet_weights)
-        return net, {"weights": os.path.basename(args.unet_weights)}
+    path = args.unet_weights or (Lr.DEFAULT_WEIGHTS if os.path.exists(Lr.DEFAULT_WEIGHTS)
+                                 else None)
+    if path:
+        net.load(path)
+        info = {"weights": os.path.relpath(path, ROOT)}
+        try:
+            import numpy as np
+            info.update(json.loads(str(np.load(path)["info"])))
+        except Exception:
+            pass
+        return net, info
     t0 = time.perf_counter()
     seeds = list(range(100, 100 + args.train_seeds))
     data = Lr.generate_pairs(seeds, 64, 64, 32, snapshots=(0, 2), iters=(0, 2, 5, 10, 20, 40),
@@ -422,10 +435,10 @@ def run_gpu(args):
     per_launch_ms = dom["total_ms"] / dom["launches"]
     achieved = dom["bytes_per_launch"] / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
-    tr = ncu_traffic(dom["name"])
+    tr, limiter = ncu_traffic(dom["name"])
     roofline = {
         "bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "peak_source": peak_kind,
+        "frac": achieved / peak, "peak_source": peak_kind, "limiter": limiter,
         "traffic": None if tr is None else tr * w.cells,
         "bytes_per_launch": dom["bytes_per_launch"], "ms_per_launch": per_launch_ms,
         "share_of_step": dom["total_ms"] / tot,

@@ -186,6 +186,7 @@ class KrylovSolver {
   // graphs
   cudaGraphExec_t g64 = nullptr;
   cudaGraphExec_t g32 = nullptr;
+  cudaGraphExec_t g32s = nullptr;  // first, short chunk of the inner solve
   const void* g64_key = nullptr;
   const void* g64_key2 = nullptr;
   Profiler* prof = nullptr;  // owner's profiler (launch counts, optional event timing)

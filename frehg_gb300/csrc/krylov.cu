@@ -355,6 +355,7 @@ void Stencil32::release() {
 KrylovSolver::~KrylovSolver() {
   if (g64) cudaGraphExecDestroy(g64);
   if (g32) cudaGraphExecDestroy(g32);
+  if (g32s) cudaGraphExecDestroy(g32s);
   cudaFree(x);
   cudaFree(r);
   cudaFree(p);

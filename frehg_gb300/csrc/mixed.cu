@@ -460,6 +460,10 @@ int KrylovSolver::ensure32(size_t n) {
     cudaGraphExecDestroy(g32);
     g32 = nullptr;
   }
+  if (g32s) {
+    cudaGraphExecDestroy(g32s);
+    g32s = nullptr;
+  }
   FG_CUDA(cudaMalloc(&xf, n * sizeof(float)));
   FG_CUDA(cudaMalloc(&rf, n * sizeof(float)));
   FG_CUDA(cudaMalloc(&pf, n * sizeof(float)));
@@ -621,14 +625,17 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       k32_spmv<<<L.grid, L.block, 0, s>>>(op32.a0, op32.a1, op32.a2, pf, wf, A.n0, A.n1, A.n2,
                                           L.planes, L.tiles, dst32, partials);
   };
-  if (!(prof && prof->on) && rebuild) {
-    if (g32) cudaGraphExecDestroy(g32);
-    g32 = nullptr;
+  // inner iterations run as CUDA graphs: a first chunk of 4 (easy systems converge in a few),
+  // then chunks of 32; iterations after convergence return at once
+  const int chunk0 = 4;
+  auto capture = [&](int iters, cudaGraphExec_t* out) -> int {
+    if (*out) cudaGraphExecDestroy(*out);
+    *out = nullptr;
     cudaStream_t cap_st;
     FG_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
     cudaGraph_t graph;
     FG_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
-    for (int q = 0; q < chunk; ++q) {
+    for (int q = 0; q < iters; ++q) {
       if (line) {
         spmv32(cap_st);
         k32_line_fwd<true><<<lb, 128, 0, cap_st>>>(xf, rf, pf, wf, lkf, dinvf, uf, ncol, nzl,
@@ -646,12 +653,17 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       set_error("graph capture failed: %s", cudaGetErrorString(e));
       return FREHG_ERR_CUDA;
     }
-    e = cudaGraphInstantiate(&g32, graph, 0);
+    e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
       set_error("graph instantiate failed: %s", cudaGetErrorString(e));
       return FREHG_ERR_CUDA;
     }
+    return FREHG_OK;
+  };
+  if (!(prof && prof->on) && rebuild) {
+    FG_TRY(capture(chunk, &g32));
+    FG_TRY(capture(chunk0, &g32s));
     g32_key = op32.a0;
     g_stream32 = st;
     g_n32 = n;
@@ -724,8 +736,9 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       FG_CUDA(cudaGetLastError());
     }
     for (int q = 0; !use_net && q < cfg.max_it / chunk + 2 && hst32->status == 0; ++q) {
+      const int iters = q == 0 ? chunk0 : chunk;
       if (prof && prof->on) {
-        for (int it = 0; it < chunk; ++it) {
+        for (int it = 0; it < iters; ++it) {
           if (line) {
             FG_LAUNCH(prof, st, vec4 ? "k32_spmv_v4" : "k32_spmv", 20.0 * dn, spmv32(st));
             FG_LAUNCH(prof, st, "k32_line_fwd", 36.0 * dn,
@@ -743,8 +756,8 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
         }
         FG_CUDA(cudaGetLastError());
       } else {
-        FG_CUDA(cudaGraphLaunch(g32, st));
-        if (prof) prof->launches += 3 * chunk;
+        FG_CUDA(cudaGraphLaunch(q == 0 ? g32s : g32, st));
+        if (prof) prof->launches += 3 * iters;
       }
       FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
       FG_CUDA(cudaStreamSynchronize(st));
