@@ -10,6 +10,8 @@
 
 #include <cstdint>
 
+#include "fastmath64.cuh"
+
 namespace fg {
 
 // One soil class with the constants the relations reuse precomputed (same values the
@@ -107,8 +109,8 @@ __device__ __forceinline__ double vg_head(const CellSoil& s, double wc) {
     if (theta - s.thr < eps) theta = s.thr + eps;
     if (theta < s.ths) {
       const double q = (wcm_val - s.thr) / (theta - s.thr);
-      const double x = expm1(s.inv_m * log(q));
-      return -(1.0 / s.alpha) * exp(s.inv_n * log(x));
+      const double x = fexpm1(s.inv_m * flog(q));
+      return -(1.0 / s.alpha) * fexp(s.inv_n * flog(x));
     }
     return 0.0;
   }
@@ -162,7 +164,8 @@ __device__ __forceinline__ double vg_kr(const CellSoil& s, double h) {
 //   C = alpha n m (ths - thr) |alpha h|^{n-1} (1+t)^{-(m+1)} = alpha n m (ths-thr) t se / (|alpha h| (1+t)).
 // The same relations as the reference's pow() forms (VanGenuchten.hpp:31-111), evaluated with
 // 2 logarithms, 2 exponentials and one expm1 instead of 11 pow() calls (se = e^{-mu/2}
-// squared); 1 - e^{x} is formed as -expm1(x) so no digits cancel when the soil is dry.  The caps and the saturated branches are the
+// squared); 1 - e^{x} is formed as -expm1(x) so no digits cancel when the soil is dry.  The
+// elementary functions are the table-driven ones of fastmath64.cuh (fewer FP64 instructions).  The caps and the saturated branches are the
 // reference's.  MVG and the exponential model use the reference forms above.
 struct Constit {
   double kr, theta, cap;
@@ -179,14 +182,14 @@ __device__ __forceinline__ Constit vg_constit(const CellSoil& s, double h) {
   }
   const double mm = s.m;
   const double ah = fabs(s.alpha * h);
-  const double L = log(ah);
+  const double L = flog(ah);
   const double nL = s.n * L;
-  const double t = exp(nL);
-  const double u = log1p(t);
+  const double t = fexp(nL);
+  const double u = flog1p(t);
   const double mu = mm * u;
   // kr; se = e^{-mu} = (e^{-mu/2})^2 serves theta
-  const double one_minus = -expm1(mm * (nL - u));
-  const double se_half = exp(-0.5 * mu);
+  const double one_minus = -fexpm1(mm * (nL - u));
+  const double se_half = fexp(-0.5 * mu);
   double kr = se_half * (one_minus * one_minus);
   if (kr > 1.0) kr = 1.0;
   if (h > 0.0) kr = 1.0;

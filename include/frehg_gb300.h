@@ -346,6 +346,11 @@ int frehg_cg_solve_noalloc(int nx, int ny, int nz, const double* diag, const dou
 /* Build information: returns the sm architecture the library was compiled for (e.g. 103). */
 int frehg_build_arch(void);
 
+/* Self-check of the library's FP64 elementary functions (not in reference): y[i] = f(x[i]) for
+ * host arrays of n values, f = the library's exp, log, log1p, expm1 (fn 0-3) as used by the
+ * constitutive kernels, or the CUDA math library's (fn 4-7) for comparison. */
+int frehg_fastmath_eval(int fn, const double* x, double* y, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif
