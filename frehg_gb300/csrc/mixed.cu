@@ -26,10 +26,13 @@ namespace fg {
 // r~ = s b - A~ x~ (FP64, kept in rres); e = 0; sums of r~^2 (scale of the inner system),
 // (r~/s)^2 = (sq r~)^2 for the true residual (sq = D^1/2) and b^2 for ||b||.  The last block
 // runs the refinement test.
+// FIRST (the first sweep, x~ = 0): r~ = s b without the stencil product, x~ written as 0, and
+// the b^2 sum that ||b|| needs; later sweeps skip that sum.
+template <bool FIRST>
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ s, const double* __restrict__ sq, const double* __restrict__ b,
-    const double* __restrict__ x, double* __restrict__ rres, float* __restrict__ ef, int n0,
+    double* __restrict__ x, double* __restrict__ rres, float* __restrict__ ef, int n0,
     int n1, int n2, int planes, int tiles, CgDevState* ir, double* partials, double ir_rtol) {
   if (ir->status) return;
   const int t0 = (n0 + 31) / 32;
@@ -42,13 +45,18 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     const int kb = blockIdx.y * planes, ke = min(n2, kb + planes);
     size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
     for (int k = kb; k < ke; ++k, c += s01) {
-      double ax = x[c];
-      if (i0 > 0) ax = fma(a0[c - 1], x[c - 1], ax);
-      if (i0 + 1 < n0) ax = fma(a0[c], x[c + 1], ax);
-      if (i1 > 0) ax = fma(a1[c - n0], x[c - n0], ax);
-      if (i1 + 1 < n1) ax = fma(a1[c], x[c + n0], ax);
-      if (k > 0) ax = fma(a2[c - s01], x[c - s01], ax);
-      if (k + 1 < n2) ax = fma(a2[c], x[c + s01], ax);
+      double ax = 0.0;
+      if (FIRST) {
+        x[c] = 0.0;
+      } else {
+        ax = x[c];
+        if (i0 > 0) ax = fma(a0[c - 1], x[c - 1], ax);
+        if (i0 + 1 < n0) ax = fma(a0[c], x[c + 1], ax);
+        if (i1 > 0) ax = fma(a1[c - n0], x[c - n0], ax);
+        if (i1 + 1 < n1) ax = fma(a1[c], x[c + n0], ax);
+        if (k > 0) ax = fma(a2[c - s01], x[c - s01], ax);
+        if (k + 1 < n2) ax = fma(a2[c], x[c + s01], ax);
+      }
       const double sc = s[c], bc = b[c];
       const double r = fma(sc, bc, -ax);
       rres[c] = r;
@@ -56,7 +64,7 @@ __global__ void __launch_bounds__(256) k_ir_residual(
       v[0] = fma(r, r, v[0]);
       const double ru = r * sq[c];  // r~ / s = D^1/2 r~
       v[1] = fma(ru, ru, v[1]);
-      v[2] = fma(bc, bc, v[2]);
+      if (FIRST) v[2] = fma(bc, bc, v[2]);
     }
   }
   double tot[3];
@@ -599,7 +607,6 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
   const bool vec4 = (A.n0 % 4) == 0 && getenv("FREHG_NO_VEC4") == nullptr;
   const StencilLaunch L4 = launch_v4(A.n0, A.n1, A.n2);
-  FG_LAUNCH(prof, st, "k_zero64", 8.0 * dn, k_zero64<<<nb, 256, 0, st>>>(x, n));
   FG_CUDA(cudaGetLastError());
   // inner preconditioner: Jacobi (unit diagonal, z = r) or vertical lines
   const bool line = !strcmp(cfg.pc_type, "line");
@@ -676,10 +683,16 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   bool fcg_fallback = false;
   const bool dbg = getenv("FREHG_DEBUG_IR") != nullptr;
   for (;;) {
-    FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
-              k_ir_residual<<<L.grid, L.block, 0, st>>>(
-                  A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
-                  L.tiles, dst, partials, cfg.ir_rtol));
+    if (sweeps == 0)
+      FG_LAUNCH(prof, st, "k_ir_residual0", 40.0 * dn,
+                k_ir_residual<true><<<L.grid, L.block, 0, st>>>(
+                    A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                    L.tiles, dst, partials, cfg.ir_rtol));
+    else
+      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
+                k_ir_residual<false><<<L.grid, L.block, 0, st>>>(
+                    A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                    L.tiles, dst, partials, cfg.ir_rtol));
     FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
               k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials, cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());

@@ -874,6 +874,16 @@ int frehg_re_finalize_initial_state(frehg_re* re) {
   FG_CUDA(cudaStreamSynchronize(re->stream));
   // dtn_ = params_.dt (ReSolver.cpp:175-178)
   FG_CUDA(cudaMemcpy(&re->sc->dtn, &re->sc->dt, sizeof(double), cudaMemcpyDeviceToDevice));
+  // a finalized initial state starts a run, also on a handle that has stepped before: ghost
+  // values as freshly allocated (zero until the first step writes them), simulated time and
+  // the boundary / elastic budgets at zero
+  FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
+  re->sc_host->time = 0.0;
+  re->sc_host->vol_top = 0.0;
+  re->sc_host->vol_bot = 0.0;
+  re->sc_host->vol_elastic = 0.0;
+  FG_CUDA(cudaMemcpy(re->sc, re->sc_host, sizeof(ReScalars), cudaMemcpyHostToDevice));
+  re->ghosts_valid = false;
   re->finalized = true;
   return FREHG_OK;
 }

@@ -150,7 +150,9 @@ int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg);
 
 /* ReSolver::initializeGeometry / setInitialWaterContent / setInitialHead /
  * finalizeInitialState / initializeUniformColumn (ReSolver.hpp:73-79, ReSolver.cpp:104-188).
- * Host arrays, interior order. */
+ * Host arrays, interior order.  finalize starts a run: on a handle that has stepped before,
+ * the ghost values (zero until the first step writes them), the simulated time and the boundary
+ * budgets restart as on a fresh handle, so a re-initialised handle steps like a new one. */
 int frehg_re_initialize_geometry(frehg_re* re);
 int frehg_re_set_initial_head(frehg_re* re, const double* h);
 int frehg_re_set_initial_water_content(frehg_re* re, const double* wc);

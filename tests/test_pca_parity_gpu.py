@@ -116,3 +116,23 @@ def test_first_step_bottom_dirichlet_quirk(gpu_lib, oracle_mod):
     w = W.config1("pca", nx=8, ny=8, nz=16, steps=3)
     g, o = pair(w, oracle_mod)
     step_compare(g, o, w.steps)
+
+
+def test_reinitialised_handle_steps_like_a_fresh_one(gpu_lib):
+    """Stepping, then setting the initial state again, reproduces a fresh handle's run (the
+    first step's zero ghosts included)."""
+    from frehg_gb300.re_solver import Grid, ReSolver
+    w = W.config1("pca", nx=16, ny=12, nz=24, steps=3)
+    grid = Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz)
+    fresh, reused = ReSolver(grid, w.params), ReSolver(grid, w.params)
+    w.apply(fresh)
+    w.apply(reused)
+    for _ in range(2):
+        reused.advance_step()
+    reused.set_params(w.params)
+    w.apply(reused)
+    for _ in range(w.steps):
+        fresh.advance_step()
+        reused.advance_step()
+        assert np.array_equal(fresh.interior("h"), reused.interior("h"))
+    assert fresh.time() == reused.time()
