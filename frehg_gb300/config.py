@@ -17,7 +17,8 @@ Keys read (reference names; "not in reference" marks the extensions):
   (Orchestrator.cpp:487-490); solver.backend (must be "gb300" here);
   soil.types[]{theta_s, theta_r, vg{alpha, n}, k_sat{x, y, z}, specific_storage, use_vg,
                use_mvg, air_entry_value}, soil.map.{from_file, file, layers, format};
-  initial_conditions.groundwater.{h | wc} (uniform values).
+  initial_conditions.groundwater.{h | wc} (uniform values);
+  groundwater.recharge.{rate, polygon} and domain.{x0, y0} (partial-width top recharge).
 """
 from __future__ import annotations
 
@@ -372,6 +373,49 @@ def soil_map(cfg, nx, ny, nz, base_dir):
     return m
 
 
+def polygon_contains(vertices, x, y):
+    """Even-odd ray casting (a +x ray from each point counts edge crossings; the ring closes
+    itself), with a bounding-box reject: the membership rule of the reference's polygon regions
+    (src/bc/Polygon.hpp:27-55).  x, y: arrays of points; returns a boolean array."""
+    import numpy as np
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    inside = np.zeros(np.broadcast(x, y).shape, dtype=bool)
+    v = [(float(a), float(b)) for a, b in vertices]
+    if len(v) < 3:
+        return inside
+    xs, ys = [p[0] for p in v], [p[1] for p in v]
+    box = (x >= min(xs)) & (x <= max(xs)) & (y >= min(ys)) & (y <= max(ys))
+    for q in range(len(v)):
+        xi, yi = v[q]
+        xj, yj = v[q - 1]
+        straddles = (yi > y) != (yj > y)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            x_cross = xj + (y - yj) * (xi - xj) / (yi - yj)
+        inside ^= straddles & (x < x_cross)
+    return inside & box
+
+
+def recharge_field(cfg, nx, ny, dx, dy):
+    """Orchestrator::buildRecharge (src/driver/Orchestrator.cpp:593-628): groundwater.recharge
+    {rate, polygon}: columns whose centre (x0 + (i + 1/2) dx, y0 + (j + 1/2) dy) lies inside the
+    ring get the rate [m/s, < 0 downward], the others 0; no ring (< 3 vertices) = the whole top.
+    Returns the per-column top flux (index i + j*nx), or None without the section."""
+    import numpy as np
+    rech = get(cfg, "groundwater.recharge", None)
+    if not isinstance(rech, dict):
+        return None
+    rate = float(rech.get("rate", 0.0) or 0.0)
+    verts = [p for p in (rech.get("polygon") or []) if isinstance(p, list) and len(p) >= 2]
+    x0 = float(get(cfg, "domain.x0", 0.0))
+    y0 = float(get(cfg, "domain.y0", 0.0))
+    xc = x0 + (np.arange(nx) + 0.5) * dx
+    yc = y0 + (np.arange(ny) + 0.5) * dy
+    X, Y = np.meshgrid(xc, yc)  # (ny, nx): index i + j*nx when raveled
+    inside = np.ones_like(X, dtype=bool) if len(verts) < 3 else polygon_contains(verts, X, Y)
+    return np.where(inside, rate, 0.0).ravel()
+
+
 def build_groundwater(cfg, base_dir="."):
     """Validate, then build and initialise a GPU ReSolver from a parsed v2 config."""
     import numpy as np
@@ -383,6 +427,9 @@ def build_groundwater(cfg, base_dir="."):
     m = soil_map(cfg, nx, ny, nz, base_dir)
     if m is not None:
         s.set_soil_map(m)
+    q = recharge_field(cfg, nx, ny, p.dx, p.dy)
+    if q is not None:
+        s.set_top_flux_field(q)
     s.initialize_geometry()
     # setupInitialConditions / applyInitialConditions (src/ic/ICConfig.cpp:121-124,
     # src/ic/ICApply.cpp:211-224): a spatial head field wins, otherwise the (constant) water

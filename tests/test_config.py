@@ -176,3 +176,24 @@ def test_yaml_column_matches_oracle(gpu_lib, oracle_mod):
         dh = np.abs(g.interior("h") - o.interior("h")).max()
         assert dh <= 1e-8, f"step {s}: head differs by {dh:.3e} m"
         assert abs(g.dt() - o.dt()) <= 1e-12 * o.dt()
+
+
+def test_recharge_polygon():
+    """groundwater.recharge: columns whose centre lies in the ring get the rate (even-odd rule,
+    concave ring), the rest 0; without a ring the whole top gets it."""
+    d = cf.load_yaml_text(COLUMN)
+    # L-shaped ring on a 6 x 4 grid of 1 m columns: the notch [3,6] x [2,4] is outside
+    d["groundwater"]["recharge"] = {"rate": -1e-6,
+                                    "polygon": [[0, 0], [6, 0], [6, 2], [3, 2], [3, 4], [0, 4]]}
+    q = cf.recharge_field(d, 6, 4, 1.0, 1.0).reshape(4, 6)
+    expect = np.zeros((4, 6))
+    expect[:2, :] = -1e-6
+    expect[2:, :3] = -1e-6
+    assert np.array_equal(q, expect)
+    d["domain"]["x0"] = 2.0  # shifted origin moves the columns, not the ring
+    q = cf.recharge_field(d, 6, 4, 1.0, 1.0).reshape(4, 6)
+    assert np.array_equal(q[:, 4:], np.zeros((4, 2)))
+    d["groundwater"]["recharge"] = {"rate": 2e-7}
+    assert np.all(cf.recharge_field(d, 6, 4, 1.0, 1.0) == 2e-7)
+    del d["groundwater"]["recharge"]
+    assert cf.recharge_field(d, 6, 4, 1.0, 1.0) is None
