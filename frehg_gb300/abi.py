@@ -261,6 +261,8 @@ SIGNATURES = {
     "frehg_re_set_learned_policy": (C.c_int, [_VP, C.c_int, C.c_double]),
     "frehg_re_training_pairs": (C.c_int, [_VP, C.c_int, _PI, C.c_int, _VP, _VP, _VP, _VP]),
     "frehg_build_arch": (C.c_int, []),
+    "frehg_re_checkpoint": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "frehg_re_restart": (C.c_int, [_VP, _VP, _VP, _VP]),
     "frehg_fastmath_eval": (C.c_int, [C.c_int, _VP, _VP, C.c_int64]),
 }
 

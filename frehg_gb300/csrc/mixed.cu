@@ -537,8 +537,11 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
         if (k > 0) {
           l = aprev * inv_d;
           double d = 1.0 - l * aprev;
-          if (!(d > 0.0)) d = 1.0;  // not SPD: that row falls back to the Jacobi step
-          inv_d = 1.0 / d;
+          if (!(d > 1e-30)) d = 1.0;  // not SPD: that row falls back to the Jacobi step
+          // 1/d from the FP32 reciprocal and one Newton step (relative error ~1e-14; the
+          // factors are stored in FP32)
+          const double y = (double)__frcp_rn((float)d);
+          inv_d = y * fma(-d, y, 2.0);
         }
         lk[c] = (float)l;
         dinv[c] = (float)inv_d;

@@ -963,6 +963,46 @@ int frehg_re_prime_adaptive_dt(frehg_re* re, double dt) {
   return FREHG_OK;
 }
 
+int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state) {
+  clear_error();
+  FG_ARG(re && h && wc && state, "null argument");
+  FG_ARG(re->finalized, "checkpoint of a handle without a finalized state");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(h, re->H[re->cur], re->n * sizeof(double), cudaMemcpyDeviceToHost));
+  FG_CUDA(cudaMemcpy(wc, re->W[re->cur], re->n * sizeof(double), cudaMemcpyDeviceToHost));
+  FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
+  const ReScalars& s = *re->sc_host;
+  const double v[FREHG_CHECKPOINT_SCALARS] = {s.time,    s.dt,      s.dtn,
+                                              s.dt_used, s.vol_top, s.vol_bot,
+                                              s.vol_elastic, re->ghosts_valid ? 1.0 : 0.0};
+  memcpy(state, v, sizeof(v));
+  return FREHG_OK;
+}
+
+int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const double* state) {
+  clear_error();
+  FG_ARG(re && h && wc && state, "null argument");
+  FG_ARG(state[1] > 0.0 && state[2] > 0.0, "checkpoint state has no positive dt");
+  FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_CUDA(cudaMemcpy(re->H[re->cur], h, re->n * sizeof(double), cudaMemcpyHostToDevice));
+  FG_CUDA(cudaMemcpy(re->W[re->cur], wc, re->n * sizeof(double), cudaMemcpyHostToDevice));
+  FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
+  ReScalars& s = *re->sc_host;
+  s.time = state[0];
+  s.dt = state[1];
+  s.dtn = state[2];  // primeAdaptiveDt's dtn_ (ReSolver.hpp:95-98)
+  s.dt_used = state[3];
+  s.vol_top = state[4];
+  s.vol_bot = state[5];
+  s.vol_elastic = state[6];
+  FG_CUDA(cudaMemcpy(re->sc, re->sc_host, sizeof(ReScalars), cudaMemcpyHostToDevice));
+  re->p.dt = state[1];
+  re->ghosts_valid = state[7] != 0.0;
+  re->have_state = true;
+  re->finalized = true;
+  return FREHG_OK;
+}
+
 // fill a halo array ((nx+2)(ny+2)(nz+2)) from an interior array; ghosts by the copy rule
 static void to_halo(const frehg_re* re, const std::vector<double>& in, double* out, bool copy_ghosts,
                     double top_ghost, bool top_fixed, double bot_ghost, bool bot_fixed) {

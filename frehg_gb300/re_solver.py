@@ -187,6 +187,21 @@ class ReSolver:
     def prime_adaptive_dt(self, dt):
         check(self._lib.frehg_re_prime_adaptive_dt(self._h, float(dt)), "primeAdaptiveDt")
 
+    def checkpoint(self) -> dict:
+        """The step state (h, wc in interior order, time, dt state, budgets, ghost flag)."""
+        n = self.grid.nx * self.grid.ny * self.grid.nz
+        h, wc, st = np.empty(n), np.empty(n), np.empty(8)
+        check(self._lib.frehg_re_checkpoint(self._h, dptr(h), dptr(wc), dptr(st)), "checkpoint")
+        return {"h": h, "wc": wc, "state": st}
+
+    def restart(self, cp: dict):
+        """Continue from a checkpoint: the parameters, soil, solver and top flux field are the
+        caller's (as a reference restart rebuilds them from the configuration)."""
+        h = np.ascontiguousarray(cp["h"], dtype=np.float64)
+        wc = np.ascontiguousarray(cp["wc"], dtype=np.float64)
+        st = np.ascontiguousarray(cp["state"], dtype=np.float64)
+        check(self._lib.frehg_re_restart(self._h, dptr(h), dptr(wc), dptr(st)), "restart")
+
     # -- outputs ---------------------------------------------------------------------------
     def field(self, name) -> np.ndarray:
         g = self.grid

@@ -345,6 +345,18 @@ int frehg_cg_solve_noalloc(int nx, int ny, int nz, const double* diag, const dou
                            const frehg_solver_config* cfg, void* stream, int* its,
                            double* rnorm);
 
+/* Checkpoint and restart of the step state (the groundwater part of writeCheckpointNow /
+ * loadCheckpointState, src/driver/Orchestrator.cpp:1461-1502, 688-747: the field state plus
+ * primeAdaptiveDt).  h and wc are host arrays of nx*ny*nz values in interior order (the only
+ * fields the next step reads; every other device array is recomputed by the step);
+ * state[FREHG_CHECKPOINT_SCALARS] = {time, dt, dtn, dt_used, top inflow volume, bottom inflow
+ * volume, elastic volume, ghosts written (1/0)}.  A handle with the same parameters, soil,
+ * solver and top flux field restarted from a checkpoint steps exactly like the run that wrote
+ * it (bit for bit). */
+#define FREHG_CHECKPOINT_SCALARS 8
+int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state);
+int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const double* state);
+
 /* Build information: returns the sm architecture the library was compiled for (e.g. 103). */
 int frehg_build_arch(void);
 

@@ -347,6 +347,24 @@ class ReSolver {
     check(frehg_re_water_volume(re_, &v), "waterVolume");
     return v;
   }
+  // checkpoint / restart of the step state (writeCheckpointNow / loadCheckpointState)
+  struct Checkpoint {
+    std::vector<real> h, wc;
+    double state[FREHG_CHECKPOINT_SCALARS];
+  };
+  Checkpoint checkpoint() const {
+    Checkpoint cp;
+    cp.h.resize((size_t)grid_.nx * grid_.ny * grid_.nz);
+    cp.wc.resize(cp.h.size());
+    check(frehg_re_checkpoint(re_, cp.h.data(), cp.wc.data(), cp.state), "checkpoint");
+    return cp;
+  }
+  void restart(const Checkpoint& cp) {
+    size_check(cp.h.size(), "restart");
+    size_check(cp.wc.size(), "restart");
+    check(frehg_re_restart(re_, cp.h.data(), cp.wc.data(), cp.state), "restart");
+    params_.dt = cp.state[1];
+  }
   frehg_re_counters counters() const {
     frehg_re_counters c;
     check(frehg_re_get_counters(re_, &c), "counters");

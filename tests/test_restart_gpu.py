@@ -1,0 +1,55 @@
+"""Checkpoint / restart of the GPU step state (the groundwater part of the reference's
+writeCheckpointNow / loadCheckpointState with primeAdaptiveDt): a new handle restarted from a
+checkpoint continues exactly like the run that wrote it (heads, water contents, dt sequence and
+time bit for bit) — the reference's restart-equals-continuous gate."""
+import numpy as np
+import pytest
+
+from frehg_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def new(w):
+    from frehg_gb300.re_solver import Grid, ReSolver
+    g = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
+    w.apply(g)
+    return g
+
+
+def continuous_vs_restart(w, before, after, column=False):
+    a = new(w)
+    if column:
+        a.initialize_uniform_column(0.033)
+    for _ in range(before):
+        a.advance_step()
+    cp = a.checkpoint()
+    b = new(w)
+    if column:
+        b.initialize_uniform_column(0.5)  # a different start, overwritten by the restart
+    b.restart(cp)
+    for s in range(after):
+        a.advance_step()
+        b.advance_step()
+        assert np.array_equal(a.interior("h"), b.interior("h")), f"step {s}"
+        assert np.array_equal(a.interior("wc"), b.interior("wc")), f"step {s}"
+        assert a.dt() == b.dt() and a.time() == b.time()
+    assert a.boundary_volumes() == b.boundary_volumes()
+
+
+def test_restart_pca_adaptive_column(gpu_lib):
+    """b2-gw column, adaptive dt: 40 steps, checkpoint, 30 more"""
+    continuous_vs_restart(W.b2gw_column(pc="jacobi", rtol=1e-10), 40, 30, column=True)
+
+
+def test_restart_pca_3d(gpu_lib):
+    """heterogeneous 3D box with top flux and bottom Dirichlet (ghost rules after step 1)"""
+    continuous_vs_restart(W.config1("pca", nx=16, ny=12, nz=24, steps=6), 3, 3)
+
+
+def test_restart_picard_rain_mixed(gpu_lib):
+    """combined workload's physics on a window, mixed precision with the line solve: dt from
+    the Picard count, rain stopping after the checkpoint"""
+    w = W.config4(nx=16, ny=12, nz=96, steps=20, precision=1, pc="line")
+    w.params.rain_until = 200.0
+    continuous_vs_restart(w, 10, 10)
