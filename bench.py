@@ -200,6 +200,52 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        if d.get("bf16_tflops"):
+            return d["bf16_tflops"], "measured (burst)"
+    return 1900.0, "fallback (burst)"
+
+
+def network_roofline(net, w, stream):
+    """One forward application of the network on the workload's grid, timed with CUDA events
+    (mean of 3 after 2 warm-up applications) against the dense BF16 tensor peak."""
+    import torch
+    from frehg_gb300.abi import check, load_library
+    from frehg_gb300.learned import UNet
+    lib = load_library()
+    n = w.cells
+    g = torch.Generator(device="cuda").manual_seed(0)
+    r = torch.randn(n, device="cuda", generator=g)
+    lnk = torch.randn(n, device="cuda", generator=g)
+    cap = torch.rand(n, device="cuda", generator=g)
+    y = torch.empty(n, device="cuda")
+
+    def apply():
+        check(lib.frehg_unet_forward(net.handle, w.nx, w.ny, w.nz, r.data_ptr(), lnk.data_ptr(),
+                                     cap.data_ptr(), y.data_ptr(), stream.cuda_stream), "forward")
+
+    for _ in range(2):
+        apply()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(3):
+        apply()
+    e1.record(stream)
+    stream.synchronize()
+    ms = e0.elapsed_time(e1) / 3
+    flops = UNet.flops(w.nx, w.ny, w.nz)
+    peak, kind = measured_bf16_peak()
+    tf = flops / (ms / 1000.0) / 1e12
+    del r, lnk, cap, y
+    torch.cuda.empty_cache()
+    return {"bound": "tensor", "kernel": "U-Net forward (k_conv3, mma.sync BF16)",
+            "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+            "peak_source": kind, "ms_per_application": ms, "flop_per_application": flops}
+
+
 def ncu_traffic(kernel):
     """(DRAM bytes per cell, limiter) of `kernel` from the committed ncu summary (profiles/)"""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
@@ -450,6 +496,8 @@ def run_gpu(args):
                     for st in stats},
     }
 
+    net_roof = network_roofline(net, w, stream) if learned else None
+
     # the plain FP64 GPU path on the same inputs and steps: throughput and head error
     comparison = None
     if not args.no_compare and (args.precision != "fp64" or args.pc != "jacobi"):
@@ -501,6 +549,7 @@ def run_gpu(args):
                 "h2d_bytes_per_step": int(q_host.numel() * 8),
                 "d2h_bytes_per_step": int(h_host.numel() * 8 + wc_host.numel() * 8)},
         "roofline": roofline,
+        "roofline_network": net_roof,
         "cpu_baseline": cpu,
         "gpu_launches": int(cnt["kernel_launches"]),
         "clocks": clk,
