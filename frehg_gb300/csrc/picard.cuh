@@ -123,8 +123,11 @@ __device__ __forceinline__ PicRow pic_row(const ReArgs& a, const CellSoil& s, si
   return r;
 }
 
-// Linearised system of one Picard iteration (diagonal into dg, +x/+y/+z couplings, rhs).
-// Launched on (32 x 8)-column tiles marching through `planes` levels (no index divisions).
+// Linearised system of one Picard iteration (diagonal into dg, +x/+y/+z couplings, rhs), with
+// the same face values as pic_row but each x and z face evaluated once: a thread marches down
+// its column and carries the face below a level to the next level as that level's face above,
+// and takes a cell's -x face from the lane to its left (warp shuffle; lane 0 evaluates its own).
+// Launched on (32 x 8)-column tiles marching through `planes` levels: a warp is one tile row.
 __global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restrict__ dg,
                                                       double* __restrict__ a0,
                                                       double* __restrict__ a1,
@@ -133,28 +136,130 @@ __global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restri
                                                       int tiles) {
   const double dt = a.sc->dt_used;
   const double V = a.dx * a.dy * a.dz;
+  const double Az = a.dx * a.dy;
+  const int hm = a.face_mean;
   const int t0 = (a.nx + 31) / 32;
+  const int lane = threadIdx.x;
+  const unsigned full = 0xffffffffu;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-  const int i = (tile % t0) * 32 + threadIdx.x;
-  const int j = (tile / t0) * 8 + threadIdx.y;
-  if (i >= a.nx || j >= a.ny) continue;
-  const size_t col = (size_t)i + (size_t)a.nx * j;
-  const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
-  for (int k = kb; k < ke; ++k) {
-    const size_t c = col + a.ncol * k;
-    const CellSoil s = soil_of(a.soil, c, col);
-    const double hc = a.h_new[c];
-    const double wcn = a.w_old[c];
-    const double th = a.wch[c];  // theta(h^m) and C(h^m) from k_constit
-    const double C = a.cap[c];
-    const PicRow r = pic_row(a, s, c, col, i, j, k);
-    dg[c] = V * (C + s.Ss * wcn * s.inv_ths) + dt * r.tsum;
-    a0[c] = -dt * r.tx;
-    a1[c] = -dt * r.ty;
-    a2[c] = -dt * r.tz;
-    const double rdt = V * (th - wcn) + V * s.Ss * (wcn * s.inv_ths) * (hc - a.h_old[c]) - dt * r.q;
-    bvec[c] = -rdt;
-  }
+    const int i = (tile % t0) * 32 + lane;
+    const int j = (tile / t0) * 8 + threadIdx.y;
+    const bool act = i < a.nx && j < a.ny;
+    const size_t col = act ? (size_t)i + (size_t)a.nx * j : 0;
+    const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
+    // face above the current level: transmissibility and flux into the current cell
+    double tzm = 0.0, fzm = 0.0;
+    if (act && kb > 0) {
+      const size_t c = col + a.ncol * kb;
+      const CellSoil s0 = soil_of(a.soil, c, col);
+      const CellSoil sm = soil_of(a.soil, c - a.ncol, col);
+      const double kf = pic_mean(hm, sm.Ksz * a.kr[c - a.ncol], s0.Ksz * a.kr[c]);
+      tzm = kf * a.cz;
+      fzm = tzm * (a.h_new[c - a.ncol] - a.h_new[c]) + Az * kf;
+    }
+    for (int k = kb; k < ke; ++k) {
+      const size_t c = col + a.ncol * k;
+      CellSoil s;
+      double hc = 0.0, krc = 0.0, Kxc = 0.0;
+      if (act) {
+        s = soil_of(a.soil, c, col);
+        hc = a.h_new[c];
+        krc = a.kr[c];
+        Kxc = s.Ksx * krc;
+      }
+      // +x face, the neighbour's K and h from the next lane (lane 31 loads them)
+      double Kxn = __shfl_down_sync(full, Kxc, 1);
+      double hxn = __shfl_down_sync(full, hc, 1);
+      double tx = 0.0, fxp = 0.0;
+      if (act && i + 1 < a.nx) {
+        if (lane == 31) {
+          const CellSoil sp = soil_of(a.soil, c + 1, col + 1);
+          Kxn = sp.Ksx * a.kr[c + 1];
+          hxn = a.h_new[c + 1];
+        }
+        tx = pic_mean(hm, Kxc, Kxn) * a.cx;
+        fxp = tx * (hxn - hc);
+      }
+      // -x face: the +x face of the previous lane (lane 0 evaluates it)
+      double txm = __shfl_up_sync(full, tx, 1);
+      double fxm = -__shfl_up_sync(full, fxp, 1);
+      if (!act) continue;  // after the shuffles: every lane took part in them
+      if (i == 0) {
+        txm = 0.0;
+        fxm = 0.0;
+      } else if (lane == 0) {
+        const CellSoil sm = soil_of(a.soil, c - 1, col - 1);
+        txm = pic_mean(hm, sm.Ksx * a.kr[c - 1], Kxc) * a.cx;
+        fxm = txm * (a.h_new[c - 1] - hc);
+      }
+      double q = fxm + fxp;
+      double tsum = txm + tx;
+      // y faces
+      const double Kyc = s.Ksy * krc, Kzc = s.Ksz * krc;
+      double ty = 0.0;
+      if (j > 0) {
+        const CellSoil sm = soil_of(a.soil, c - a.nx, col - a.nx);
+        const double t = pic_mean(hm, sm.Ksy * a.kr[c - a.nx], Kyc) * a.cy;
+        q += t * (a.h_new[c - a.nx] - hc);
+        tsum += t;
+      }
+      if (j + 1 < a.ny) {
+        const CellSoil sp = soil_of(a.soil, c + a.nx, col + a.nx);
+        ty = pic_mean(hm, Kyc, sp.Ksy * a.kr[c + a.nx]) * a.cy;
+        q += ty * (a.h_new[c + a.nx] - hc);
+        tsum += ty;
+      }
+      // face above: carried, or the top boundary
+      if (k > 0) {
+        q += fzm;
+        tsum += tzm;
+      } else if (a.bc5 == 1) {
+        const double kf = s.Ksz;
+        const double t = kf * (2.0 * a.cz);
+        q += t * (a.htop - hc) + Az * kf;
+        tsum += t;
+      } else if (a.bc5 == 2) {
+        const double qin = -pic_qtop(a, col) * Az;
+        const double tD = s.Ksz * (2.0 * a.cz);
+        const double fD = tD * (0.0 - hc) + Az * s.Ksz;
+        if (a.rain_rate != 0.0 && qin > 0.0 && fD < qin) {
+          q += fD;  // no ponding: Dirichlet h = 0 face for this iterate
+          tsum += tD;
+        } else {
+          q += qin;
+        }
+      }
+      // face below: evaluated here and carried to the next level, or the bottom boundary
+      double tz = 0.0;
+      if (k + 1 < a.nz) {
+        const CellSoil sp = soil_of(a.soil, c + a.ncol, col);
+        const double kf = pic_mean(hm, Kzc, sp.Ksz * a.kr[c + a.ncol]);
+        tz = kf * a.cz;
+        const double fz = tz * (a.h_new[c + a.ncol] - hc) - Az * kf;
+        q += fz;
+        tsum += tz;
+        tzm = tz;
+        fzm = -fz;
+      } else if (a.bc4 == 1) {
+        const double kbv = s.Ksz * vg_kr(s, a.hbot);
+        const double kf = pic_mean(hm, Kzc, kbv);
+        const double t = kf * (2.0 * a.cz);
+        q += t * (a.hbot - hc) - Az * kf;
+        tsum += t;
+      } else if (a.bc4 == 2) {
+        q += a.qbot * Az;
+      } else if (a.bc4 == 3) {
+        q += -Kzc * Az;
+      }
+      const double wcn = a.w_old[c];
+      dg[c] = V * (a.cap[c] + s.Ss * wcn * s.inv_ths) + dt * tsum;
+      a0[c] = -dt * tx;
+      a1[c] = -dt * ty;
+      a2[c] = -dt * tz;
+      const double rdt =
+          V * (a.wch[c] - wcn) + V * s.Ss * (wcn * s.inv_ths) * (hc - a.h_old[c]) - dt * q;
+      bvec[c] = -rdt;
+    }
   }
 }
 
