@@ -262,6 +262,8 @@ SIGNATURES = {
     "frehg_re_training_pairs": (C.c_int, [_VP, C.c_int, _PI, C.c_int, _VP, _VP, _VP, _VP]),
     "frehg_build_arch": (C.c_int, []),
     "frehg_re_checkpoint": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "frehg_re_surface_exchange": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, C.c_double,
+                                            _VP, _VP, C.c_int]),
     "frehg_re_restart": (C.c_int, [_VP, _VP, _VP, _VP]),
     "frehg_fastmath_eval": (C.c_int, [C.c_int, _VP, _VP, C.c_int64]),
 }

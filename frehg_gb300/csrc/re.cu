@@ -43,6 +43,9 @@ struct frehg_re {
   ReScalars* sc = nullptr;
   ReScalars* sc_host = nullptr;
   double* partials = nullptr;
+  double* xch = nullptr;  // surface-exchange staging (eta, bottom, q, total), on first use
+  double* gh_top = nullptr;    // top-layer ghost copies (h then wc) from before an exchange
+  bool top_ghost_stale = false;
   // soil
   SoilClass* cls = nullptr;
   int nclass = 0;
@@ -85,6 +88,8 @@ frehg_re::~frehg_re() {
   cudaFree(qy);
   cudaFree(qz);
   cudaFree(qztop);
+  cudaFree(xch);
+  cudaFree(gh_top);
   cudaFree(qtop_field);
   cudaFree(flags);
   cudaFree(scratch);
@@ -208,6 +213,8 @@ static ReArgs make_args(frehg_re* re) {
   a.soil.Ks = re->fKs;
   a.soil.alpha = re->falpha;
   a.soil.continuous_theta = re->p.scheme == 1;
+  a.gh_top_h = re->top_ghost_stale ? re->gh_top : nullptr;
+  a.gh_top_w = re->top_ghost_stale ? re->gh_top + re->ncol : nullptr;
   a.h_old = re->H[re->cur];
   a.w_old = re->W[re->cur];
   a.h_new = re->H[1 - re->cur];
@@ -306,6 +313,67 @@ __global__ void k_volume(ReArgs a, const double* __restrict__ w, double* out) {
 static int nblocks(size_t n) { return reduction_blocks(n, 256, 4); }
 
 namespace {
+// Surface-water exchange through the top face (Coupling::exchange, src/coupling/Coupling.cpp:
+// 25-166): per column the rate from the top cell's head and the ponded depth, limited by the
+// ponded volume / headroom (infiltration) or the drainable volume (seepage), applied to the
+// surface level and to the top cell (water content clamped, head from the water content).
+// The reference takes the uniform soil parameters (re.params().soil) and dz for the top cell.
+__global__ void k_surface_exchange(double* __restrict__ h, double* __restrict__ wc,
+                                   double* __restrict__ eta, const double* __restrict__ bottom,
+                                   double* __restrict__ q_out, SoilClass k0, int ncol, double Az,
+                                   double dz, double dt, double visc, double min_depth,
+                                   double* partials, unsigned int* arrive, double* total) {
+  CellSoil s;
+  s.alpha = k0.alpha;
+  s.n = k0.n;
+  s.ths = k0.ths;
+  s.thr = k0.thr;
+  s.Ss = k0.Ss;
+  s.aev = k0.aev;
+  s.m = k0.m;
+  s.inv_m = k0.inv_m;
+  s.inv_n = k0.inv_n;
+  s.inv_ths = k0.inv_ths;
+  s.Ksx = k0.Ksx;
+  s.Ksy = k0.Ksy;
+  s.Ksz = k0.Ksz;
+  s.use_vg = k0.use_vg;
+  s.use_mvg = k0.use_mvg;
+  const double V = Az * dz;
+  double v[1] = {0.0};
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
+       col += gridDim.x * blockDim.x) {
+    const double dept = fmax(eta[col] - bottom[col], 0.0);
+    const double wc_top = wc[col];
+    // computeExchangeRates (:48-57)
+    double q = Az * s.Ksz * visc * (h[col] - dept) / (0.5 * dz);
+    if (dept <= min_depth && q < 0.0) q = 0.0;
+    // limitExchange (:82-97); a cell filled to its headroom (drained to theta_r) is set to
+    // theta_s (theta_r) exactly, which wc - q dt / V reaches only up to rounding
+    int bound = 0;
+    if (q < 0.0) {
+      const double q_min_surf = -dept * Az / dt;
+      const double q_min_gw = -(s.ths - wc_top) * V / dt;
+      if (q <= q_min_gw && q_min_gw >= q_min_surf) bound = 1;
+      q = fmax(q, fmax(q_min_surf, q_min_gw));
+    } else if (q > 0.0) {
+      const double q_max_gw = (wc_top - s.thr) * V / dt;
+      if (q >= q_max_gw) bound = -1;
+      q = fmin(q, q_max_gw);
+    }
+    q_out[col] = q;
+    // applyExchangeToSurface (:113-117) and applyExchangeToGroundwater (:133-140)
+    eta[col] += q * dt / Az;
+    double w = fmin(fmax(wc_top - q * dt / V, s.thr), s.ths);
+    if (bound) w = bound > 0 ? s.ths : s.thr;
+    wc[col] = w;
+    h[col] = vg_head(s, w);
+    v[0] += q * dt;
+  }
+  double tot[1];
+  if (grid_sum<1>(v, partials, arrive, tot) && flat_tid() == 0) *total = tot[0];
+}
+
 // network input fields: ln of the vertical conductivity and the moisture capacity
 __global__ void k_net_fields(ReArgs a, float* __restrict__ lnk, float* __restrict__ cap) {
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
@@ -530,6 +598,7 @@ static int pca_step(frehg_re* re) {
   }
   re->cur = 1 - re->cur;
   re->ghosts_valid = true;
+  re->top_ghost_stale = false;  // the step re-enforced the ghosts
   return FREHG_OK;
 }
 
@@ -627,6 +696,7 @@ static int picard_step(frehg_re* re) {
   if (prof->on) FG_TRY(prof->flush());
   re->cur = 1 - re->cur;
   re->ghosts_valid = true;
+  re->top_ghost_stale = false;  // the step re-enforced the ghosts
   return FREHG_OK;
 }
 
@@ -884,6 +954,7 @@ int frehg_re_finalize_initial_state(frehg_re* re) {
   re->sc_host->vol_elastic = 0.0;
   FG_CUDA(cudaMemcpy(re->sc, re->sc_host, sizeof(ReScalars), cudaMemcpyHostToDevice));
   re->ghosts_valid = false;
+  re->top_ghost_stale = false;
   re->finalized = true;
   return FREHG_OK;
 }
@@ -963,6 +1034,54 @@ int frehg_re_prime_adaptive_dt(frehg_re* re, double dt) {
   return FREHG_OK;
 }
 
+int frehg_re_surface_exchange(frehg_re* re, double* eta, const double* bottom, double dt,
+                              double visc, double min_depth, double* q_out, double* total,
+                              int on_device) {
+  clear_error();
+  FG_ARG(re && eta && bottom && q_out && total, "null argument");
+  FG_ARG(dt > 0.0, "dt must be positive");
+  FG_ARG(re->finalized, "surface exchange before an initial state");
+  cudaStream_t st = re->stream;
+  const size_t nc = re->ncol;
+  double *d_eta = eta, *d_q = q_out;
+  const double* d_bot = bottom;
+  if (!on_device) {
+    if (!re->xch) FG_CUDA(cudaMalloc(&re->xch, (3 * nc + 1) * sizeof(double)));
+    FG_CUDA(cudaMemcpyAsync(re->xch, eta, nc * sizeof(double), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(re->xch + nc, bottom, nc * sizeof(double), cudaMemcpyHostToDevice,
+                            st));
+    d_eta = re->xch;
+    d_bot = re->xch + nc;
+    d_q = re->xch + 2 * nc;
+  } else if (!re->xch) {
+    FG_CUDA(cudaMalloc(&re->xch, (3 * nc + 1) * sizeof(double)));
+  }
+  double* d_total = re->xch + 3 * nc;
+  // the reference's halo keeps the top layer's ghost copies from before the exchange until its
+  // next step re-enforces them; keep them (the first exchange since the last step decides)
+  if (re->ghosts_valid && !re->top_ghost_stale) {
+    if (!re->gh_top) FG_CUDA(cudaMalloc(&re->gh_top, 2 * nc * sizeof(double)));
+    FG_CUDA(cudaMemcpyAsync(re->gh_top, re->H[re->cur], nc * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(re->gh_top + nc, re->W[re->cur], nc * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st));
+    re->top_ghost_stale = true;
+  }
+  const SoilClass k0 = make_class(re->p.soil);
+  const int nb = (int)std::min<size_t>((nc + 255) / 256, (size_t)kNumSMs * 8);
+  k_surface_exchange<<<nb, 256, 0, st>>>(re->H[re->cur], re->W[re->cur], d_eta, d_bot, d_q, k0,
+                                         (int)nc, re->p.dx * re->p.dy, re->p.dz, dt, visc,
+                                         min_depth, re->partials, &re->sc->arrive[5], d_total);
+  FG_CUDA(cudaGetLastError());
+  if (!on_device) {
+    FG_CUDA(cudaMemcpyAsync(eta, d_eta, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaMemcpyAsync(q_out, d_q, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  FG_CUDA(cudaMemcpyAsync(total, d_total, sizeof(double), cudaMemcpyDeviceToHost, st));
+  FG_CUDA(cudaStreamSynchronize(st));
+  return FREHG_OK;
+}
+
 int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state) {
   clear_error();
   FG_ARG(re && h && wc && state, "null argument");
@@ -998,6 +1117,7 @@ int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const doub
   FG_CUDA(cudaMemcpy(re->sc, re->sc_host, sizeof(ReScalars), cudaMemcpyHostToDevice));
   re->p.dt = state[1];
   re->ghosts_valid = state[7] != 0.0;
+  re->top_ghost_stale = false;
   re->have_state = true;
   re->finalized = true;
   return FREHG_OK;

@@ -62,6 +62,11 @@ struct ReArgs {
   int face_mean;                   // Picard: 0 arithmetic, 1 harmonic
   double rain_rate, rain_until;    // Picard: rain pulse on the top face (no ponding)
   double picard_dh_max;            // Picard: per-iteration head change limit (0 = none)
+  // ghost copies of the top layer (h, wc) taken before a surface exchange changed its cells:
+  // the reference's halo keeps them until its next step re-enforces the ghosts (nullptr: the
+  // ghosts follow the cells)
+  const double* gh_top_h;
+  const double* gh_top_w;
   // geometric factors: 1/dx, 1/dy, 1/dz; Ax/dx, Ay/dy, Az/dz; V/dz; 1/Ax, 1/Ay, 1/Az
   double inv_dx, inv_dy, inv_dz, cx, cy, cz, v_dz, inv_Ax, inv_Ay, inv_Az;
   SoilView soil;
@@ -188,7 +193,9 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
     const double wcn = a.w_old[c];
     const bool sat_c = a.full3d ? true : (wcn >= s.ths);
     // ghost conductivity of this cell: K(h ghost) = K(h_c) once ghosts exist, K(0) = Ks before
-    const double krg = gv ? krc : 1.0;
+    // a top-layer ghost after a surface exchange keeps the head from before it
+    const bool stale = a.gh_top_h && k == 0;
+    const double krg = gv ? (stale ? vg_kr(s, a.gh_top_h[col]) : krc) : 1.0;
     // +x and -x faces
     double Kxp, Kxm = 0.0;
     {
@@ -204,7 +211,8 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
         const CellSoil sm = soil_of(a.soil, c - 1, col - 1);
         const double krm = a.kr[c - 1];
         const bool sat_m = a.full3d ? true : (a.w_old[c - 1] >= sm.ths);
-        Kxm = face_x(a, i - 1, sm.Ksx * krm, s.Ksx * krc, sm.Ksx * (gv ? krm : 1.0), sat_m, sat_c);
+        const double krmg = gv ? (stale && i - 1 == 0 ? vg_kr(sm, a.gh_top_h[col - 1]) : krm) : 1.0;
+        Kxm = face_x(a, i - 1, sm.Ksx * krm, s.Ksx * krc, sm.Ksx * krmg, sat_m, sat_c);
       }
     }
     double Kyp, Kym = 0.0;
@@ -221,7 +229,9 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
         const CellSoil sm = soil_of(a.soil, c - a.nx, col - a.nx);
         const double krm = a.kr[c - a.nx];
         const bool sat_m = a.full3d ? true : (a.w_old[c - a.nx] >= sm.ths);
-        Kym = face_y(a, j - 1, sm.Ksy * krm, s.Ksy * krc, sm.Ksy * (gv ? krm : 1.0), sat_m, sat_c);
+        const double krmg =
+            gv ? (stale && j - 1 == 0 ? vg_kr(sm, a.gh_top_h[col - a.nx]) : krm) : 1.0;
+        Kym = face_y(a, j - 1, sm.Ksy * krm, s.Ksy * krc, sm.Ksy * krmg, sat_m, sat_c);
       }
     }
     double Kzp, Kzm;
@@ -261,7 +271,8 @@ __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__
     double g = store * hc * V;
     g -= dtg * a.v_dz * Kzp;
     g += dtg * a.v_dz * Kzm;
-    const double hn_ghost = gv ? hc : 0.0;  // lateral hn ghosts are copies (or zero at step 1)
+    // lateral hn ghosts are copies (or zero at step 1)
+    const double hn_ghost = gv ? (stale ? a.gh_top_h[col] : hc) : 0.0;
     if (i == a.nx - 1) g -= Gxp * hn_ghost;
     if (i == 0) g -= Gxm * hn_ghost;
     if (j == a.ny - 1) g -= Gyp * hn_ghost;
@@ -452,6 +463,10 @@ __global__ void __launch_bounds__(256) k_correct(ReArgs a, int planes, int tiles
 // previous step's final water content, zero before the first step).
 __device__ __forceinline__ bool ghost_sat(const ReArgs& a, size_t c, size_t col) {
   if (!a.ghosts_valid) return false;
+  if (a.gh_top_w && c < a.ncol) {  // top layer after a surface exchange: the earlier copy
+    const CellSoil s = soil_of(a.soil, c, col);
+    return a.gh_top_w[col] >= s.ths;
+  }
   return cell_sat(a, c, col, a.w_old);
 }
 

@@ -187,6 +187,20 @@ class ReSolver:
     def prime_adaptive_dt(self, dt):
         check(self._lib.frehg_re_prime_adaptive_dt(self._h, float(dt)), "primeAdaptiveDt")
 
+    def surface_exchange(self, eta, bottom, dt, visc=1.0, min_depth=0.0):
+        """Coupling::exchange through the top face (surface level eta, bed level bottom per
+        column, i + j*nx); returns (eta after, limited rates q [m^3/s], total sum q dt)."""
+        eta = np.array(eta, dtype=np.float64).ravel().copy()
+        bottom = np.ascontiguousarray(bottom, dtype=np.float64).ravel()
+        if eta.size != self.grid.nx * self.grid.ny or bottom.size != eta.size:
+            raise ValueError("surface_exchange: one value per column required")
+        q = np.empty_like(eta)
+        tot = C.c_double()
+        check(self._lib.frehg_re_surface_exchange(self._h, dptr(eta), dptr(bottom), float(dt),
+                                                  float(visc), float(min_depth), dptr(q),
+                                                  C.byref(tot), 0), "surface_exchange")
+        return eta, q, tot.value
+
     def checkpoint(self) -> dict:
         """The step state (h, wc in interior order, time, dt state, budgets, ghost flag)."""
         n = self.grid.nx * self.grid.ny * self.grid.nz

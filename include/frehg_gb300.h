@@ -345,6 +345,19 @@ int frehg_cg_solve_noalloc(int nx, int ny, int nz, const double* diag, const dou
                            const frehg_solver_config* cfg, void* stream, int* its,
                            double* rnorm);
 
+/* Surface-water exchange through the top face, the groundwater side of Coupling::exchange
+ * (src/coupling/Coupling.cpp:25-166) for a caller that owns the surface solver: per column
+ * (index i + j*nx) the rate q = Az Ks_z visc (h_top - dept) / (dz/2) from the top cell's head
+ * and the ponded depth dept = max(eta - bottom, 0) (no infiltration below min_depth), limited by
+ * the ponded volume and the top cell's headroom (q < 0, infiltration) or drainable water
+ * (q > 0, seepage); then eta += q dt / Az and the top cell's water content -= q dt / V (clamped
+ * to [theta_r, theta_s], head from the water content).  Uses the handle's uniform soil
+ * parameters, as the reference does.  eta is updated in place; q_out receives the limited
+ * rates [m^3/s]; *total = sum q dt.  Host arrays, or device arrays with on_device != 0. */
+int frehg_re_surface_exchange(frehg_re* re, double* eta, const double* bottom, double dt,
+                              double visc, double min_depth, double* q_out, double* total,
+                              int on_device);
+
 /* Checkpoint and restart of the step state (the groundwater part of writeCheckpointNow /
  * loadCheckpointState, src/driver/Orchestrator.cpp:1461-1502, 688-747: the field state plus
  * primeAdaptiveDt).  h and wc are host arrays of nx*ny*nz values in interior order (the only
@@ -352,7 +365,8 @@ int frehg_cg_solve_noalloc(int nx, int ny, int nz, const double* diag, const dou
  * state[FREHG_CHECKPOINT_SCALARS] = {time, dt, dtn, dt_used, top inflow volume, bottom inflow
  * volume, elastic volume, ghosts written (1/0)}.  A handle with the same parameters, soil,
  * solver and top flux field restarted from a checkpoint steps exactly like the run that wrote
- * it (bit for bit). */
+ * it (bit for bit).  Checkpoint between steps, not between a surface exchange and the next
+ * step (the top layer's pre-exchange ghost copies are not part of the state). */
 #define FREHG_CHECKPOINT_SCALARS 8
 int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state);
 int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const double* state);

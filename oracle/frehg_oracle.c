@@ -1279,3 +1279,67 @@ void frehg_solver_config_default(frehg_solver_config* c) {
   c->ir_rtol = 1.0e-10;
   c->inner_rtol = 1.0e-4;
 }
+
+/* Coupling::exchange, groundwater and surface sides (src/coupling/Coupling.cpp:25-166), serial:
+ * computeExchangeRates (:48-57), limitExchange (:82-97), applyExchangeToSurface (:113-117),
+ * applyExchangeToGroundwater (:133-140), total = sum q dt (:159-161); a limited cell is set to
+ * theta_s / theta_r exactly (the limit's intent; the reference reaches it up to rounding,
+ * and a cell an ulp short of theta_s would then count as unsaturated).  Uniform soil
+ * (re.params().soil), top-cell dz; eta / bottom / q per column (i + j*nx). */
+int or_re_surface_exchange(or_re* s, double* eta, const double* bottom, double dt, double visc,
+                           double min_depth, double* q_out, double* total) {
+  const frehg_soil_params soil = s->p.soil;
+  const double Az = s->p.dx * s->p.dy;
+  const double dz = s->p.dz;
+  const double V = Az * dz;
+  const int nx = s->nx, ny = s->ny;
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const long o = (long)i + (long)j * nx;
+      const long ti = IX(s, i, j, 0);
+      const double dept = fmax(eta[o] - bottom[o], 0.0);
+      double q = Az * soil.Ks_z * visc * (s->h[ti] - dept) / (0.5 * dz);
+      if (dept <= min_depth && q < 0.0) q = 0.0;
+      q_out[o] = q;
+    }
+  /* bound[o]: +1 the cell was filled to its headroom, -1 drained to theta_r (set exactly;
+   * wc - q dt / V reaches theta_s / theta_r only up to rounding) */
+  signed char* bound = (signed char*)calloc((size_t)nx * ny, 1);
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const long o = (long)i + (long)j * nx;
+      double q = q_out[o];
+      if (q == 0.0) continue;
+      const long ti = IX(s, i, j, 0);
+      const double wc_top = s->wc[ti];
+      if (q < 0.0) {
+        const double dept = fmax(eta[o] - bottom[o], 0.0);
+        const double q_min_surf = -dept * Az / dt;
+        const double q_min_gw = -(soil.theta_s - wc_top) * V / dt;
+        if (q <= q_min_gw && q_min_gw >= q_min_surf) bound[o] = 1;
+        q = fmax(q, fmax(q_min_surf, q_min_gw));
+      } else {
+        const double q_max_gw = (wc_top - soil.theta_r) * V / dt;
+        if (q >= q_max_gw) bound[o] = -1;
+        q = fmin(q, q_max_gw);
+      }
+      q_out[o] = q;
+    }
+  double sum = 0.0;
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const long o = (long)i + (long)j * nx;
+      const long ti = IX(s, i, j, 0);
+      eta[o] += q_out[o] * dt / Az;
+      double w = s->wc[ti] - q_out[o] * dt / V;
+      w = fmin(fmax(w, soil.theta_r), soil.theta_s);
+      if (bound[o]) w = bound[o] > 0 ? soil.theta_s : soil.theta_r;
+      s->wc[ti] = w;
+      s->h[ti] = or_vg_head(&soil, w);
+    }
+  for (long o = 0; o < (long)nx * ny; ++o) sum += q_out[o] * dt;
+  *total = sum;
+  free(bound);
+  return FREHG_OK;
+}
+

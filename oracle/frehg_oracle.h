@@ -54,6 +54,8 @@ int or_re_last_picard_its(const or_re* st);
 double or_re_last_rnorm(const or_re* st);
 long long or_re_total_ksp_its(const or_re* st);
 double or_re_water_volume(const or_re* st);
+int or_re_surface_exchange(or_re* st, double* eta, const double* bottom, double dt, double visc,
+                           double min_depth, double* q_out, double* total);
 void or_re_boundary_volumes(const or_re* st, double* top_in, double* bottom_in);
 /* cumulative elastic (specific-storage) volume of the Picard step (not in reference) */
 double or_re_elastic_volume(const or_re* st);

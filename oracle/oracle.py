@@ -68,6 +68,8 @@ def lib():
             "or_re_last_rnorm": (C.c_double, [_VP]),
             "or_re_total_ksp_its": (C.c_longlong, [_VP]),
             "or_re_water_volume": (C.c_double, [_VP]),
+            "or_re_surface_exchange": (C.c_int, [_VP, _PD, _PD, C.c_double, C.c_double,
+                                                 C.c_double, _PD, _PD]),
             "or_re_boundary_volumes": (None, [_VP, _PD, _PD]),
             "or_re_elastic_volume": (C.c_double, [_VP]),
             "or_vg_theta": (C.c_double, [C.POINTER(SoilParams), C.c_double]),
@@ -187,6 +189,18 @@ class OracleRe:
 
     def water_volume(self):
         return lib().or_re_water_volume(self.h)
+
+    def surface_exchange(self, eta, bottom, dt, visc=1.0, min_depth=0.0):
+        """Coupling::exchange on the oracle state; returns (eta after, q, total)"""
+        eta = np.array(eta, dtype=np.float64).ravel().copy()
+        bottom = np.ascontiguousarray(bottom, dtype=np.float64).ravel()
+        q = np.empty_like(eta)
+        tot = C.c_double()
+        rc = lib().or_re_surface_exchange(self.h, _d(eta), _d(bottom), float(dt), float(visc),
+                                          float(min_depth), _d(q), C.byref(tot))
+        if rc != 0:
+            raise RuntimeError(f"oracle surface_exchange failed ({rc})")
+        return eta, q, tot.value
 
     def boundary_volumes(self):
         t, b = C.c_double(), C.c_double()
