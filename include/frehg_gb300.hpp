@@ -365,6 +365,21 @@ class ReSolver {
     check(frehg_re_restart(re_, cp.h.data(), cp.wc.data(), cp.state), "restart");
     params_.dt = cp.state[1];
   }
+  // groundwater side of Coupling::exchange: eta (surface level per column, i + j*nx) is updated
+  // in place, q (if given) receives the limited rates [m^3/s]; returns sum q dt
+  real surfaceExchange(std::vector<real>& eta, const std::vector<real>& bottom, real dt,
+                       real visc = 1.0, real minDepth = 0.0, std::vector<real>* q = nullptr) {
+    const size_t ncol = (size_t)grid_.nx * grid_.ny;
+    if (eta.size() != ncol || bottom.size() != ncol)
+      throw std::invalid_argument("surfaceExchange: one value per owned column required");
+    std::vector<real> rates(ncol);
+    double total = 0.0;
+    check(frehg_re_surface_exchange(re_, eta.data(), bottom.data(), dt, visc, minDepth,
+                                    rates.data(), &total, 0),
+          "surfaceExchange");
+    if (q) *q = std::move(rates);
+    return total;
+  }
   frehg_re_counters counters() const {
     frehg_re_counters c;
     check(frehg_re_get_counters(re_, &c), "counters");

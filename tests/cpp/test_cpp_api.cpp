@@ -178,6 +178,21 @@ static void closed_box() {
          h.size());
   EXPECT(std::isfinite(h[grid.getIndex(1, 2, 3)]) && re.dtUsed() == 5.0,
          "fields() readable, dtUsed %.1f", re.dtUsed());
+
+  // ponded water on half the columns infiltrates through the top face: the surface loses what
+  // the soil gains
+  std::vector<double> eta((size_t)nx * ny), bottom((size_t)nx * ny, 0.0), q;
+  for (size_t c = 0; c < eta.size(); ++c) eta[c] = (c % 2) ? 0.004 : 0.0;
+  double surf0 = 0.0, surf1 = 0.0;
+  for (double e : eta) surf0 += e * 2.0 * 1.0;
+  const double total = re.surfaceExchange(eta, bottom, 5.0, 1.0, 0.0, &q);
+  for (double e : eta) surf1 += e * 2.0 * 1.0;
+  const double v2 = re.waterVolume();
+  EXPECT(total < 0.0 && q.size() == eta.size() && q[0] == 0.0 && q[1] < 0.0,
+         "surfaceExchange: infiltration where ponded (total %.3e m^3)", total);
+  const double bal = std::fabs((surf1 - surf0) + (v2 - v1)) / std::fabs(total);
+  EXPECT(bal < 1e-10 && std::fabs((surf0 - surf1) + total) < 1e-15,
+         "surfaceExchange conserves water: imbalance %.3e of the exchanged volume", bal);
 }
 
 int main() {
