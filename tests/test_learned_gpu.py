@@ -87,16 +87,17 @@ def test_learned_fcg_accuracy_and_iterations(gpu_lib, trained):
           f"(held-out loss {before:.3e} -> {after:.3e}); solve ms: line {cl.plain_ms:.1f}, "
           f"learned {cn.net_ms + cn.plain_ms:.1f} ({cn.net_solves} network solves, "
           f"{cn.fcg_fallbacks} fallbacks)")
-    for a, b, c in zip(h64, hl, hn):
-        assert np.abs(a - b).max() <= 1e-8
-        assert np.abs(a - c).max() <= 1e-8
+    for s, (a, b, c) in enumerate(zip(h64, hl, hn)):
+        assert np.abs(a - b).max() <= 1e-8, f"step {s}: line-PCG head {np.abs(a - b).max():.3e}"
+        assert np.abs(a - c).max() <= 1e-8, f"step {s}: learned head {np.abs(a - c).max():.3e}"
     # the first solve of the learned handle is its network-free reference solve
-    assert lrn[0] == line[0]
-    assert cn.net_solves == len(lrn) - 1
-    # a solve that passes twice the reference count finishes without the network (which at
-    # most repeats the reference solve's work)
+    assert lrn[0] == line[0], (lrn, line)
+    assert cn.net_solves == len(lrn) - 1, (cn.net_solves, lrn)
+    # a solve whose inner count passes twice the reference count (checked every 4 network
+    # iterations) continues with line-PCG from its iterate: at most 2 * ref + 4 network
+    # iterations, then line-PCG work comparable to a solve of its own
     for a in lrn[1:]:
-        assert a <= 3 * lrn[0] + 8
+        assert a <= 2 * lrn[0] + 4 + 4 * max(line) + 4, (lrn, line, cn.fcg_fallbacks)
 
 
 def test_time_policy(gpu_lib, trained):
