@@ -98,7 +98,7 @@ class ReParams(C.Structure):
         ("rain_rate", C.c_double),
         ("rain_until", C.c_double),
         ("picard_dt_adapt", C.c_int32),
-        ("pad_", C.c_int32),
+        ("picard_fp64", C.c_int32),
         ("picard_dh_max", C.c_double),
     ]
 
@@ -266,6 +266,7 @@ SIGNATURES = {
                                             _VP, _VP, C.c_int]),
     "frehg_re_restart": (C.c_int, [_VP, _VP, _VP, _VP]),
     "frehg_fastmath_eval": (C.c_int, [C.c_int, _VP, _VP, C.c_int64]),
+    "frehg_constit_eval": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_int64, _VP, _VP, _VP]),
 }
 
 _lib = None

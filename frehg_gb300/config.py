@@ -317,6 +317,9 @@ def re_params(cfg, scheme):
     p.picard_max_it = int(get(cfg, "groundwater.picard_max_it", 50))
     p.picard_dt_adapt = int(bool(get(cfg, "groundwater.picard_dt_adapt", False)))
     p.picard_dh_max = float(get(cfg, "groundwater.picard_dh_max", 0.0))
+    # constitutive relations, assembly and final update of the Picard scheme in native FP64
+    # (true) or in float-float arithmetic on the FP32 pipe (false, the default)
+    p.picard_fp64 = int(bool(get(cfg, "groundwater.picard_fp64", False)))
     p.rain_rate = float(get(cfg, "groundwater.rain.rate", 0.0))
     p.rain_until = float(get(cfg, "groundwater.rain.until", 0.0))
     return p

@@ -191,6 +191,10 @@ class KrylovSolver {
   const void* g64_key2 = nullptr;
   Profiler* prof = nullptr;  // owner's profiler (launch counts, optional event timing)
   NetPrecond net;            // learned preconditioner (FCG inner solves when set)
+  // the mixed path's scaled couplings in float-float (2^-48) instead of FP64 products: for
+  // solves whose result is an update of an iterate (Picard), where the operator's last bits
+  // change the update, not the fixed point; solves whose result is the solution keep FP64
+  bool ff_operator = false;
   float* zf = nullptr;
   // vertical-line preconditioner (FP32 factors and sweep scratch)
   int ensure_line(size_t n);

@@ -11,6 +11,7 @@
 // The FP32 inner iteration moves 56 B/cell (vs 120 B/cell in FP64) and leaves the FP64 pipe,
 // the limiter of the FP64 path on GB300, idle.  Convergence is always to the FP64 true
 // residual, so the inner precision changes the iteration count, not the accuracy.
+#include "ff32.cuh"
 #include "internal.h"
 #include "krylov_kernels.cuh"
 #include "line.cuh"
@@ -24,10 +25,13 @@
 namespace fg {
 
 // r~ = s b - A~ x~ (FP64, kept in rres); e = 0; sums of r~^2 (scale of the inner system),
-// (r~/s)^2 = (sq r~)^2 for the true residual (sq = D^1/2) and b^2 for ||b||.  The last block
+// (r~/s)^2 = (sq r~)^2 for the true residual (sq = 1/s) and b^2 for ||b||.  The last block
 // runs the refinement test.
 // FIRST (the first sweep, x~ = 0): r~ = s b without the stencil product, x~ written as 0, and
-// the b^2 sum that ||b|| needs; later sweeps skip that sum.
+// the b^2 sum that ||b|| needs (with x~ = 0 the true residual is b itself).  Later sweeps form
+// the stencil product in FP64: the residual is a difference of nearly equal terms, and the
+// refinement converges only as far as this product is accurate (a float-float form, 2^-48,
+// was both slower here and short of 1e-12 on ill-conditioned systems).
 template <bool FIRST>
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
@@ -36,35 +40,48 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     int n1, int n2, int planes, int tiles, CgDevState* ir, double* partials, double ir_rtol) {
   if (ir->status) return;
   const int t0 = (n0 + 31) / 32;
+  const size_t s01 = (size_t)n0 * n1;
   double v[3] = {0.0, 0.0, 0.0};
-  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const int i0 = (tile % t0) * 32 + threadIdx.x;
-    const int i1 = (tile / t0) * 8 + threadIdx.y;
-    if (i0 >= n0 || i1 >= n1) continue;
-    const size_t s01 = (size_t)n0 * n1;
-    const int kb = blockIdx.y * planes, ke = min(n2, kb + planes);
-    size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
-    for (int k = kb; k < ke; ++k, c += s01) {
-      double ax = 0.0;
-      if (FIRST) {
+  if (FIRST) {
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+      const int i0 = (tile % t0) * 32 + threadIdx.x;
+      const int i1 = (tile / t0) * 8 + threadIdx.y;
+      if (i0 >= n0 || i1 >= n1) continue;
+      const int kb = blockIdx.y * planes, ke = min(n2, kb + planes);
+      size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
+      for (int k = kb; k < ke; ++k, c += s01) {
         x[c] = 0.0;
-      } else {
-        ax = x[c];
+        const double bc = b[c];
+        const double r = s[c] * bc;
+        rres[c] = r;
+        ef[c] = 0.0f;
+        v[0] = fma(r, r, v[0]);
+        v[2] = fma(bc, bc, v[2]);
+      }
+    }
+    v[1] = v[2];
+  } else {
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+      const int i0 = (tile % t0) * 32 + threadIdx.x;
+      const int i1 = (tile / t0) * 8 + threadIdx.y;
+      if (i0 >= n0 || i1 >= n1) continue;
+      const int kb = blockIdx.y * planes, ke = min(n2, kb + planes);
+      size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
+      for (int k = kb; k < ke; ++k, c += s01) {
+        double ax = x[c];
         if (i0 > 0) ax = fma(a0[c - 1], x[c - 1], ax);
         if (i0 + 1 < n0) ax = fma(a0[c], x[c + 1], ax);
         if (i1 > 0) ax = fma(a1[c - n0], x[c - n0], ax);
         if (i1 + 1 < n1) ax = fma(a1[c], x[c + n0], ax);
         if (k > 0) ax = fma(a2[c - s01], x[c - s01], ax);
         if (k + 1 < n2) ax = fma(a2[c], x[c + s01], ax);
+        const double r = fma(s[c], b[c], -ax);
+        rres[c] = r;
+        ef[c] = 0.0f;
+        v[0] = fma(r, r, v[0]);
+        const double ru = r * sq[c];  // r~ / s = D^1/2 r~
+        v[1] = fma(ru, ru, v[1]);
       }
-      const double sc = s[c], bc = b[c];
-      const double r = fma(sc, bc, -ax);
-      rres[c] = r;
-      ef[c] = 0.0f;
-      v[0] = fma(r, r, v[0]);
-      const double ru = r * sq[c];  // r~ / s = D^1/2 r~
-      v[1] = fma(ru, ru, v[1]);
-      if (FIRST) v[2] = fma(bc, bc, v[2]);
     }
   }
   double tot[3];
@@ -89,11 +106,13 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
                            const CgDevState* ir, CgDevState* in, double* partials,
                            double inner_rtol) {
   if (ir->status) return;
-  const double sig = 1.0 / ir->a;
+  const float sig = (float)(1.0 / ir->a);
   Kahan32 acc;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
        c += (size_t)gridDim.x * blockDim.x) {
-    const float r32 = (float)(rres[c] * sig);
+    // the FP32 right-hand side from the residual's leading 24 bits (integer split: GB300's
+    // double->float conversion runs on the FP64 pipe)
+    const float r32 = ff_hi_of(rres[c]) * sig;
     rf[c] = r32;
     acc.add(r32 * r32);
   }
@@ -489,21 +508,57 @@ int KrylovSolver::ensure32(size_t n) {
   return FREHG_OK;
 }
 
-// Scaling of a fresh operator for the mixed path in two passes: s = D^-1/2 with sq = D^1/2
-// (the true-residual norm multiplies by it), then one pass per column that scales the
-// couplings in place (FP64, for the refinement residual), writes their FP32 copies and, with
-// the line preconditioner, the column factors (FP64 recurrence, one division per cell).
+// Scaling of a fresh operator for the mixed path in two passes: s = D^-1/2 with sq = 1/s (the
+// true-residual norm multiplies by it), then one pass per column that scales the couplings in
+// place (for the refinement residual), writes their FP32 copies and, with the line
+// preconditioner, the column factors.
+//
+// FF_OP (solves whose result is an update of an iterate): s is rounded to FP32.  The scaling is
+// a similarity transform (A~ = S A S, b~ = S b, x = S x~), so s_c s_n is then an exact float
+// product and the scaled couplings a s_c s_n cost one float-float product each instead of two
+// FP64 multiplications (GB300 runs FP64 at 1/73 of the FP32 rate).  The scaled diagonal d s^2
+// is then 1 only to FP32 precision while the refinement takes it as 1: the update changes in
+// its last digits, the iterate's fixed point does not.  Solves whose result is the solution
+// itself keep the FP64 s (d s^2 = 1 to rounding).
+template <bool FF_OP>
 __global__ void k_diag_rsqrt_sq(double* __restrict__ s, double* __restrict__ sq, size_t n) {
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
        c += (size_t)gridDim.x * blockDim.x) {
-    double d = s[c];
-    if (d == 0.0) d = 1.0;  // PCJacobi replaces a zero diagonal entry by 1
-    const double r = rsqrt(d);
-    s[c] = r;
-    sq[c] = d * r;
+    const double d = s[c];
+    if (FF_OP) {
+      // PCJacobi replaces a zero diagonal entry by 1
+      const float df = (__double_as_longlong(d) << 1) == 0 ? 1.0f : ff_hi_of(d);
+      const float r = rsqrtf(df);
+      s[c] = (double)r;
+      sq[c] = (double)__frcp_rn(r);
+    } else {
+      const double dd = d == 0.0 ? 1.0 : d;
+      const double r = rsqrt(dd);
+      s[c] = r;
+      sq[c] = dd * r;
+    }
   }
 }
 
+// The scaled couplings v = a s_c s_n written back as doubles and as floats: in FP64 (two
+// multiplications; FF_OP false) or in float-float (FF_OP true: s_c s_n exact, a split from its
+// double, about 48 significant bits); the line factors
+//   l_k = v2_{k-1} / d_{k-1},  d_k = 1 - l_k v2_{k-1}   (d_0 = 1)
+// in float-float, stored as floats.  The FP32 copies are the leading 24 bits (no double->float
+// conversion, which runs on the FP64 pipe).
+template <bool FF_OP>
+__device__ __forceinline__ ff scaled_coupling(double* a, size_t c, double sc, double sn) {
+  if (FF_OP) {  // sc, sn hold floats
+    const ff v = ff_mul(ff_from_double(a[c]), two_prod(ff_hi_of(sc), ff_hi_of(sn)));
+    a[c] = ff_to_double(v);
+    return v;
+  }
+  const double v = a[c] * sc * sn;
+  a[c] = v;
+  return ff_make(ff_hi_of(v));
+}
+
+template <bool FF_OP>
 __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
                                                      double* __restrict__ a1,
                                                      double* __restrict__ a2,
@@ -516,37 +571,38 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
                                                      int n2, int line) {
   const int ncol = n0 * n1;
   const size_t sk = (size_t)ncol;
+  const ff zero = ff_make(0.0f);
   for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
        col += gridDim.x * blockDim.x) {
     const int i0 = col % n0, i1 = col / n0;
-    double inv_d = 1.0, aprev = 0.0;
+    ff inv_d = ff_make(1.0f), aprev = zero;
     size_t c = (size_t)col;
+    double sc = s[c];
     for (int k = 0; k < n2; ++k, c += sk) {
-      const double sc = s[c];
-      const double v0 = (i0 + 1 < n0) ? a0[c] * sc * s[c + 1] : 0.0;
-      const double v1 = (i1 + 1 < n1) ? a1[c] * sc * s[c + n0] : 0.0;
-      const double v2 = (k + 1 < n2) ? a2[c] * sc * s[c + sk] : 0.0;
-      a0[c] = v0;
-      a1[c] = v1;
-      a2[c] = v2;
-      f0[c] = (float)v0;
-      f1[c] = (float)v1;
-      f2[c] = (float)v2;
+      const double sb = (k + 1 < n2) ? s[c + sk] : 0.0;
+      ff v0 = zero, v1 = zero, v2 = zero;
+      if (i0 + 1 < n0) v0 = scaled_coupling<FF_OP>(a0, c, sc, s[c + 1]);
+      else a0[c] = 0.0;
+      if (i1 + 1 < n1) v1 = scaled_coupling<FF_OP>(a1, c, sc, s[c + n0]);
+      else a1[c] = 0.0;
+      if (k + 1 < n2) v2 = scaled_coupling<FF_OP>(a2, c, sc, sb);
+      else a2[c] = 0.0;
+      f0[c] = v0.h;
+      f1[c] = v1.h;
+      f2[c] = v2.h;
       if (line) {
-        double l = 0.0;
+        ff l = zero;
         if (k > 0) {
-          l = aprev * inv_d;
-          double d = 1.0 - l * aprev;
-          if (!(d > 1e-30)) d = 1.0;  // not SPD: that row falls back to the Jacobi step
-          // 1/d from the FP32 reciprocal and one Newton step (relative error ~1e-14; the
-          // factors are stored in FP32)
-          const double y = (double)__frcp_rn((float)d);
-          inv_d = y * fma(-d, y, 2.0);
+          l = ff_mul(aprev, inv_d);
+          ff d = ff_add_f(ff_neg(ff_mul(l, aprev)), 1.0f);
+          if (!(d.h > 1e-30f)) d = ff_make(1.0f);  // not SPD: that row falls back to Jacobi
+          inv_d = ff_div(ff_make(1.0f), d);
         }
-        lk[c] = (float)l;
-        dinv[c] = (float)inv_d;
+        lk[c] = l.h;
+        dinv[c] = inv_d.h;
         aprev = v2;
       }
+      sc = sb;
     }
   }
 }
@@ -567,12 +623,22 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line) {
   const int ncol = A.n0 * A.n1;
   const int lb = (int)std::min<long>((ncol + 127) / 128, kMaxRedBlocks);
   if (!A.scaled) {
-    FG_LAUNCH(prof, st, "k_diag_rsqrt_sq", 24.0 * dn,
-              k_diag_rsqrt_sq<<<nb, 256, 0, st>>>(A.s, r, n));
-    FG_LAUNCH(prof, st, "k_scale_mixed", (56.0 + 12.0 + (line ? 8.0 : 0.0)) * dn,
-              k_scale_mixed<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, op32.a0, op32.a1,
-                                                op32.a2, lkf, dinvf, A.n0, A.n1, A.n2,
-                                                line ? 1 : 0));
+    if (ff_operator)
+      FG_LAUNCH(prof, st, "k_diag_rsqrt_sq", 24.0 * dn,
+                k_diag_rsqrt_sq<true><<<nb, 256, 0, st>>>(A.s, r, n));
+    else
+      FG_LAUNCH(prof, st, "k_diag_rsqrt_sq", 24.0 * dn,
+                k_diag_rsqrt_sq<false><<<nb, 256, 0, st>>>(A.s, r, n));
+    if (ff_operator)
+      FG_LAUNCH(prof, st, "k_scale_mixed", (56.0 + 12.0 + (line ? 8.0 : 0.0)) * dn,
+                k_scale_mixed<true><<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, op32.a0, op32.a1,
+                                                        op32.a2, lkf, dinvf, A.n0, A.n1, A.n2,
+                                                        line ? 1 : 0));
+    else
+      FG_LAUNCH(prof, st, "k_scale_mixed", (56.0 + 12.0 + (line ? 8.0 : 0.0)) * dn,
+                k_scale_mixed<false><<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, op32.a0,
+                                                         op32.a1, op32.a2, lkf, dinvf, A.n0,
+                                                         A.n1, A.n2, line ? 1 : 0));
     FG_CUDA(cudaGetLastError());
     A.scaled = true;
     return FREHG_OK;

@@ -263,19 +263,31 @@ __global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restri
   }
 }
 
-// h^{m+1} = h^m + d (d limited to +-picard_dh_max when set) and |d|_inf
+// h^{m+1} = h^m + d (d limited to +-picard_dh_max when set) and |d|_inf.  The limit and the
+// maximum compare bit patterns (non-negative doubles order like their 64-bit integers), which
+// keeps them off the FP64 pipe; a NaN in d counts as an infinite change, which fails the
+// convergence test.
 __global__ void k_pic_update(ReArgs a, const double* __restrict__ d) {
-  double m = 0.0;
+  const long long kAbs = 0x7fffffffffffffffll;
+  long long m = 0;
   const double lim = a.picard_dh_max;
+  const long long lim_bits = lim > 0.0 ? __double_as_longlong(lim) : kAbs;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
        c += (size_t)gridDim.x * blockDim.x) {
     double dc = d[c];
-    if (lim > 0.0) dc = fmin(fmax(dc, -lim), lim);
+    const long long b = __double_as_longlong(dc);
+    long long ab = b & kAbs;
+    if (ab > lim_bits) {
+      ab = lim_bits;
+      dc = __longlong_as_double((b & ~kAbs) | lim_bits);
+    }
     a.h_new[c] += dc;
-    m = fmax(m, fabs(dc));
+    m = ab > m ? ab : m;
   }
+  m = m > 0x7ff0000000000000ll ? 0x7ff0000000000000ll : m;  // NaN -> inf
   double tot;
-  if (grid_max(m, a.partials + 2 * kMaxRedBlocks, &a.sc->arrive[1], &tot) && flat_tid() == 0)
+  if (grid_max(__longlong_as_double(m), a.partials + 2 * kMaxRedBlocks, &a.sc->arrive[1], &tot) &&
+      flat_tid() == 0)
     a.sc->dq_max = tot;
 }
 

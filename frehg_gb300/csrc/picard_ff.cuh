@@ -1,0 +1,330 @@
+// Float-float forms of the Picard assembly and of the conservative final update (not in
+// reference): the same faces, boundary closures, residual and update as k_pic_assemble /
+// k_pic_final (picard.cuh), with every FP64 operation replaced by float-float arithmetic on
+// the FP32 pipe (ff32.cuh; about 48 significant bits).  GB300 runs FP64 at 1/73 of the FP32
+// rate, and the FP64 forms of these kernels are bound by that pipe, not by memory.
+//
+// Doubles are read and split into float-float with integer operations; results are written
+// back as doubles.  The residual keeps the accuracy the fixed point needs (absolute errors of
+// a few 2^-48 of its terms); the face fluxes of two neighbouring cells are exact negatives of
+// each other (the face mean takes its arguments in index order, the head difference changes
+// sign exactly), so the water budget of the final update closes to rounding as in FP64.
+#pragma once
+
+#include "picard.cuh"
+
+namespace fg {
+
+// head and the three directional conductivities Ks * kr of one cell, float-float
+struct FfCell {
+  ff h, kx, ky, kz;
+};
+
+__device__ __forceinline__ const SoilClass& class_of(const ReArgs& a, size_t c, size_t col) {
+  return a.soil.cls[a.soil.cid ? (int)a.soil.cid[a.soil.cid3d ? c : col] : 0];
+}
+
+// Ks of one cell along axis d (0 x, 1 y, 2 z)
+__device__ __forceinline__ ff ff_ks(const ReArgs& a, const SoilClass& k, size_t c, int d) {
+  if (a.soil.Ks) return ff_from_double(a.soil.Ks[c]);
+  return ff_make(k.ff_ks[d][0], k.ff_ks[d][1]);
+}
+
+__device__ __forceinline__ FfCell ff_cell(const ReArgs& a, size_t c, size_t col) {
+  const SoilClass& k = class_of(a, c, col);
+  const ff kr = ff_from_double(a.kr[c]);
+  FfCell r;
+  r.h = ff_from_double(a.h_new[c]);
+  if (a.soil.Ks || k.ks_iso) {
+    r.kx = ff_mul(ff_ks(a, k, c, 0), kr);
+    r.ky = r.kx;
+    r.kz = r.kx;
+  } else {
+    r.kx = ff_mul(ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
+    r.ky = ff_mul(ff_make(k.ff_ks[1][0], k.ff_ks[1][1]), kr);
+    r.kz = ff_mul(ff_make(k.ff_ks[2][0], k.ff_ks[2][1]), kr);
+  }
+  return r;
+}
+
+// pic_mean of two non-negative conductivities (lower index first)
+__device__ __forceinline__ ff ff_face_mean(int harmonic, ff lo, ff hi) {
+  const ff s = ff_add_fast(lo, hi);
+  if (!harmonic) return ff_scale(s, 0.5f);
+  return s.h > 0.0f ? ff_scale(ff_div(ff_mul(lo, hi), s), 2.0f) : ff_make(0.0f);
+}
+
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+
+// geometric factors and boundary values of a launch, float-float
+struct FfConst {
+  ff cx, cy, cz, cz2, Az, V, dt, htop, hbot, qbot;
+};
+
+__device__ __forceinline__ FfConst ff_consts(const ReArgs& a, double dt) {
+  FfConst k;
+  k.cx = ff_from_double(a.cx);
+  k.cy = ff_from_double(a.cy);
+  k.cz = ff_from_double(a.cz);
+  k.cz2 = ff_scale(k.cz, 2.0f);
+  k.Az = ff_from_double(a.dx * a.dy);
+  k.V = ff_from_double(a.dx * a.dy * a.dz);
+  k.dt = ff_from_double(dt);
+  k.htop = ff_from_double(a.htop);
+  k.hbot = ff_from_double(a.hbot);
+  k.qbot = ff_from_double(a.qbot);
+  return k;
+}
+
+// the top-face closure of one cell: flux into the cell and the transmissibility it adds to the
+// diagonal (pic_row's k = 0 branch)
+__device__ __forceinline__ void ff_top_face(const ReArgs& a, const FfConst& K, const FfCell& cell,
+                                            const SoilClass& kc, size_t c, size_t col, ff* flux,
+                                            ff* trans) {
+  *flux = ff_make(0.0f);
+  *trans = ff_make(0.0f);
+  if (a.bc5 == 1) {
+    const ff kf = ff_ks(a, kc, c, 2);
+    const ff t = ff_mul(kf, K.cz2);
+    *flux = ff_add(ff_mul(t, ff_sub(K.htop, cell.h)), ff_mul(K.Az, kf));
+    *trans = t;
+  } else if (a.bc5 == 2) {
+    const ff qin = ff_neg(ff_mul(ff_from_double(pic_qtop(a, col)), K.Az));
+    const ff ksz = ff_ks(a, kc, c, 2);
+    const ff tD = ff_mul(ksz, K.cz2);
+    const ff fD = ff_add(ff_neg(ff_mul(tD, cell.h)), ff_mul(K.Az, ksz));
+    if (a.rain_rate != 0.0 && qin.h > 0.0f && ff_lt(fD, qin)) {
+      *flux = fD;  // no ponding: Dirichlet h = 0 face for this iterate
+      *trans = tD;
+    } else {
+      *flux = qin;
+    }
+  }
+}
+
+// the bottom-face closure (pic_row's k = nz-1 branch)
+__device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K,
+                                               const FfCell& cell, size_t c, size_t col, ff* flux,
+                                               ff* trans) {
+  *flux = ff_make(0.0f);
+  *trans = ff_make(0.0f);
+  if (a.bc4 == 1) {
+    const CellSoil s = soil_of(a.soil, c, col);
+    const ff kb = ff_from_double(s.Ksz * vg_kr(s, a.hbot));
+    const ff kf = ff_face_mean(a.face_mean, cell.kz, kb);
+    const ff t = ff_mul(kf, K.cz2);
+    *flux = ff_sub(ff_mul(t, ff_sub(K.hbot, cell.h)), ff_mul(K.Az, kf));
+    *trans = t;
+  } else if (a.bc4 == 2) {
+    *flux = ff_mul(K.qbot, K.Az);
+  } else if (a.bc4 == 3) {
+    *flux = ff_neg(ff_mul(cell.kz, K.Az));
+  }
+}
+
+// k_pic_assemble in float-float: same launch shape and face sharing (x faces by warp shuffle,
+// z faces carried down the column, and here the cell below carried as the next level's cell)
+__global__ void __launch_bounds__(256) k_pic_assemble_ff(ReArgs a, double* __restrict__ dg,
+                                                         double* __restrict__ a0,
+                                                         double* __restrict__ a1,
+                                                         double* __restrict__ a2,
+                                                         double* __restrict__ bvec, int planes,
+                                                         int tiles) {
+  const FfConst K = ff_consts(a, a.sc->dt_used);
+  const int hm = a.face_mean;
+  const int t0 = (a.nx + 31) / 32;
+  const int lane = threadIdx.x;
+  const unsigned full = 0xffffffffu;
+  const ff zero = ff_make(0.0f);
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i = (tile % t0) * 32 + lane;
+    const int j = (tile / t0) * 8 + threadIdx.y;
+    const bool act = i < a.nx && j < a.ny;
+    const size_t col = act ? (size_t)i + (size_t)a.nx * j : 0;
+    const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
+    FfCell cur = {zero, zero, zero, zero};
+    ff tzm = zero, fzm = zero;  // top face of the current cell
+    if (act && kb < ke) {
+      cur = ff_cell(a, col + a.ncol * kb, col);
+      if (kb > 0) {
+        const FfCell up = ff_cell(a, col + a.ncol * (kb - 1), col);
+        const ff kf = ff_face_mean(hm, up.kz, cur.kz);
+        tzm = ff_mul(kf, K.cz);
+        fzm = ff_add(ff_mul(tzm, ff_sub(up.h, cur.h)), ff_mul(K.Az, kf));
+      }
+    }
+    for (int k = kb; k < ke; ++k) {
+      const size_t c = col + a.ncol * k;
+      // +x face from the next lane's cell (lane 31 loads its neighbour)
+      ff Kxn = ff_make(__shfl_down_sync(full, cur.kx.h, 1), __shfl_down_sync(full, cur.kx.l, 1));
+      ff hxn = ff_make(__shfl_down_sync(full, cur.h.h, 1), __shfl_down_sync(full, cur.h.l, 1));
+      ff tx = zero, fxp = zero;
+      if (act && i + 1 < a.nx) {
+        if (lane == 31) {
+          const FfCell nb = ff_cell(a, c + 1, col + 1);
+          Kxn = nb.kx;
+          hxn = nb.h;
+        }
+        tx = ff_mul(ff_face_mean(hm, cur.kx, Kxn), K.cx);
+        fxp = ff_mul(tx, ff_sub(hxn, cur.h));
+      }
+      // -x face: the previous lane's +x face (lane 0 evaluates its own)
+      ff txm = ff_make(__shfl_up_sync(full, tx.h, 1), __shfl_up_sync(full, tx.l, 1));
+      ff fxm = ff_neg(ff_make(__shfl_up_sync(full, fxp.h, 1), __shfl_up_sync(full, fxp.l, 1)));
+      if (!act) continue;  // after the shuffles: every lane took part in them
+      if (i == 0) {
+        txm = zero;
+        fxm = zero;
+      } else if (lane == 0) {
+        const FfCell nb = ff_cell(a, c - 1, col - 1);
+        txm = ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx);
+        fxm = ff_mul(txm, ff_sub(nb.h, cur.h));
+      }
+      ff q = ff_add(fxm, fxp);
+      ff tsum = ff_add_fast(txm, tx);
+      // y faces
+      ff ty = zero;
+      if (j > 0) {
+        const FfCell nb = ff_cell(a, c - a.nx, col - a.nx);
+        const ff t = ff_mul(ff_face_mean(hm, nb.ky, cur.ky), K.cy);
+        q = ff_add(q, ff_mul(t, ff_sub(nb.h, cur.h)));
+        tsum = ff_add_fast(tsum, t);
+      }
+      if (j + 1 < a.ny) {
+        const FfCell nb = ff_cell(a, c + a.nx, col + a.nx);
+        ty = ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy);
+        q = ff_add(q, ff_mul(ty, ff_sub(nb.h, cur.h)));
+        tsum = ff_add_fast(tsum, ty);
+      }
+      const SoilClass& kc = class_of(a, c, col);
+      // face above: carried, or the top boundary
+      if (k > 0) {
+        q = ff_add(q, fzm);
+        tsum = ff_add_fast(tsum, tzm);
+      } else {
+        ff f, t;
+        ff_top_face(a, K, cur, kc, c, col, &f, &t);
+        q = ff_add(q, f);
+        tsum = ff_add_fast(tsum, t);
+      }
+      // face below: evaluated here and carried to the next level with the cell below
+      ff tz = zero;
+      FfCell below = cur;
+      if (k + 1 < a.nz) {
+        below = ff_cell(a, c + a.ncol, col);
+        const ff kf = ff_face_mean(hm, cur.kz, below.kz);
+        tz = ff_mul(kf, K.cz);
+        const ff fz = ff_sub(ff_mul(tz, ff_sub(below.h, cur.h)), ff_mul(K.Az, kf));
+        q = ff_add(q, fz);
+        tsum = ff_add_fast(tsum, tz);
+        tzm = tz;
+        fzm = ff_neg(fz);
+      } else {
+        ff f, t;
+        ff_bottom_face(a, K, cur, c, col, &f, &t);
+        q = ff_add(q, f);
+        tsum = ff_add_fast(tsum, t);
+      }
+      // diagonal V (C + Ss wcn/ths) + dt sum T, couplings -dt T, rhs -Rdt with
+      // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q
+      const ff wcn = ff_from_double(a.w_old[c]);
+      const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
+      dg[c] = ff_to_double(ff_add_fast(ff_mul(K.V, ff_add_fast(ff_from_double(a.cap[c]), st)),
+                                       ff_mul(K.dt, tsum)));
+      a0[c] = -ff_to_double(ff_mul(K.dt, tx));
+      a1[c] = -ff_to_double(ff_mul(K.dt, ty));
+      a2[c] = -ff_to_double(ff_mul(K.dt, tz));
+      const ff dth = ff_sub(ff_from_double(a.wch[c]), wcn);
+      const ff dh = ff_sub(cur.h, ff_from_double(a.h_old[c]));
+      const ff rdt = ff_sub(ff_mul(K.V, ff_add(dth, ff_mul(st, dh))), ff_mul(K.dt, q));
+      bvec[c] = -ff_to_double(rdt);
+      cur = below;
+    }
+  }
+}
+
+// Net inflow of one cell with its top / bottom boundary parts (pic_row in float-float, each
+// face evaluated from the cells' own values, as pic_row does)
+struct FfRow {
+  ff q, top, bot;
+};
+
+__device__ __forceinline__ FfRow ff_pic_row(const ReArgs& a, const FfConst& K, size_t c,
+                                            size_t col, int i, int j, int k) {
+  const int hm = a.face_mean;
+  const FfCell cur = ff_cell(a, c, col);
+  FfRow r = {ff_make(0.0f), ff_make(0.0f), ff_make(0.0f)};
+  if (i > 0) {
+    const FfCell nb = ff_cell(a, c - 1, col - 1);
+    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx), ff_sub(nb.h, cur.h)));
+  }
+  if (i + 1 < a.nx) {
+    const FfCell nb = ff_cell(a, c + 1, col + 1);
+    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.kx, nb.kx), K.cx), ff_sub(nb.h, cur.h)));
+  }
+  if (j > 0) {
+    const FfCell nb = ff_cell(a, c - a.nx, col - a.nx);
+    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.ky, cur.ky), K.cy), ff_sub(nb.h, cur.h)));
+  }
+  if (j + 1 < a.ny) {
+    const FfCell nb = ff_cell(a, c + a.nx, col + a.nx);
+    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy), ff_sub(nb.h, cur.h)));
+  }
+  if (k > 0) {
+    const FfCell nb = ff_cell(a, c - a.ncol, col);
+    const ff kf = ff_face_mean(hm, nb.kz, cur.kz);
+    r.q = ff_add(r.q, ff_add(ff_mul(ff_mul(kf, K.cz), ff_sub(nb.h, cur.h)), ff_mul(K.Az, kf)));
+  } else {
+    ff t;
+    ff_top_face(a, K, cur, class_of(a, c, col), c, col, &r.top, &t);
+    r.q = ff_add(r.q, r.top);
+  }
+  if (k + 1 < a.nz) {
+    const FfCell nb = ff_cell(a, c + a.ncol, col);
+    const ff kf = ff_face_mean(hm, cur.kz, nb.kz);
+    r.q = ff_add(r.q, ff_sub(ff_mul(ff_mul(kf, K.cz), ff_sub(nb.h, cur.h)), ff_mul(K.Az, kf)));
+  } else {
+    ff t;
+    ff_bottom_face(a, K, cur, c, col, &r.bot, &t);
+    r.q = ff_add(r.q, r.bot);
+  }
+  return r;
+}
+
+// k_pic_final in float-float: th^{n+1} = th^n + (dt Q - V Ss (th^n/ths)(h^{n+1} - h^n)) / V,
+// boundary and elastic volumes (summed in FP64 across the grid) and time
+__global__ void __launch_bounds__(256) k_pic_final_ff(ReArgs a, int planes, int tiles) {
+  const double dtd = a.sc->dt_used;
+  const FfConst K = ff_consts(a, dtd);
+  const ff inv_V = ff_div(ff_make(1.0f), K.V);
+  double v[3] = {0.0, 0.0, 0.0};
+  const int t0 = (a.nx + 31) / 32;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i = (tile % t0) * 32 + threadIdx.x;
+    const int j = (tile / t0) * 8 + threadIdx.y;
+    if (i >= a.nx || j >= a.ny) continue;
+    const size_t col = (size_t)i + (size_t)a.nx * j;
+    const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
+    for (int k = kb; k < ke; ++k) {
+      const size_t c = col + a.ncol * k;
+      const SoilClass& kc = class_of(a, c, col);
+      const ff wcn = ff_from_double(a.w_old[c]);
+      const FfRow r = ff_pic_row(a, K, c, col, i, j, k);
+      const ff dh = ff_sub(ff_from_double(a.h_new[c]), ff_from_double(a.h_old[c]));
+      const ff el = ff_mul(ff_mul(K.V, ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn)), dh);
+      a.w_new[c] = ff_to_double(ff_add(wcn, ff_mul(ff_sub(ff_mul(K.dt, r.q), el), inv_V)));
+      if (k == 0) v[0] += ff_to_double(ff_mul(r.top, K.dt));
+      if (k + 1 == a.nz) v[1] += ff_to_double(ff_mul(r.bot, K.dt));
+      v[2] += ff_to_double(el);
+    }
+  }
+  double tot[3];
+  if (grid_sum<3>(v, a.partials, &a.sc->arrive[0], tot) && flat_tid() == 0) {
+    a.sc->vol_top += tot[0];
+    a.sc->vol_bot += tot[1];
+    a.sc->vol_elastic += tot[2];
+    a.sc->time += dtd;
+  }
+}
+
+}  // namespace fg

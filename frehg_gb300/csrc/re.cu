@@ -4,6 +4,7 @@
 #include "internal.h"
 #include "re_kernels.cuh"
 #include "picard.cuh"
+#include "picard_ff.cuh"
 #include "krylov_kernels.cuh"
 
 #include <cmath>
@@ -106,25 +107,6 @@ frehg_re::~frehg_re() {
   if (own_stream) cudaStreamDestroy(own_stream);
 }
 
-static SoilClass make_class(const frehg_soil_params& s) {
-  SoilClass k;
-  k.alpha = s.alpha;
-  k.n = s.n;
-  k.ths = s.theta_s;
-  k.thr = s.theta_r;
-  k.Ksx = s.Ks_x;
-  k.Ksy = s.Ks_y;
-  k.Ksz = s.Ks_z;
-  k.Ss = s.Ss;
-  k.aev = s.air_entry;
-  k.m = 1.0 - 1.0 / s.n;
-  k.inv_m = 1.0 / k.m;
-  k.inv_n = 1.0 / s.n;
-  k.inv_ths = 1.0 / s.theta_s;
-  k.use_vg = s.use_vg;
-  k.use_mvg = s.use_mvg;
-  return k;
-}
 
 static int validate_params(const frehg_re_params* p) {
   FG_ARG(p->dx > 0 && p->dy > 0 && p->dz > 0, "dx, dy, dz must be positive");
@@ -157,7 +139,7 @@ static int validate_params(const frehg_re_params* p) {
 
 static int upload_class0(frehg_re* re) {
   if (re->nclass > 0 && re->cid) return FREHG_OK;  // a soil map owns the table
-  const SoilClass k = make_class(re->p.soil);
+  const SoilClass k = make_soil_class(re->p.soil);
   if (!re->cls) FG_CUDA(cudaMalloc(&re->cls, sizeof(SoilClass) * 256));
   FG_CUDA(cudaMemcpy(re->cls, &k, sizeof(SoilClass), cudaMemcpyHostToDevice));
   re->nclass = 1;
@@ -462,6 +444,8 @@ static int time_network(frehg_re* re) {
 static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
   cudaStream_t st = re->stream;
   frehg_solver_config cfg = re->cfg;
+  // a Picard solve yields an update of the iterate: its operator may carry 48 bits
+  re->ksp.ff_operator = re->p.scheme == 1 && !re->p.picard_fp64;
   const bool learned = !strncmp(cfg.pc_type, "unet", 4);
   re->ksp.net = NetPrecond();
   bool use_net = false;
@@ -630,13 +614,25 @@ static int picard_step(frehg_re* re) {
     bool converged = false;
     int fail = FREHG_OK;
     for (its = 0; its < re->p.picard_max_it; ++its) {
-      FG_LAUNCH(prof, st, "k_kr", (32.0 + sb) * n,
-                (k_constit<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch, re->cap)));
+      if (re->p.picard_fp64)
+        FG_LAUNCH(prof, st, "k_kr", (32.0 + sb) * n,
+                  (k_constit<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch,
+                                                             re->cap)));
+      else
+        FG_LAUNCH(prof, st, "k_kr_ff", (32.0 + sb) * n,
+                  (k_constit_ff<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch,
+                                                                re->cap)));
       re->A.scaled = false;
-      FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
-                k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
-                                                             re->A.a2, re->A.b, PL.planes,
-                                                             PL.tiles));
+      if (re->p.picard_fp64)
+        FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
+                  k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
+                                                               re->A.a2, re->A.b, PL.planes,
+                                                               PL.tiles));
+      else
+        FG_LAUNCH(prof, st, "k_pic_assemble_ff", (64.0 + sb) * n,
+                  k_pic_assemble_ff<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0,
+                                                                  re->A.a1, re->A.a2, re->A.b,
+                                                                  PL.planes, PL.tiles));
       FG_CUDA(cudaGetLastError());
       CgResult res;
       const int rc = solve_system(re, re->scratch, &res);
@@ -677,8 +673,12 @@ static int picard_step(frehg_re* re) {
     }
     dt = fmax(0.5 * dt, dt_floor);
   }
-  FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n,
-            k_pic_final<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
+  if (re->p.picard_fp64)
+    FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n,
+              k_pic_final<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
+  else
+    FG_LAUNCH(prof, st, "k_pic_final_ff", (48.0 + sb) * n,
+              k_pic_final_ff<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
   FG_CUDA(cudaGetLastError());
   re->cnt.last_picard_iterations = its;
   if (re->p.picard_dt_adapt) {
@@ -844,7 +844,7 @@ int frehg_re_set_soil_map(frehg_re* re, const frehg_soil_params* classes, int nc
     ids[c] = (uint8_t)class_index[c];
   }
   std::vector<SoilClass> tab(nclass);
-  for (int q = 0; q < nclass; ++q) tab[q] = make_class(classes[q]);
+  for (int q = 0; q < nclass; ++q) tab[q] = make_soil_class(classes[q]);
   if (!re->cls) FG_CUDA(cudaMalloc(&re->cls, sizeof(SoilClass) * 256));
   FG_CUDA(cudaStreamSynchronize(re->stream));
   FG_CUDA(cudaMemcpy(re->cls, tab.data(), sizeof(SoilClass) * nclass, cudaMemcpyHostToDevice));
@@ -1067,7 +1067,7 @@ int frehg_re_surface_exchange(frehg_re* re, double* eta, const double* bottom, d
                             cudaMemcpyDeviceToDevice, st));
     re->top_ghost_stale = true;
   }
-  const SoilClass k0 = make_class(re->p.soil);
+  const SoilClass k0 = make_soil_class(re->p.soil);
   const int nb = (int)std::min<size_t>((nc + 255) / 256, (size_t)kNumSMs * 8);
   k_surface_exchange<<<nb, 256, 0, st>>>(re->H[re->cur], re->W[re->cur], d_eta, d_bot, d_q, k0,
                                          (int)nc, re->p.dx * re->p.dy, re->p.dz, dt, visc,

@@ -166,6 +166,34 @@ __global__ void k_constit(ReArgs a, const double* __restrict__ h, double* __rest
   }
 }
 
+// k_constit with the van Genuchten classes evaluated in float-float arithmetic on the FP32 pipe
+// (vg_constit_ff); MVG and exponential classes take the FP64 forms
+template <bool THETA, bool CAP>
+__global__ void k_constit_ff(ReArgs a, const double* __restrict__ h, double* __restrict__ kr,
+                             double* __restrict__ th, double* __restrict__ cap) {
+  const bool col_map = a.soil.cid && !a.soil.cid3d;
+  const bool small = a.n <= 0xffffffffull;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = !col_map ? 0
+                       : small  ? (size_t)((uint32_t)c % (uint32_t)a.ncol)
+                                : c % a.ncol;
+    const int id = a.soil.cid ? (int)a.soil.cid[a.soil.cid3d ? c : col] : 0;
+    const SoilClass& k = a.soil.cls[id];
+    const double hc = h[c];
+    Constit r;
+    if (k.use_vg && !k.use_mvg) {
+      const double alpha = a.soil.alpha ? a.soil.alpha[c] : k.alpha;
+      r = vg_constit_ff<THETA, CAP>(k, alpha, a.soil.continuous_theta ? 0.0 : k.aev, hc);
+    } else {
+      r = vg_constit<THETA, CAP>(soil_of(a.soil, c, col), hc);
+    }
+    kr[c] = r.kr;
+    if (THETA) th[c] = r.theta;
+    if (CAP) cap[c] = r.cap;
+  }
+}
+
 // groundwaterMatCoeff + groundwaterRhs + the COO rows of assembleAndSolve, written as the
 // diagonal (into A.s), the +x/+y/+z couplings and b.
 __global__ void __launch_bounds__(256) k_assemble(ReArgs a, double* __restrict__ dg,

@@ -10,7 +10,9 @@
 
 #include <cstdint>
 
+#include "../../include/frehg_gb300.h"
 #include "fastmath64.cuh"
+#include "ff32.cuh"
 
 namespace fg {
 
@@ -20,7 +22,48 @@ struct SoilClass {
   double alpha, n, ths, thr, Ksx, Ksy, Ksz, Ss, aev;
   double m, inv_m, inv_n, inv_ths;
   int32_t use_vg, use_mvg;
+  // float-float copies (hi, lo) for vg_constit_ff: alpha, n, m, theta_r, theta_s - theta_r,
+  // n m (theta_s - theta_r); for the float-float Picard kernels: Ks_x, Ks_y, Ks_z, Ss/theta_s
+  float ff_alpha[2], ff_n[2], ff_m[2], ff_thr[2], ff_dth[2], ff_nmdth[2];
+  float ff_ks[3][2], ff_ss_ths[2];
+  int32_t ks_iso;  // Ks_x == Ks_y == Ks_z
 };
+
+// SoilClass of one parameter block (host)
+inline SoilClass make_soil_class(const frehg_soil_params& s) {
+  SoilClass k;
+  k.alpha = s.alpha;
+  k.n = s.n;
+  k.ths = s.theta_s;
+  k.thr = s.theta_r;
+  k.Ksx = s.Ks_x;
+  k.Ksy = s.Ks_y;
+  k.Ksz = s.Ks_z;
+  k.Ss = s.Ss;
+  k.aev = s.air_entry;
+  k.m = 1.0 - 1.0 / s.n;
+  k.inv_m = 1.0 / k.m;
+  k.inv_n = 1.0 / s.n;
+  k.inv_ths = 1.0 / s.theta_s;
+  k.use_vg = s.use_vg;
+  k.use_mvg = s.use_mvg;
+  auto split = [](double v, float* out) {
+    out[0] = (float)v;
+    out[1] = (float)(v - (double)out[0]);
+  };
+  split(k.alpha, k.ff_alpha);
+  split(k.n, k.ff_n);
+  split(k.m, k.ff_m);
+  split(k.thr, k.ff_thr);
+  split(k.ths - k.thr, k.ff_dth);
+  split(k.n * k.m * (k.ths - k.thr), k.ff_nmdth);
+  split(k.Ksx, k.ff_ks[0]);
+  split(k.Ksy, k.ff_ks[1]);
+  split(k.Ksz, k.ff_ks[2]);
+  split(k.Ss / k.ths, k.ff_ss_ths);
+  k.ks_iso = (k.Ksx == k.Ksy && k.Ksx == k.Ksz) ? 1 : 0;
+  return k;
+}
 
 // Soil of one cell after the per-cell overrides (not in reference: continuous Ks / alpha).
 struct CellSoil {
@@ -215,6 +258,63 @@ __device__ __forceinline__ Constit vg_constit(const CellSoil& s, double h) {
     r.cap = c;
   } else {
     r.cap = 0.0;
+  }
+  return r;
+}
+
+// vg_constit in float-float arithmetic on the FP32 pipe (ff32.cuh): the same relations, caps and
+// saturated branches, about 48 significant bits per operation instead of 53, for the VG branch
+// (MVG and the exponential model take vg_constit).  Where the soil is drier than |alpha h| = 1,
+// (1 - se^{1/m})^m is formed from ln(1 + 1/t) rather than from the difference nL - u, so dry
+// cells keep the relative accuracy of K that the FP64 forms (and the reference's pow forms)
+// lose there.  k: the cell's class (its
+// float-float constants); alpha: the cell's alpha (class value or per-cell field); aev: the
+// head above which theta = theta_s.  Heads h >= 0 (and |alpha h| too small for the float range)
+// give kr = 1, C = 0 and theta_s exactly, as the FP64 forms do.
+template <bool WANT_THETA, bool WANT_CAP>
+__device__ __forceinline__ Constit vg_constit_ff(const SoilClass& k, double alpha, double aev,
+                                                 double h) {
+  Constit r;
+  r.kr = 1.0;
+  r.theta = k.ths;
+  r.cap = 0.0;
+  const ff ah = ff_mul(ff_from_double(alpha), ff_from_double(-h));  // |alpha h| for h < 0
+  if (!(ah.h > 0.0f)) return r;
+  const ff n = ff_make(k.ff_n[0], k.ff_n[1]);
+  const ff m = ff_make(k.ff_m[0], k.ff_m[1]);
+  const ff L = ff_log(ah);
+  const ff nL = ff_mul(n, L);
+  const ff t = ff_exp(nL);
+  // u = ln(1 + t) and y = m (nL - u) = m ln(t / (1 + t)); for t > 1 (drier than |alpha h| = 1)
+  // as u = nL + v, y = -m v with v = ln(1 + 1/t), so that y keeps its relative accuracy where
+  // nL and u nearly cancel (the FP64 forms lose about log10(t) digits there)
+  ff u, y;
+  if (t.h > 1.0f) {
+    const ff v = ff_log1p(ff_div(ff_make(1.0f), t));
+    u = ff_add_fast(nL, v);
+    y = ff_neg(ff_mul(m, v));
+  } else {
+    u = ff_log1p(t);
+    y = ff_mul(m, ff_sub(nL, u));
+  }
+  const ff mu = ff_mul(m, u);
+  const ff one_minus = ff_neg(ff_expm1(y));
+  const ff se_half = ff_exp(ff_scale(mu, -0.5f));
+  const ff kr = ff_mul(se_half, ff_sqr(one_minus));
+  r.kr = ff_ge1(kr) ? 1.0 : ff_to_double(kr);
+  const ff se = ff_sqr(se_half);
+  if (WANT_THETA && !(h > aev)) {
+    // theta_r + (theta_s - theta_r) se with se in [0, 1]: theta_s where se rounds to >= 1
+    const ff wc = ff_add_fast(ff_make(k.ff_thr[0], k.ff_thr[1]),
+                              ff_mul(ff_make(k.ff_dth[0], k.ff_dth[1]), se));
+    r.theta = ff_ge1(se) ? k.ths : ff_to_double(wc);
+  }
+  if (WANT_CAP) {
+    // alpha n m (ths - thr) t se / (|alpha h| (1 + t))
+    const ff num = ff_mul(ff_mul(ff_from_double(alpha), ff_make(k.ff_nmdth[0], k.ff_nmdth[1])),
+                          ff_mul(t, se));
+    const ff den = ff_mul(ah, ff_add_f(t, 1.0f));
+    r.cap = ff_to_double(ff_div(num, den));
   }
   return r;
 }

@@ -101,7 +101,9 @@ typedef struct frehg_re_params {
                              admits (no ponding, the excess runs off); 0 disables             */
   double rain_until;      /* [s]                                                             */
   int32_t picard_dt_adapt;/* Picard-count driven dt (1) or fixed (0)                         */
-  int32_t pad_;
+  int32_t picard_fp64;    /* Picard constitutive relations (van Genuchten classes) in native
+                             FP64 (1) or in float-float arithmetic on the FP32 pipe, ~48
+                             significant bits, several times faster on GB300 (0, default)    */
   double picard_dh_max;   /* largest head change one Picard iteration applies per cell [m];
                              0 = unlimited (default)                                         */
 } frehg_re_params;
@@ -374,10 +376,20 @@ int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const doub
 /* Build information: returns the sm architecture the library was compiled for (e.g. 103). */
 int frehg_build_arch(void);
 
-/* Self-check of the library's FP64 elementary functions (not in reference): y[i] = f(x[i]) for
- * host arrays of n values, f = the library's exp, log, log1p, expm1 (fn 0-3) as used by the
- * constitutive kernels, or the CUDA math library's (fn 4-7) for comparison. */
+/* Self-check of the library's elementary functions (not in reference): y[i] = f(x[i]) for
+ * host arrays of n values, f = the library's FP64 exp, log, log1p, expm1 (fn 0-3) as used by
+ * the constitutive kernels, the CUDA math library's (fn 4-7) for comparison, or the
+ * float-float exp, log, log1p, expm1 (fn 8-11), the double -> float-float -> double round trip
+ * (fn 12) and the float-float reciprocal (fn 13), each with the argument split from a double
+ * and the result summed back into one. */
 int frehg_fastmath_eval(int fn, const double* x, double* y, int64_t n);
+
+/* Self-check of the constitutive evaluation (not in reference): K/Ks, theta and C at n heads
+ * (host arrays) for one soil, by the FP64 forms (arith 0) or the float-float forms of the
+ * Picard kernels (arith 1); continuous_theta 1 drops the air-entry switch of theta as the
+ * Picard scheme does. */
+int frehg_constit_eval(const frehg_soil_params* soil, int arith, int continuous_theta,
+                       const double* h, int64_t n, double* kr, double* wc, double* cap);
 
 #ifdef __cplusplus
 }

@@ -1,7 +1,8 @@
 """GPU mixed-form modified Picard step vs the oracle's FP64 statement of it (not in reference).
 
 Per step: head within 1e-8 m (max norm), equal Picard iteration counts; cumulative mass
-balance closes below 1e-12 relative on the GPU."""
+balance closes below 1e-12 relative on the GPU.  The GPU kernels run in float-float arithmetic
+(the default, picard_fp64 = 0) unless a test selects native FP64 (picard_fp64 = 1)."""
 import numpy as np
 import pytest
 
@@ -38,17 +39,22 @@ def test_config0_picard_small(gpu_lib, oracle_mod):
     run_compare(g, o, w.steps)
 
 
-def test_config0_picard_harmonic(gpu_lib, oracle_mod):
+@pytest.mark.parametrize("fp64", [0, 1])
+def test_config0_picard_harmonic(gpu_lib, oracle_mod, fp64):
     w = W.config0("picard", nx=8, ny=6, nz=30, steps=8)
     w.params.face_mean = 1
+    w.params.picard_fp64 = fp64
     g, o = pair(w, oracle_mod)
     run_compare(g, o, w.steps)
 
 
-def test_config1_picard_small(gpu_lib, oracle_mod):
+@pytest.mark.parametrize("fp64", [0, 1])
+def test_config1_picard_small(gpu_lib, oracle_mod, fp64):
     w = W.config1("picard", nx=16, ny=12, nz=24, steps=6)
+    w.params.picard_fp64 = fp64
     g, o = pair(w, oracle_mod)
-    run_compare(g, o, w.steps)
+    worst = run_compare(g, o, w.steps)
+    print(f"\n  picard_fp64={fp64}: max head difference to the oracle {worst:.2e} m")
 
 
 def test_rain_pulse_and_picard_dt(gpu_lib, oracle_mod):
