@@ -151,11 +151,13 @@ __device__ __forceinline__ ff ff_from_double(double x) {
 // instructions.
 // x rounded to a float (to nearest, ties away from zero) without a double->float conversion:
 // the significand's leading 24 bits plus the first dropped bit, added as an integer (a carry
-// moves into the exponent).  0, subnormal, huge, inf and NaN x take the conversion instruction.
+// moves into the exponent).  |x| below the normal float range gives a signed zero; huge, inf and
+// NaN x take the conversion instruction.
 __device__ __forceinline__ float ff_hi_of(double x) {
   const int hx = __double2hiint(x);
   const int E = (hx >> 20) & 0x7ff;
-  if (E < 1023 - 126 || E > 1023 + 126) return ff_from_double_rare(x).h;
+  if (E < 1023 - 126) return __int_as_float(hx & (int)0x80000000);
+  if (E > 1023 + 126) return ff_from_double_rare(x).h;
   const unsigned lx = (unsigned)__double2loint(x);
   return __int_as_float(((hx & (int)0x80000000) | ((E - 1023 + 127) << 23) |
                          ((hx & 0x000fffff) << 3) | (int)(lx >> 29)) +
@@ -302,9 +304,12 @@ __device__ __forceinline__ ff ff_log(ff x) {
   // e ln2 = e L1 (exact) + e L2 (exact as a product pair) + e L3
   const float ef = (float)e;
   const ff el2 = two_prod(ef, kFfLn2L2);
-  ff a = ff_add(ff_make(__fmul_rn(ef, kFfLn2L1)), ff_make(el2.h, __fmaf_rn(ef, kFfLn2L3, el2.l)));
-  a = ff_add(a, ff_make(L.z, L.w));
-  return ff_add(a, p);
+  // the sums need absolute accuracy only (every logarithm here feeds an exponential): the
+  // double-word additions whose error is a few u^2 of the operands serve
+  ff a = ff_add_fast(ff_make(__fmul_rn(ef, kFfLn2L1)),
+                     ff_make(el2.h, __fmaf_rn(ef, kFfLn2L3, el2.l)));
+  a = ff_add_fast(a, ff_make(L.z, L.w));
+  return ff_add_fast(a, p);
 }
 
 // ln(1 + t), t >= 0 (or t > -1)

@@ -61,6 +61,12 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     }
     v[1] = v[2];
   } else {
+    // the sums of squares in FP32 (compensated), after scaling by the previous sweep's norms,
+    // which keeps the terms far from the FP32 range limits: they only set the inner scale and
+    // the stopping test, and the FP64 pipe stays with the stencil product
+    const double rs0 = ir->a, rs1 = ir->ir_rnorm;
+    const float sig0 = (float)(1.0 / rs0), sig1 = (float)(1.0 / rs1);
+    Kahan32 k0, k1;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
       const int i0 = (tile % t0) * 32 + threadIdx.x;
       const int i1 = (tile / t0) * 8 + threadIdx.y;
@@ -78,11 +84,14 @@ __global__ void __launch_bounds__(256) k_ir_residual(
         const double r = fma(s[c], b[c], -ax);
         rres[c] = r;
         ef[c] = 0.0f;
-        v[0] = fma(r, r, v[0]);
-        const double ru = r * sq[c];  // r~ / s = D^1/2 r~
-        v[1] = fma(ru, ru, v[1]);
+        const float rf = ff_hi_of(r);
+        const float q0 = rf * sig0, q1 = rf * ff_hi_of(sq[c]) * sig1;  // sq r~ = r~ / s
+        k0.add(q0 * q0);
+        k1.add(q1 * q1);
       }
     }
+    v[0] = k0.value() * rs0 * rs0;
+    v[1] = k1.value() * rs1 * rs1;
   }
   double tot[3];
   if (!grid_sum<3>(v, partials, &ir->arrive[0], tot)) return;

@@ -5,10 +5,14 @@
 // rate, and the FP64 forms of these kernels are bound by that pipe, not by memory.
 //
 // Doubles are read and split into float-float with integer operations; results are written
-// back as doubles.  The residual keeps the accuracy the fixed point needs (absolute errors of
-// a few 2^-48 of its terms); the face fluxes of two neighbouring cells are exact negatives of
-// each other (the face mean takes its arguments in index order, the head difference changes
-// sign exactly), so the water budget of the final update closes to rounding as in FP64.
+// back as doubles.  The matrix (diagonal and couplings) is formed from the leading floats of
+// the float-float transmissibilities: it shapes each Picard update, not the fixed point the
+// iteration converges to, and the mixed-precision solve rounds it to FP32 anyway.  Sums use
+// the double-word addition whose error is a few 2^-48 of the operands (not of the result): the
+// residual, which fixes the iteration's fixed point, needs absolute accuracy relative to its
+// largest terms.  The face fluxes of two neighbouring cells are exact negatives of each other
+// (the face mean takes its arguments in index order, the head difference changes sign
+// exactly), so the water budget of the final update closes to rounding as in FP64.
 #pragma once
 
 #include "picard.cuh"
@@ -55,6 +59,10 @@ __device__ __forceinline__ ff ff_face_mean(int harmonic, ff lo, ff hi) {
 }
 
 __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+
+// a - b with SloppyDWPlusDW (absolute error a few 2^-48 (|a| + |b|)); antisymmetric:
+// ff_dif(a, b) = -ff_dif(b, a) exactly, so the two cells of a face see opposite fluxes
+__device__ __forceinline__ ff ff_dif(ff a, ff b) { return ff_add_fast(a, ff_neg(b)); }
 
 // geometric factors and boundary values of a launch, float-float
 struct FfConst {
@@ -124,13 +132,14 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
 
 // k_pic_assemble in float-float: same launch shape and face sharing (x faces by warp shuffle,
 // z faces carried down the column, and here the cell below carried as the next level's cell)
-__global__ void __launch_bounds__(256) k_pic_assemble_ff(ReArgs a, double* __restrict__ dg,
+__global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __restrict__ dg,
                                                          double* __restrict__ a0,
                                                          double* __restrict__ a1,
                                                          double* __restrict__ a2,
                                                          double* __restrict__ bvec, int planes,
                                                          int tiles) {
   const FfConst K = ff_consts(a, a.sc->dt_used);
+  const float dtf = K.dt.h, Vf = K.V.h;
   const int hm = a.face_mean;
   const int t0 = (a.nx + 31) / 32;
   const int lane = threadIdx.x;
@@ -143,14 +152,16 @@ __global__ void __launch_bounds__(256) k_pic_assemble_ff(ReArgs a, double* __res
     const size_t col = act ? (size_t)i + (size_t)a.nx * j : 0;
     const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
     FfCell cur = {zero, zero, zero, zero};
-    ff tzm = zero, fzm = zero;  // top face of the current cell
+    ff fzm = zero;     // flux into the current cell through its top face
+    float tzm = 0.0f;  // and that face's transmissibility (leading float)
     if (act && kb < ke) {
       cur = ff_cell(a, col + a.ncol * kb, col);
       if (kb > 0) {
         const FfCell up = ff_cell(a, col + a.ncol * (kb - 1), col);
         const ff kf = ff_face_mean(hm, up.kz, cur.kz);
-        tzm = ff_mul(kf, K.cz);
-        fzm = ff_add(ff_mul(tzm, ff_sub(up.h, cur.h)), ff_mul(K.Az, kf));
+        const ff t = ff_mul(kf, K.cz);
+        tzm = t.h;
+        fzm = ff_add_fast(ff_mul(t, ff_dif(up.h, cur.h)), ff_mul(K.Az, kf));
       }
     }
     for (int k = kb; k < ke; ++k) {
@@ -158,85 +169,89 @@ __global__ void __launch_bounds__(256) k_pic_assemble_ff(ReArgs a, double* __res
       // +x face from the next lane's cell (lane 31 loads its neighbour)
       ff Kxn = ff_make(__shfl_down_sync(full, cur.kx.h, 1), __shfl_down_sync(full, cur.kx.l, 1));
       ff hxn = ff_make(__shfl_down_sync(full, cur.h.h, 1), __shfl_down_sync(full, cur.h.l, 1));
-      ff tx = zero, fxp = zero;
+      float tx = 0.0f;
+      ff fxp = zero;
       if (act && i + 1 < a.nx) {
         if (lane == 31) {
           const FfCell nb = ff_cell(a, c + 1, col + 1);
           Kxn = nb.kx;
           hxn = nb.h;
         }
-        tx = ff_mul(ff_face_mean(hm, cur.kx, Kxn), K.cx);
-        fxp = ff_mul(tx, ff_sub(hxn, cur.h));
+        const ff t = ff_mul(ff_face_mean(hm, cur.kx, Kxn), K.cx);
+        tx = t.h;
+        fxp = ff_mul(t, ff_dif(hxn, cur.h));
       }
       // -x face: the previous lane's +x face (lane 0 evaluates its own)
-      ff txm = ff_make(__shfl_up_sync(full, tx.h, 1), __shfl_up_sync(full, tx.l, 1));
+      float txm = __shfl_up_sync(full, tx, 1);
       ff fxm = ff_neg(ff_make(__shfl_up_sync(full, fxp.h, 1), __shfl_up_sync(full, fxp.l, 1)));
       if (!act) continue;  // after the shuffles: every lane took part in them
       if (i == 0) {
-        txm = zero;
+        txm = 0.0f;
         fxm = zero;
       } else if (lane == 0) {
         const FfCell nb = ff_cell(a, c - 1, col - 1);
-        txm = ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx);
-        fxm = ff_mul(txm, ff_sub(nb.h, cur.h));
+        const ff t = ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx);
+        txm = t.h;
+        fxm = ff_mul(t, ff_dif(nb.h, cur.h));
       }
-      ff q = ff_add(fxm, fxp);
-      ff tsum = ff_add_fast(txm, tx);
+      ff q = ff_add_fast(fxm, fxp);
+      float tsum = txm + tx;
       // y faces
-      ff ty = zero;
+      float ty = 0.0f;
       if (j > 0) {
         const FfCell nb = ff_cell(a, c - a.nx, col - a.nx);
         const ff t = ff_mul(ff_face_mean(hm, nb.ky, cur.ky), K.cy);
-        q = ff_add(q, ff_mul(t, ff_sub(nb.h, cur.h)));
-        tsum = ff_add_fast(tsum, t);
+        q = ff_add_fast(q, ff_mul(t, ff_dif(nb.h, cur.h)));
+        tsum += t.h;
       }
       if (j + 1 < a.ny) {
         const FfCell nb = ff_cell(a, c + a.nx, col + a.nx);
-        ty = ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy);
-        q = ff_add(q, ff_mul(ty, ff_sub(nb.h, cur.h)));
-        tsum = ff_add_fast(tsum, ty);
+        const ff t = ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy);
+        ty = t.h;
+        q = ff_add_fast(q, ff_mul(t, ff_dif(nb.h, cur.h)));
+        tsum += ty;
       }
       const SoilClass& kc = class_of(a, c, col);
       // face above: carried, or the top boundary
       if (k > 0) {
-        q = ff_add(q, fzm);
-        tsum = ff_add_fast(tsum, tzm);
+        q = ff_add_fast(q, fzm);
+        tsum += tzm;
       } else {
         ff f, t;
         ff_top_face(a, K, cur, kc, c, col, &f, &t);
-        q = ff_add(q, f);
-        tsum = ff_add_fast(tsum, t);
+        q = ff_add_fast(q, f);
+        tsum += t.h;
       }
       // face below: evaluated here and carried to the next level with the cell below
-      ff tz = zero;
+      float tz = 0.0f;
       FfCell below = cur;
       if (k + 1 < a.nz) {
         below = ff_cell(a, c + a.ncol, col);
         const ff kf = ff_face_mean(hm, cur.kz, below.kz);
-        tz = ff_mul(kf, K.cz);
-        const ff fz = ff_sub(ff_mul(tz, ff_sub(below.h, cur.h)), ff_mul(K.Az, kf));
-        q = ff_add(q, fz);
-        tsum = ff_add_fast(tsum, tz);
+        const ff t = ff_mul(kf, K.cz);
+        tz = t.h;
+        const ff fz = ff_dif(ff_mul(t, ff_dif(below.h, cur.h)), ff_mul(K.Az, kf));
+        q = ff_add_fast(q, fz);
+        tsum += tz;
         tzm = tz;
         fzm = ff_neg(fz);
       } else {
         ff f, t;
         ff_bottom_face(a, K, cur, c, col, &f, &t);
-        q = ff_add(q, f);
-        tsum = ff_add_fast(tsum, t);
+        q = ff_add_fast(q, f);
+        tsum += t.h;
       }
-      // diagonal V (C + Ss wcn/ths) + dt sum T, couplings -dt T, rhs -Rdt with
-      // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q
+      // diagonal V (C + Ss wcn/ths) + dt sum T and couplings -dt T (FP32), rhs -Rdt with
+      // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q (float-float)
       const ff wcn = ff_from_double(a.w_old[c]);
       const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
-      dg[c] = ff_to_double(ff_add_fast(ff_mul(K.V, ff_add_fast(ff_from_double(a.cap[c]), st)),
-                                       ff_mul(K.dt, tsum)));
-      a0[c] = -ff_to_double(ff_mul(K.dt, tx));
-      a1[c] = -ff_to_double(ff_mul(K.dt, ty));
-      a2[c] = -ff_to_double(ff_mul(K.dt, tz));
-      const ff dth = ff_sub(ff_from_double(a.wch[c]), wcn);
-      const ff dh = ff_sub(cur.h, ff_from_double(a.h_old[c]));
-      const ff rdt = ff_sub(ff_mul(K.V, ff_add(dth, ff_mul(st, dh))), ff_mul(K.dt, q));
+      dg[c] = (double)fmaf(dtf, tsum, Vf * (ff_hi_of(a.cap[c]) + st.h));
+      a0[c] = (double)(-dtf * tx);
+      a1[c] = (double)(-dtf * ty);
+      a2[c] = (double)(-dtf * tz);
+      const ff dth = ff_dif(ff_from_double(a.wch[c]), wcn);
+      const ff dh = ff_dif(cur.h, ff_from_double(a.h_old[c]));
+      const ff rdt = ff_dif(ff_mul(K.V, ff_add_fast(dth, ff_mul(st, dh))), ff_mul(K.dt, q));
       bvec[c] = -ff_to_double(rdt);
       cur = below;
     }
@@ -256,37 +271,37 @@ __device__ __forceinline__ FfRow ff_pic_row(const ReArgs& a, const FfConst& K, s
   FfRow r = {ff_make(0.0f), ff_make(0.0f), ff_make(0.0f)};
   if (i > 0) {
     const FfCell nb = ff_cell(a, c - 1, col - 1);
-    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx), ff_sub(nb.h, cur.h)));
+    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx), ff_dif(nb.h, cur.h)));
   }
   if (i + 1 < a.nx) {
     const FfCell nb = ff_cell(a, c + 1, col + 1);
-    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.kx, nb.kx), K.cx), ff_sub(nb.h, cur.h)));
+    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.kx, nb.kx), K.cx), ff_dif(nb.h, cur.h)));
   }
   if (j > 0) {
     const FfCell nb = ff_cell(a, c - a.nx, col - a.nx);
-    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.ky, cur.ky), K.cy), ff_sub(nb.h, cur.h)));
+    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.ky, cur.ky), K.cy), ff_dif(nb.h, cur.h)));
   }
   if (j + 1 < a.ny) {
     const FfCell nb = ff_cell(a, c + a.nx, col + a.nx);
-    r.q = ff_add(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy), ff_sub(nb.h, cur.h)));
+    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy), ff_dif(nb.h, cur.h)));
   }
   if (k > 0) {
     const FfCell nb = ff_cell(a, c - a.ncol, col);
     const ff kf = ff_face_mean(hm, nb.kz, cur.kz);
-    r.q = ff_add(r.q, ff_add(ff_mul(ff_mul(kf, K.cz), ff_sub(nb.h, cur.h)), ff_mul(K.Az, kf)));
+    r.q = ff_add_fast(r.q, ff_add_fast(ff_mul(ff_mul(kf, K.cz), ff_dif(nb.h, cur.h)), ff_mul(K.Az, kf)));
   } else {
     ff t;
     ff_top_face(a, K, cur, class_of(a, c, col), c, col, &r.top, &t);
-    r.q = ff_add(r.q, r.top);
+    r.q = ff_add_fast(r.q, r.top);
   }
   if (k + 1 < a.nz) {
     const FfCell nb = ff_cell(a, c + a.ncol, col);
     const ff kf = ff_face_mean(hm, cur.kz, nb.kz);
-    r.q = ff_add(r.q, ff_sub(ff_mul(ff_mul(kf, K.cz), ff_sub(nb.h, cur.h)), ff_mul(K.Az, kf)));
+    r.q = ff_add_fast(r.q, ff_dif(ff_mul(ff_mul(kf, K.cz), ff_dif(nb.h, cur.h)), ff_mul(K.Az, kf)));
   } else {
     ff t;
     ff_bottom_face(a, K, cur, c, col, &r.bot, &t);
-    r.q = ff_add(r.q, r.bot);
+    r.q = ff_add_fast(r.q, r.bot);
   }
   return r;
 }
@@ -310,9 +325,9 @@ __global__ void __launch_bounds__(256) k_pic_final_ff(ReArgs a, int planes, int 
       const SoilClass& kc = class_of(a, c, col);
       const ff wcn = ff_from_double(a.w_old[c]);
       const FfRow r = ff_pic_row(a, K, c, col, i, j, k);
-      const ff dh = ff_sub(ff_from_double(a.h_new[c]), ff_from_double(a.h_old[c]));
+      const ff dh = ff_dif(ff_from_double(a.h_new[c]), ff_from_double(a.h_old[c]));
       const ff el = ff_mul(ff_mul(K.V, ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn)), dh);
-      a.w_new[c] = ff_to_double(ff_add(wcn, ff_mul(ff_sub(ff_mul(K.dt, r.q), el), inv_V)));
+      a.w_new[c] = ff_to_double(ff_add_fast(wcn, ff_mul(ff_dif(ff_mul(K.dt, r.q), el), inv_V)));
       if (k == 0) v[0] += ff_to_double(ff_mul(r.top, K.dt));
       if (k + 1 == a.nz) v[1] += ff_to_double(ff_mul(r.bot, K.dt));
       v[2] += ff_to_double(el);

@@ -169,8 +169,10 @@ __global__ void k_constit(ReArgs a, const double* __restrict__ h, double* __rest
 // k_constit with the van Genuchten classes evaluated in float-float arithmetic on the FP32 pipe
 // (vg_constit_ff); MVG and exponential classes take the FP64 forms
 template <bool THETA, bool CAP>
-__global__ void k_constit_ff(ReArgs a, const double* __restrict__ h, double* __restrict__ kr,
-                             double* __restrict__ th, double* __restrict__ cap) {
+__global__ void __launch_bounds__(256, 4) k_constit_ff(ReArgs a, const double* __restrict__ h,
+                                                       double* __restrict__ kr,
+                                                       double* __restrict__ th,
+                                                       double* __restrict__ cap) {
   const bool col_map = a.soil.cid && !a.soil.cid3d;
   const bool small = a.n <= 0xffffffffull;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
