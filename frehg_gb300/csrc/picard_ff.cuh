@@ -130,26 +130,45 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
   }
 }
 
-// k_pic_assemble in float-float: same launch shape and face sharing (x faces by warp shuffle,
-// z faces carried down the column, and here the cell below carried as the next level's cell)
+// One level of a (32 x 8)-column tile plus the rows above and below it: the head and the
+// axis-1 conductivity of each cell, float-float (the y faces read their neighbours here).
+struct FfYPlane {
+  float hh[10][32], hl[10][32], kh[10][32], kl[10][32];
+};
+
+// k_pic_assemble in float-float as a tiled stencil: a (32 x 8)-thread block marches its column
+// tile down `planes` levels.  Per level each thread stages its own cell's (h, K_y) in shared
+// memory (threads 0-63 also stage the rows above and below the tile), then, after one barrier,
+// forms the faces: x from the adjacent lanes (warp shuffles; lanes 0 and 31 load their outer
+// neighbour), y from shared memory, z with the cell below, which it loads while the others
+// stage and carries to the next level as its own cell.  The level buffers alternate, so one
+// barrier per level suffices: a buffer is rewritten two levels later, after every thread has
+// passed the barrier that follows its last read.
 __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __restrict__ dg,
-                                                         double* __restrict__ a0,
-                                                         double* __restrict__ a1,
-                                                         double* __restrict__ a2,
-                                                         double* __restrict__ bvec, int planes,
-                                                         int tiles) {
+                                                           double* __restrict__ a0,
+                                                           double* __restrict__ a1,
+                                                           double* __restrict__ a2,
+                                                           double* __restrict__ bvec, int planes,
+                                                           int tiles) {
+  __shared__ FfYPlane ys[2];
   const FfConst K = ff_consts(a, a.sc->dt_used);
   const float dtf = K.dt.h, Vf = K.V.h;
   const int hm = a.face_mean;
   const int t0 = (a.nx + 31) / 32;
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x, row = threadIdx.y;
+  const int tid = row * 32 + lane;
   const unsigned full = 0xffffffffu;
   const ff zero = ff_make(0.0f);
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int i = (tile % t0) * 32 + lane;
-    const int j = (tile / t0) * 8 + threadIdx.y;
+    const int j0 = (tile / t0) * 8, j = j0 + row;
     const bool act = i < a.nx && j < a.ny;
     const size_t col = act ? (size_t)i + (size_t)a.nx * j : 0;
+    // halo rows of the tile: threads 0-31 stage row j0 - 1, threads 32-63 row j0 + 8
+    const int jh = tid < 32 ? j0 - 1 : j0 + 8;
+    const bool act_h = tid < 64 && i < a.nx && jh >= 0 && jh < a.ny;
+    const size_t colh = act_h ? (size_t)i + (size_t)a.nx * jh : 0;
+    const int hrow = tid < 32 ? 0 : 9;
     const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
     FfCell cur = {zero, zero, zero, zero};
     ff fzm = zero;     // flux into the current cell through its top face
@@ -165,7 +184,40 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
       }
     }
     for (int k = kb; k < ke; ++k) {
+      FfYPlane& P = ys[k & 1];
       const size_t c = col + a.ncol * k;
+      // stage this level: the own cell and the halo rows
+      P.hh[row + 1][lane] = cur.h.h;
+      P.hl[row + 1][lane] = cur.h.l;
+      P.kh[row + 1][lane] = cur.ky.h;
+      P.kl[row + 1][lane] = cur.ky.l;
+      if (tid < 64) {
+        FfCell hc = {zero, zero, zero, zero};
+        if (act_h) hc = ff_cell(a, colh + a.ncol * k, colh);
+        P.hh[hrow][lane] = hc.h.h;
+        P.hl[hrow][lane] = hc.h.l;
+        P.kh[hrow][lane] = hc.ky.h;
+        P.kl[hrow][lane] = hc.ky.l;
+      }
+      // raw loads for the cell below (z face, carried to the next level) and for this cell's
+      // residual, issued before the barrier and converted after it, so that their latency
+      // overlaps the barrier and the x and y faces
+      const bool has_below = act && k + 1 < a.nz;
+      const size_t cb = has_below ? c + a.ncol : c;
+      double rb_h = 0.0, rb_kr = 0.0, rb_ks = 0.0;
+      int rb_id = 0;
+      double r_wo = 0.0, r_wch = 0.0, r_ho = 0.0, r_cap = 0.0;
+      if (act) {
+        rb_h = a.h_new[cb];
+        rb_kr = a.kr[cb];
+        if (a.soil.Ks) rb_ks = a.soil.Ks[cb];
+        if (a.soil.cid) rb_id = a.soil.cid[a.soil.cid3d ? cb : col];
+        r_wo = a.w_old[c];
+        r_wch = a.wch[c];
+        r_ho = a.h_old[c];
+        r_cap = a.cap[c];
+      }
+      __syncthreads();
       // +x face from the next lane's cell (lane 31 loads its neighbour)
       ff Kxn = ff_make(__shfl_down_sync(full, cur.kx.h, 1), __shfl_down_sync(full, cur.kx.l, 1));
       ff hxn = ff_make(__shfl_down_sync(full, cur.h.h, 1), __shfl_down_sync(full, cur.h.l, 1));
@@ -184,77 +236,93 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
       // -x face: the previous lane's +x face (lane 0 evaluates its own)
       float txm = __shfl_up_sync(full, tx, 1);
       ff fxm = ff_neg(ff_make(__shfl_up_sync(full, fxp.h, 1), __shfl_up_sync(full, fxp.l, 1)));
-      if (!act) continue;  // after the shuffles: every lane took part in them
-      if (i == 0) {
-        txm = 0.0f;
-        fxm = zero;
-      } else if (lane == 0) {
-        const FfCell nb = ff_cell(a, c - 1, col - 1);
-        const ff t = ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx);
-        txm = t.h;
-        fxm = ff_mul(t, ff_dif(nb.h, cur.h));
-      }
-      ff q = ff_add_fast(fxm, fxp);
-      float tsum = txm + tx;
-      // y faces
-      float ty = 0.0f;
-      if (j > 0) {
-        const FfCell nb = ff_cell(a, c - a.nx, col - a.nx);
-        const ff t = ff_mul(ff_face_mean(hm, nb.ky, cur.ky), K.cy);
-        q = ff_add_fast(q, ff_mul(t, ff_dif(nb.h, cur.h)));
-        tsum += t.h;
-      }
-      if (j + 1 < a.ny) {
-        const FfCell nb = ff_cell(a, c + a.nx, col + a.nx);
-        const ff t = ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy);
-        ty = t.h;
-        q = ff_add_fast(q, ff_mul(t, ff_dif(nb.h, cur.h)));
-        tsum += ty;
-      }
-      const SoilClass& kc = class_of(a, c, col);
-      // face above: carried, or the top boundary
-      if (k > 0) {
-        q = ff_add_fast(q, fzm);
-        tsum += tzm;
-      } else {
-        ff f, t;
-        ff_top_face(a, K, cur, kc, c, col, &f, &t);
-        q = ff_add_fast(q, f);
-        tsum += t.h;
-      }
-      // face below: evaluated here and carried to the next level with the cell below
-      float tz = 0.0f;
       FfCell below = cur;
-      if (k + 1 < a.nz) {
-        below = ff_cell(a, c + a.ncol, col);
-        const ff kf = ff_face_mean(hm, cur.kz, below.kz);
-        const ff t = ff_mul(kf, K.cz);
-        tz = t.h;
-        const ff fz = ff_dif(ff_mul(t, ff_dif(below.h, cur.h)), ff_mul(K.Az, kf));
-        q = ff_add_fast(q, fz);
-        tsum += tz;
-        tzm = tz;
-        fzm = ff_neg(fz);
-      } else {
-        ff f, t;
-        ff_bottom_face(a, K, cur, c, col, &f, &t);
-        q = ff_add_fast(q, f);
-        tsum += t.h;
+      if (act) {
+        if (i == 0) {
+          txm = 0.0f;
+          fxm = zero;
+        } else if (lane == 0) {
+          const FfCell nb = ff_cell(a, c - 1, col - 1);
+          const ff t = ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx);
+          txm = t.h;
+          fxm = ff_mul(t, ff_dif(nb.h, cur.h));
+        }
+        ff q = ff_add_fast(fxm, fxp);
+        float tsum = txm + tx;
+        // y faces from the staged neighbours
+        float ty = 0.0f;
+        if (j > 0) {
+          const ff hn = ff_make(P.hh[row][lane], P.hl[row][lane]);
+          const ff kn = ff_make(P.kh[row][lane], P.kl[row][lane]);
+          const ff t = ff_mul(ff_face_mean(hm, kn, cur.ky), K.cy);
+          q = ff_add_fast(q, ff_mul(t, ff_dif(hn, cur.h)));
+          tsum += t.h;
+        }
+        if (j + 1 < a.ny) {
+          const ff hn = ff_make(P.hh[row + 2][lane], P.hl[row + 2][lane]);
+          const ff kn = ff_make(P.kh[row + 2][lane], P.kl[row + 2][lane]);
+          const ff t = ff_mul(ff_face_mean(hm, cur.ky, kn), K.cy);
+          ty = t.h;
+          q = ff_add_fast(q, ff_mul(t, ff_dif(hn, cur.h)));
+          tsum += ty;
+        }
+        const SoilClass& kc = class_of(a, c, col);
+        // face above: carried, or the top boundary
+        if (k > 0) {
+          q = ff_add_fast(q, fzm);
+          tsum += tzm;
+        } else {
+          ff f, t;
+          ff_top_face(a, K, cur, kc, c, col, &f, &t);
+          q = ff_add_fast(q, f);
+          tsum += t.h;
+        }
+        // face below, carried to the next level
+        float tz = 0.0f;
+        if (has_below) {
+          const SoilClass& kb = a.soil.cls[rb_id];
+          const ff kr = ff_from_double(rb_kr);
+          below.h = ff_from_double(rb_h);
+          if (a.soil.Ks || kb.ks_iso) {
+            below.kx = ff_mul(a.soil.Ks ? ff_from_double(rb_ks)
+                                        : ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
+            below.ky = below.kx;
+            below.kz = below.kx;
+          } else {
+            below.kx = ff_mul(ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
+            below.ky = ff_mul(ff_make(kb.ff_ks[1][0], kb.ff_ks[1][1]), kr);
+            below.kz = ff_mul(ff_make(kb.ff_ks[2][0], kb.ff_ks[2][1]), kr);
+          }
+          const ff kf = ff_face_mean(hm, cur.kz, below.kz);
+          const ff t = ff_mul(kf, K.cz);
+          tz = t.h;
+          const ff fz = ff_dif(ff_mul(t, ff_dif(below.h, cur.h)), ff_mul(K.Az, kf));
+          q = ff_add_fast(q, fz);
+          tsum += tz;
+          tzm = tz;
+          fzm = ff_neg(fz);
+        } else {
+          ff f, t;
+          ff_bottom_face(a, K, cur, c, col, &f, &t);
+          q = ff_add_fast(q, f);
+          tsum += t.h;
+        }
+        // diagonal V (C + Ss wcn/ths) + dt sum T and couplings -dt T (FP32), rhs -Rdt with
+        // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q (float-float)
+        const ff wcn = ff_from_double(r_wo);
+        const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
+        dg[c] = (double)fmaf(dtf, tsum, Vf * (ff_hi_of(r_cap) + st.h));
+        a0[c] = (double)(-dtf * tx);
+        a1[c] = (double)(-dtf * ty);
+        a2[c] = (double)(-dtf * tz);
+        const ff dth = ff_dif(ff_from_double(r_wch), wcn);
+        const ff dh = ff_dif(cur.h, ff_from_double(r_ho));
+        const ff rdt = ff_dif(ff_mul(K.V, ff_add_fast(dth, ff_mul(st, dh))), ff_mul(K.dt, q));
+        bvec[c] = -ff_to_double(rdt);
       }
-      // diagonal V (C + Ss wcn/ths) + dt sum T and couplings -dt T (FP32), rhs -Rdt with
-      // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q (float-float)
-      const ff wcn = ff_from_double(a.w_old[c]);
-      const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
-      dg[c] = (double)fmaf(dtf, tsum, Vf * (ff_hi_of(a.cap[c]) + st.h));
-      a0[c] = (double)(-dtf * tx);
-      a1[c] = (double)(-dtf * ty);
-      a2[c] = (double)(-dtf * tz);
-      const ff dth = ff_dif(ff_from_double(a.wch[c]), wcn);
-      const ff dh = ff_dif(cur.h, ff_from_double(a.h_old[c]));
-      const ff rdt = ff_dif(ff_mul(K.V, ff_add_fast(dth, ff_mul(st, dh))), ff_mul(K.dt, q));
-      bvec[c] = -ff_to_double(rdt);
       cur = below;
     }
+    __syncthreads();  // the next tile restages both buffers
   }
 }
 

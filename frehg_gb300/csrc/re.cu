@@ -1268,6 +1268,9 @@ int frehg_re_attach_unet(frehg_re* re, frehg_unet* net) {
   FG_ARG(re, "null handle");
   FG_ARG(re->nx % 4 == 0 && re->ny % 4 == 0 && re->nz % 4 == 0,
          "the learned preconditioner needs nx, ny, nz divisible by 4");
+  // the time of one network application depends on the network and the grid only: keep it when
+  // the same network is attached again (a restarted run), time it anew otherwise
+  if (net != re->net) re->apply_ms = -1.0;
   re->net = net;
   if (net && !re->lnk_f) {
     FG_CUDA(cudaMalloc(&re->lnk_f, re->n * sizeof(float)));
@@ -1278,7 +1281,6 @@ int frehg_re_attach_unet(frehg_re* re, frehg_unet* net) {
   re->probe_pending = true;
   re->solves_since_probe = 0;
   re->last_plain_ms = 0.0;
-  re->apply_ms = -1.0;
   return FREHG_OK;
 }
 
