@@ -8,13 +8,15 @@ h = -5 m, 50 mm/h rain for 1800 s then none, free-drainage bottom, mixed-form mo
 over the whole grid, all its Picard iterations included.  The timed arm is the learned +
 mixed-precision solver (FP32 flexible CG with z = M_line^-1 r + NN(r) inside FP64 iterative
 refinement to a true relative residual of 1e-12, network time policy and iteration fallback);
-the same steps are then run with the plain FP64 Jacobi-PCG path (rtol 1e-12) for the
-comparison and the head error between the two.  Inputs are seeded and synthetic; the working
-set (> 10 GB) is far larger than L2, so no flush is needed between steps.
+the Picard kernels (constitutive relations, assembly, final update) compute in float-float
+arithmetic on the FP32 pipe (--picard-fp64: native FP64).  The same steps are then run with the
+plain FP64 path (native FP64 Picard kernels, FP64 Jacobi-PCG at rtol 1e-12) for the comparison
+and the head error between the two.  Inputs are seeded and synthetic; the working set (> 10 GB)
+is far larger than L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--config c0..c4] [--scheme pca|picard] [--precision fp64|mixed]
-                    [--pc jacobi|line|unet|unet-line]
+                    [--pc jacobi|line|unet|unet-line] [--picard-fp64]
 
 --impl reference times the CPU restatement of the reference path (oracle/, OpenMP on every
 host core) on a bounded window of the same workload; under torchrun only rank 0 runs it.
@@ -73,6 +75,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-window", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--picard-fp64", action="store_true",
+                    help="Picard kernels in native FP64 instead of float-float on the FP32 pipe")
     ap.add_argument("--profile-steps", type=int, default=1)
     ap.add_argument("--nx", type=int, default=None, help="window of the workload (smaller case)")
     ap.add_argument("--ny", type=int, default=None)
@@ -109,6 +113,7 @@ def workload(args, nx=None, ny=None, precision=None, pc=None):
         w = W.config4(precision=prec, pc=pc if prec else "jacobi", **kw)
     w.solver.precision = prec
     w.solver.pc_type = (pc if prec else "jacobi").encode()
+    w.params.picard_fp64 = 1 if getattr(args, "picard_fp64", False) else 0
     if prec:
         w.solver.ir_rtol = 1e-12
         w.solver.inner_rtol = args.inner_rtol or 1e-6
@@ -498,13 +503,18 @@ def run_gpu(args):
 
     net_roof = network_roofline(net, w, stream) if learned else None
 
-    # the plain FP64 GPU path on the same inputs and steps: throughput and head error
+    # the plain FP64 GPU path on the same inputs and steps (FP64 Jacobi-PCG, native FP64
+    # Picard kernels): throughput and head error
     comparison = None
-    if not args.no_compare and (args.precision != "fp64" or args.pc != "jacobi"):
+    ff_kernels = args.scheme == "picard" and not w.params.picard_fp64
+    if not args.no_compare and (args.precision != "fp64" or args.pc != "jacobi" or ff_kernels):
         torch.cuda.empty_cache()
         from frehg_gb300.abi import SolverConfig
-        w64 = dataclasses.replace(w, solver=SolverConfig("cg", "jacobi", rtol=w.solver.rtol,
-                                                          max_it=w.solver.max_it))
+        p64 = type(w.params).from_buffer_copy(w.params)
+        p64.picard_fp64 = 1
+        w64 = dataclasses.replace(w, params=p64,
+                                  solver=SolverConfig("cg", "jacobi", rtol=w.solver.rtol,
+                                                      max_it=w.solver.max_it))
         s64, ms64, cnt64, _ = time_arm(args, w64, None, stream, barrier, args.steps,
                                        args.warmup)
         ms64 = max_over_ranks(ms64)
@@ -535,11 +545,16 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f64+f32" + ("+bf16" if learned else ""),
+        "dtype": ("f64" if args.precision == "fp64" else "f64+f32" + ("+bf16" if learned else ""))
+                 + ("+ff" if args.scheme == "picard" and not w.params.picard_fp64 else ""),
         "data": "synthetic (seeded soil fields)",
         "config": {"workload": w.name, "cells": w.cells, "scheme": args.scheme,
                    "precision": args.precision, "pc": args.pc, "solver": solver,
                    "parallelism": f"replicas x{world}",
+                   "picard_arith": ("native fp64" if args.scheme != "picard" or w.params.picard_fp64
+                                    else "float-float (two fp32, ~48-bit significand) for the "
+                                         "constitutive relations, assembly and final update; "
+                                         "refinement residual fp64"),
                    "l2": "working set > 1 GB, larger than the 129 MB L2 (no flush needed)",
                    "picard_iterations": cnt["picard_iterations"],
                    "cg_iterations": cnt["ksp_iterations"], "ir_sweeps": cnt["ir_sweeps"],
