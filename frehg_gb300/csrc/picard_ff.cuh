@@ -24,6 +24,12 @@ struct FfCell {
   ff h, kx, ky, kz;
 };
 
+// the axis-1 / axis-2 conductivity of a cell (kx itself when one serves all axes)
+template <bool ISO>
+__device__ __forceinline__ ff cell_ky(const FfCell& c) { return ISO ? c.kx : c.ky; }
+template <bool ISO>
+__device__ __forceinline__ ff cell_kz(const FfCell& c) { return ISO ? c.kx : c.kz; }
+
 __device__ __forceinline__ const SoilClass& class_of(const ReArgs& a, size_t c, size_t col) {
   return a.soil.cls[a.soil.cid ? (int)a.soil.cid[a.soil.cid3d ? c : col] : 0];
 }
@@ -34,11 +40,23 @@ __device__ __forceinline__ ff ff_ks(const ReArgs& a, const SoilClass& k, size_t 
   return ff_make(k.ff_ks[d][0], k.ff_ks[d][1]);
 }
 
+// ISO: one conductivity serves all three axes (a per-cell Ks field, or isotropic classes
+// only); the cell then carries kx alone
+template <bool ISO = false>
 __device__ __forceinline__ FfCell ff_cell(const ReArgs& a, size_t c, size_t col) {
-  const SoilClass& k = class_of(a, c, col);
   const ff kr = ff_from_double(a.kr[c]);
   FfCell r;
   r.h = ff_from_double(a.h_new[c]);
+  if (ISO) {
+    if (a.soil.Ks) {
+      r.kx = ff_mul(ff_from_double(a.soil.Ks[c]), kr);
+    } else {
+      const SoilClass& k = class_of(a, c, col);
+      r.kx = ff_mul(ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
+    }
+    return r;
+  }
+  const SoilClass& k = class_of(a, c, col);
   if (a.soil.Ks || k.ks_iso) {
     r.kx = ff_mul(ff_ks(a, k, c, 0), kr);
     r.ky = r.kx;
@@ -111,6 +129,7 @@ __device__ __forceinline__ void ff_top_face(const ReArgs& a, const FfConst& K, c
 }
 
 // the bottom-face closure (pic_row's k = nz-1 branch)
+template <bool ISO = false>
 __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K,
                                                const FfCell& cell, size_t c, size_t col, ff* flux,
                                                ff* trans) {
@@ -119,14 +138,14 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
   if (a.bc4 == 1) {
     const CellSoil s = soil_of(a.soil, c, col);
     const ff kb = ff_from_double(s.Ksz * vg_kr(s, a.hbot));
-    const ff kf = ff_face_mean(a.face_mean, cell.kz, kb);
+    const ff kf = ff_face_mean(a.face_mean, cell_kz<ISO>(cell), kb);
     const ff t = ff_mul(kf, K.cz2);
     *flux = ff_sub(ff_mul(t, ff_sub(K.hbot, cell.h)), ff_mul(K.Az, kf));
     *trans = t;
   } else if (a.bc4 == 2) {
     *flux = ff_mul(K.qbot, K.Az);
   } else if (a.bc4 == 3) {
-    *flux = ff_neg(ff_mul(cell.kz, K.Az));
+    *flux = ff_neg(ff_mul(cell_kz<ISO>(cell), K.Az));
   }
 }
 
@@ -144,6 +163,7 @@ struct FfYPlane {
 // stage and carries to the next level as its own cell.  The level buffers alternate, so one
 // barrier per level suffices: a buffer is rewritten two levels later, after every thread has
 // passed the barrier that follows its last read.
+template <bool ISO>
 __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __restrict__ dg,
                                                            double* __restrict__ a0,
                                                            double* __restrict__ a1,
@@ -151,8 +171,10 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
                                                            double* __restrict__ bvec, int planes,
                                                            int tiles) {
   __shared__ FfYPlane ys[2];
-  const FfConst K = ff_consts(a, a.sc->dt_used);
-  const float dtf = K.dt.h, Vf = K.V.h;
+  // the launch's constants in shared memory rather than in 20 registers per thread
+  __shared__ FfConst K;
+  if (threadIdx.x == 0 && threadIdx.y == 0) K = ff_consts(a, a.sc->dt_used);
+  __syncthreads();
   const int hm = a.face_mean;
   const int t0 = (a.nx + 31) / 32;
   const int lane = threadIdx.x, row = threadIdx.y;
@@ -174,10 +196,10 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
     ff fzm = zero;     // flux into the current cell through its top face
     float tzm = 0.0f;  // and that face's transmissibility (leading float)
     if (act && kb < ke) {
-      cur = ff_cell(a, col + a.ncol * kb, col);
+      cur = ff_cell<ISO>(a, col + a.ncol * kb, col);
       if (kb > 0) {
-        const FfCell up = ff_cell(a, col + a.ncol * (kb - 1), col);
-        const ff kf = ff_face_mean(hm, up.kz, cur.kz);
+        const FfCell up = ff_cell<ISO>(a, col + a.ncol * (kb - 1), col);
+        const ff kf = ff_face_mean(hm, cell_kz<ISO>(up), cell_kz<ISO>(cur));
         const ff t = ff_mul(kf, K.cz);
         tzm = t.h;
         fzm = ff_add_fast(ff_mul(t, ff_dif(up.h, cur.h)), ff_mul(K.Az, kf));
@@ -189,15 +211,15 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
       // stage this level: the own cell and the halo rows
       P.hh[row + 1][lane] = cur.h.h;
       P.hl[row + 1][lane] = cur.h.l;
-      P.kh[row + 1][lane] = cur.ky.h;
-      P.kl[row + 1][lane] = cur.ky.l;
+      P.kh[row + 1][lane] = cell_ky<ISO>(cur).h;
+      P.kl[row + 1][lane] = cell_ky<ISO>(cur).l;
       if (tid < 64) {
         FfCell hc = {zero, zero, zero, zero};
-        if (act_h) hc = ff_cell(a, colh + a.ncol * k, colh);
+        if (act_h) hc = ff_cell<ISO>(a, colh + a.ncol * k, colh);
         P.hh[hrow][lane] = hc.h.h;
         P.hl[hrow][lane] = hc.h.l;
-        P.kh[hrow][lane] = hc.ky.h;
-        P.kl[hrow][lane] = hc.ky.l;
+        P.kh[hrow][lane] = cell_ky<ISO>(hc).h;
+        P.kl[hrow][lane] = cell_ky<ISO>(hc).l;
       }
       // raw loads for the cell below (z face, carried to the next level) and for this cell's
       // residual, issued before the barrier and converted after it, so that their latency
@@ -225,7 +247,7 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
       ff fxp = zero;
       if (act && i + 1 < a.nx) {
         if (lane == 31) {
-          const FfCell nb = ff_cell(a, c + 1, col + 1);
+          const FfCell nb = ff_cell<ISO>(a, c + 1, col + 1);
           Kxn = nb.kx;
           hxn = nb.h;
         }
@@ -242,7 +264,7 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
           txm = 0.0f;
           fxm = zero;
         } else if (lane == 0) {
-          const FfCell nb = ff_cell(a, c - 1, col - 1);
+          const FfCell nb = ff_cell<ISO>(a, c - 1, col - 1);
           const ff t = ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx);
           txm = t.h;
           fxm = ff_mul(t, ff_dif(nb.h, cur.h));
@@ -254,14 +276,14 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
         if (j > 0) {
           const ff hn = ff_make(P.hh[row][lane], P.hl[row][lane]);
           const ff kn = ff_make(P.kh[row][lane], P.kl[row][lane]);
-          const ff t = ff_mul(ff_face_mean(hm, kn, cur.ky), K.cy);
+          const ff t = ff_mul(ff_face_mean(hm, kn, cell_ky<ISO>(cur)), K.cy);
           q = ff_add_fast(q, ff_mul(t, ff_dif(hn, cur.h)));
           tsum += t.h;
         }
         if (j + 1 < a.ny) {
           const ff hn = ff_make(P.hh[row + 2][lane], P.hl[row + 2][lane]);
           const ff kn = ff_make(P.kh[row + 2][lane], P.kl[row + 2][lane]);
-          const ff t = ff_mul(ff_face_mean(hm, cur.ky, kn), K.cy);
+          const ff t = ff_mul(ff_face_mean(hm, cell_ky<ISO>(cur), kn), K.cy);
           ty = t.h;
           q = ff_add_fast(q, ff_mul(t, ff_dif(hn, cur.h)));
           tsum += ty;
@@ -283,17 +305,19 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
           const SoilClass& kb = a.soil.cls[rb_id];
           const ff kr = ff_from_double(rb_kr);
           below.h = ff_from_double(rb_h);
-          if (a.soil.Ks || kb.ks_iso) {
+          if (ISO || a.soil.Ks || kb.ks_iso) {
             below.kx = ff_mul(a.soil.Ks ? ff_from_double(rb_ks)
                                         : ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
-            below.ky = below.kx;
-            below.kz = below.kx;
+            if (!ISO) {
+              below.ky = below.kx;
+              below.kz = below.kx;
+            }
           } else {
             below.kx = ff_mul(ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
             below.ky = ff_mul(ff_make(kb.ff_ks[1][0], kb.ff_ks[1][1]), kr);
             below.kz = ff_mul(ff_make(kb.ff_ks[2][0], kb.ff_ks[2][1]), kr);
           }
-          const ff kf = ff_face_mean(hm, cur.kz, below.kz);
+          const ff kf = ff_face_mean(hm, cell_kz<ISO>(cur), cell_kz<ISO>(below));
           const ff t = ff_mul(kf, K.cz);
           tz = t.h;
           const ff fz = ff_dif(ff_mul(t, ff_dif(below.h, cur.h)), ff_mul(K.Az, kf));
@@ -303,7 +327,7 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
           fzm = ff_neg(fz);
         } else {
           ff f, t;
-          ff_bottom_face(a, K, cur, c, col, &f, &t);
+          ff_bottom_face<ISO>(a, K, cur, c, col, &f, &t);
           q = ff_add_fast(q, f);
           tsum += t.h;
         }
@@ -311,7 +335,8 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
         // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q (float-float)
         const ff wcn = ff_from_double(r_wo);
         const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
-        dg[c] = (double)fmaf(dtf, tsum, Vf * (ff_hi_of(r_cap) + st.h));
+        const float dtf = K.dt.h;
+        dg[c] = (double)fmaf(dtf, tsum, K.V.h * (ff_hi_of(r_cap) + st.h));
         a0[c] = (double)(-dtf * tx);
         a1[c] = (double)(-dtf * ty);
         a2[c] = (double)(-dtf * tz);
@@ -376,10 +401,15 @@ __device__ __forceinline__ FfRow ff_pic_row(const ReArgs& a, const FfConst& K, s
 
 // k_pic_final in float-float: th^{n+1} = th^n + (dt Q - V Ss (th^n/ths)(h^{n+1} - h^n)) / V,
 // boundary and elastic volumes (summed in FP64 across the grid) and time
-__global__ void __launch_bounds__(256) k_pic_final_ff(ReArgs a, int planes, int tiles) {
+__global__ void __launch_bounds__(256, 3) k_pic_final_ff(ReArgs a, int planes, int tiles) {
   const double dtd = a.sc->dt_used;
-  const FfConst K = ff_consts(a, dtd);
-  const ff inv_V = ff_div(ff_make(1.0f), K.V);
+  __shared__ FfConst K;  // the launch's constants in shared memory, not in registers
+  __shared__ ff inv_V;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    K = ff_consts(a, dtd);
+    inv_V = ff_div(ff_make(1.0f), K.V);
+  }
+  __syncthreads();
   double v[3] = {0.0, 0.0, 0.0};
   const int t0 = (a.nx + 31) / 32;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {

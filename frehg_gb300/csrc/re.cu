@@ -49,6 +49,7 @@ struct frehg_re {
   bool top_ghost_stale = false;
   // soil
   SoilClass* cls = nullptr;
+  std::vector<SoilClass> cls_host;  // host copy of the class table
   int nclass = 0;
   uint8_t* cid = nullptr;
   int cid3d = 0;
@@ -142,6 +143,7 @@ static int upload_class0(frehg_re* re) {
   const SoilClass k = make_soil_class(re->p.soil);
   if (!re->cls) FG_CUDA(cudaMalloc(&re->cls, sizeof(SoilClass) * 256));
   FG_CUDA(cudaMemcpy(re->cls, &k, sizeof(SoilClass), cudaMemcpyHostToDevice));
+  re->cls_host.assign(1, k);
   re->nclass = 1;
   return FREHG_OK;
 }
@@ -605,6 +607,12 @@ static int picard_step(frehg_re* re) {
   double dt = re->sc_host->dt;
   ReArgs a = make_args(re);
   const StencilLaunch PL = stencil_launch(re->nx, re->ny, re->nz);
+  // one conductivity serves all axes: a per-cell Ks field, or isotropic classes only
+  bool iso = re->fKs != nullptr;
+  if (!iso) {
+    iso = true;
+    for (const SoilClass& k : re->cls_host) iso = iso && k.ks_iso;
+  }
   int its = 0;
   for (;;) {
     FG_CUDA(cudaMemcpyAsync(&re->sc->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st));
@@ -628,11 +636,14 @@ static int picard_step(frehg_re* re) {
                   k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
                                                                re->A.a2, re->A.b, PL.planes,
                                                                PL.tiles));
+      else if (iso)
+        FG_LAUNCH(prof, st, "k_pic_assemble_ff", (64.0 + sb) * n,
+                  k_pic_assemble_ff<true><<<PL.grid, PL.block, 0, st>>>(
+                      a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b, PL.planes, PL.tiles));
       else
         FG_LAUNCH(prof, st, "k_pic_assemble_ff", (64.0 + sb) * n,
-                  k_pic_assemble_ff<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0,
-                                                                  re->A.a1, re->A.a2, re->A.b,
-                                                                  PL.planes, PL.tiles));
+                  k_pic_assemble_ff<false><<<PL.grid, PL.block, 0, st>>>(
+                      a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b, PL.planes, PL.tiles));
       FG_CUDA(cudaGetLastError());
       CgResult res;
       const int rc = solve_system(re, re->scratch, &res);
@@ -848,6 +859,7 @@ int frehg_re_set_soil_map(frehg_re* re, const frehg_soil_params* classes, int nc
   if (!re->cls) FG_CUDA(cudaMalloc(&re->cls, sizeof(SoilClass) * 256));
   FG_CUDA(cudaStreamSynchronize(re->stream));
   FG_CUDA(cudaMemcpy(re->cls, tab.data(), sizeof(SoilClass) * nclass, cudaMemcpyHostToDevice));
+  re->cls_host = tab;
   cudaFree(re->cid);
   re->cid = nullptr;
   FG_CUDA(cudaMalloc(&re->cid, cnt));
