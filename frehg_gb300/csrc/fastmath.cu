@@ -52,7 +52,8 @@ __global__ void k_constit_eval(SoilClass k, int arith, int continuous, const dou
        i += (size_t)gridDim.x * blockDim.x) {
     Constit r;
     if (arith == 1 && k.use_vg && !k.use_mvg)
-      r = vg_constit_ff<true, true>(k, k.alpha, continuous ? 0.0 : k.aev, h[i]);
+      r = vg_constit_ff<true, true>(k, ff_make(k.ff_alpha[0], k.ff_alpha[1]),
+                                    continuous ? 0.0 : k.aev, h[i]);
     else
       r = vg_constit<true, true>(soil_of(v, i, 0), h[i]);
     kr[i] = r.kr;

@@ -185,7 +185,8 @@ __global__ void __launch_bounds__(256, 4) k_constit_ff(ReArgs a, const double* _
     const double hc = h[c];
     Constit r;
     if (k.use_vg && !k.use_mvg) {
-      const double alpha = a.soil.alpha ? a.soil.alpha[c] : k.alpha;
+      const ff alpha = a.soil.alpha ? ff_from_double(a.soil.alpha[c])
+                                    : ff_make(k.ff_alpha[0], k.ff_alpha[1]);
       r = vg_constit_ff<THETA, CAP>(k, alpha, a.soil.continuous_theta ? 0.0 : k.aev, hc);
     } else {
       r = vg_constit<THETA, CAP>(soil_of(a.soil, c, col), hc);

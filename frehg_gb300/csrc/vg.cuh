@@ -263,22 +263,23 @@ __device__ __forceinline__ Constit vg_constit(const CellSoil& s, double h) {
 }
 
 // vg_constit in float-float arithmetic on the FP32 pipe (ff32.cuh): the same relations, caps and
-// saturated branches, about 48 significant bits per operation instead of 53, for the VG branch
-// (MVG and the exponential model take vg_constit).  Where the soil is drier than |alpha h| = 1,
+// saturated branches, about 48 significant bits per operation instead of 53 for K and theta,
+// FP32 for C (which enters only the matrix diagonal), for the VG branch (MVG and the
+// exponential model take vg_constit).  Where the soil is drier than |alpha h| = 1,
 // (1 - se^{1/m})^m is formed from ln(1 + 1/t) rather than from the difference nL - u, so dry
 // cells keep the relative accuracy of K that the FP64 forms (and the reference's pow forms)
 // lose there.  k: the cell's class (its
-// float-float constants); alpha: the cell's alpha (class value or per-cell field); aev: the
-// head above which theta = theta_s.  Heads h >= 0 (and |alpha h| too small for the float range)
+// float-float constants); alpha: the cell's alpha, float-float (class value or per-cell
+// field); aev: the head above which theta = theta_s.  Heads h >= 0 (and |alpha h| too small for the float range)
 // give kr = 1, C = 0 and theta_s exactly, as the FP64 forms do.
 template <bool WANT_THETA, bool WANT_CAP>
-__device__ __forceinline__ Constit vg_constit_ff(const SoilClass& k, double alpha, double aev,
+__device__ __forceinline__ Constit vg_constit_ff(const SoilClass& k, ff alpha, double aev,
                                                  double h) {
   Constit r;
   r.kr = 1.0;
   r.theta = k.ths;
   r.cap = 0.0;
-  const ff ah = ff_mul(ff_from_double(alpha), ff_from_double(-h));  // |alpha h| for h < 0
+  const ff ah = ff_mul(alpha, ff_from_double(-h));  // |alpha h| for h < 0
   if (!(ah.h > 0.0f)) return r;
   const ff n = ff_make(k.ff_n[0], k.ff_n[1]);
   const ff m = ff_make(k.ff_m[0], k.ff_m[1]);
@@ -310,11 +311,10 @@ __device__ __forceinline__ Constit vg_constit_ff(const SoilClass& k, double alph
     r.theta = ff_ge1(se) ? k.ths : ff_to_double(wc);
   }
   if (WANT_CAP) {
-    // alpha n m (ths - thr) t se / (|alpha h| (1 + t))
-    const ff num = ff_mul(ff_mul(ff_from_double(alpha), ff_make(k.ff_nmdth[0], k.ff_nmdth[1])),
-                          ff_mul(t, se));
-    const ff den = ff_mul(ah, ff_add_f(t, 1.0f));
-    r.cap = ff_to_double(ff_div(num, den));
+    // alpha n m (ths - thr) t se / (|alpha h| (1 + t)) from the leading floats: C enters only
+    // the matrix diagonal, which the float-float Picard path forms in FP32
+    const float num = alpha.h * k.ff_nmdth[0] * (t.h * se.h);
+    r.cap = (double)__fdividef(num, ah.h * (1.0f + t.h));
   }
   return r;
 }

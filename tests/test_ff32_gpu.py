@@ -145,7 +145,7 @@ def test_constitutive_ff(gpu_lib, name):
     live = kref > 1e-300
     e_kr = rel(k1[live], kref[live]).max()
     e_wc = np.abs(w1 - wref).max()
-    cb = cref > 1e-300
+    cb = cref > 1e-30
     e_c = rel(c1[cb], cref[cb]).max()
     wet = live & (np.abs(s.alpha * h) < 1.0)
     e_kr64 = rel(k0[live], kref[live]).max()
@@ -158,8 +158,9 @@ def test_constitutive_ff(gpu_lib, name):
     assert np.all(w1 <= s.theta_s) and np.all(w1 >= s.theta_r)
     assert e_wc <= 64 * U2
     # t = e^{n ln|alpha h|} carries the argument's absolute error |n ln|alpha h|| u^2 as a
-    # relative error; K and C inherit it (about 1e-12 at |alpha h| = 1e3)
+    # relative error; K inherits it (about 1e-12 at |alpha h| = 1e3).  C is formed in FP32
+    # (it enters only the FP32 matrix diagonal of the float-float Picard path).
     assert e_kr <= 1e-11
-    assert e_c <= 1e-11
+    assert e_c <= 1e-6
     # in wet cells the two device forms agree to float-float precision
     assert rel(k1[wet], k0[wet]).max() <= 1e-12
