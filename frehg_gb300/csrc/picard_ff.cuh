@@ -153,14 +153,17 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
 // axis-1 conductivity of each cell, float-float (the y faces read their neighbours here).
 struct FfYPlane {
   float hh[10][32], hl[10][32], kh[10][32], kl[10][32];
+  // the cells left (0) and right (1) of each tile row: head and axis-0 conductivity
+  float xhh[8][2], xhl[8][2], xkh[8][2], xkl[8][2];
 };
 
 // k_pic_assemble in float-float as a tiled stencil: a (32 x 8)-thread block marches its column
 // tile down `planes` levels.  Per level each thread stages its own cell's (h, K_y) in shared
-// memory (threads 0-63 also stage the rows above and below the tile), then, after one barrier,
-// forms the faces: x from the adjacent lanes (warp shuffles; lanes 0 and 31 load their outer
-// neighbour), y from shared memory, z with the cell below, which it loads while the others
-// stage and carries to the next level as its own cell.  The level buffers alternate, so one
+// memory (threads 0-63 also stage the rows above and below the tile, threads 64-79 the cells
+// left and right of its rows), then, after one barrier, forms the faces: x from the adjacent
+// lanes (warp shuffles; lanes 0 and 31 read their outer neighbour from shared memory), y from
+// shared memory, z with the cell below, which it loads while the others stage and carries to
+// the next level as its own cell.  The level buffers alternate, so one
 // barrier per level suffices: a buffer is rewritten two levels later, after every thread has
 // passed the barrier that follows its last read.
 template <bool ISO>
@@ -220,6 +223,18 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
         P.hl[hrow][lane] = hc.h.l;
         P.kh[hrow][lane] = cell_ky<ISO>(hc).h;
         P.kl[hrow][lane] = cell_ky<ISO>(hc).l;
+      } else if (tid < 80) {
+        const int xr = (tid - 64) >> 1, side = (tid - 64) & 1;
+        const int ix = (tile % t0) * 32 + (side ? 32 : -1), jx = j0 + xr;
+        FfCell xc = {zero, zero, zero, zero};
+        if (ix >= 0 && ix < a.nx && jx < a.ny) {
+          const size_t colx = (size_t)ix + (size_t)a.nx * jx;
+          xc = ff_cell<ISO>(a, colx + a.ncol * k, colx);
+        }
+        P.xhh[xr][side] = xc.h.h;
+        P.xhl[xr][side] = xc.h.l;
+        P.xkh[xr][side] = xc.kx.h;
+        P.xkl[xr][side] = xc.kx.l;
       }
       // raw loads for the cell below (z face, carried to the next level) and for this cell's
       // residual, issued before the barrier and converted after it, so that their latency
@@ -247,9 +262,8 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
       ff fxp = zero;
       if (act && i + 1 < a.nx) {
         if (lane == 31) {
-          const FfCell nb = ff_cell<ISO>(a, c + 1, col + 1);
-          Kxn = nb.kx;
-          hxn = nb.h;
+          Kxn = ff_make(P.xkh[row][1], P.xkl[row][1]);
+          hxn = ff_make(P.xhh[row][1], P.xhl[row][1]);
         }
         const ff t = ff_mul(ff_face_mean(hm, cur.kx, Kxn), K.cx);
         tx = t.h;
@@ -264,10 +278,11 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
           txm = 0.0f;
           fxm = zero;
         } else if (lane == 0) {
-          const FfCell nb = ff_cell<ISO>(a, c - 1, col - 1);
-          const ff t = ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx);
+          const ff kxm = ff_make(P.xkh[row][0], P.xkl[row][0]);
+          const ff hxm = ff_make(P.xhh[row][0], P.xhl[row][0]);
+          const ff t = ff_mul(ff_face_mean(hm, kxm, cur.kx), K.cx);
           txm = t.h;
-          fxm = ff_mul(t, ff_dif(nb.h, cur.h));
+          fxm = ff_mul(t, ff_dif(hxm, cur.h));
         }
         ff q = ff_add_fast(fxm, fxp);
         float tsum = txm + tx;
