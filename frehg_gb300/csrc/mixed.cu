@@ -782,6 +782,11 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     // inner FP32 solve: flexible CG with the learned preconditioner, or Jacobi CG
     FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
+    // a sweep that starts with the network's budget (twice the reference solve's inner
+    // iterations) spent runs without it, as do the later ones
+    if (net.net != nullptr && !fcg_fallback && net.max_inner > 0 &&
+        inner_total >= net.max_inner)
+      fcg_fallback = true;
     const bool use_net = net.net != nullptr && !fcg_fallback;
     if (use_net) {
       if (!zf) {
