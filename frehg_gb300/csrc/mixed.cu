@@ -567,6 +567,18 @@ __device__ __forceinline__ ff scaled_coupling(double* a, size_t c, double sc, do
   return ff_make(ff_hi_of(v));
 }
 
+// the float-float path's scale factors are floats, and so are the couplings the float-float
+// Picard assembly writes: a s_c s_n = a (p_h + p_l) with p = s_c s_n exact, one float-float by
+// float product; a coupling with more than 24 significant bits takes the float-float split
+__device__ __forceinline__ ff scaled_coupling_f(double* a, size_t c, float sc, float sn) {
+  const double ad = a[c];
+  const ff p = two_prod(sc, sn);
+  const ff v = ((unsigned)__double2loint(ad) & 0x1fffffffu) == 0u ? ff_mul_f(p, ff_hi_of(ad))
+                                                                 : ff_mul(ff_from_double(ad), p);
+  a[c] = ff_to_double(v);
+  return v;
+}
+
 template <bool FF_OP>
 __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
                                                      double* __restrict__ a1,
@@ -587,15 +599,26 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
     ff inv_d = ff_make(1.0f), aprev = zero;
     size_t c = (size_t)col;
     double sc = s[c];
+    float scf = FF_OP ? ff_hi_of(sc) : 0.0f;
     for (int k = 0; k < n2; ++k, c += sk) {
       const double sb = (k + 1 < n2) ? s[c + sk] : 0.0;
+      const float sbf = FF_OP ? ff_hi_of(sb) : 0.0f;
       ff v0 = zero, v1 = zero, v2 = zero;
-      if (i0 + 1 < n0) v0 = scaled_coupling<FF_OP>(a0, c, sc, s[c + 1]);
-      else a0[c] = 0.0;
-      if (i1 + 1 < n1) v1 = scaled_coupling<FF_OP>(a1, c, sc, s[c + n0]);
-      else a1[c] = 0.0;
-      if (k + 1 < n2) v2 = scaled_coupling<FF_OP>(a2, c, sc, sb);
-      else a2[c] = 0.0;
+      if (FF_OP) {
+        if (i0 + 1 < n0) v0 = scaled_coupling_f(a0, c, scf, ff_hi_of(s[c + 1]));
+        else a0[c] = 0.0;
+        if (i1 + 1 < n1) v1 = scaled_coupling_f(a1, c, scf, ff_hi_of(s[c + n0]));
+        else a1[c] = 0.0;
+        if (k + 1 < n2) v2 = scaled_coupling_f(a2, c, scf, sbf);
+        else a2[c] = 0.0;
+      } else {
+        if (i0 + 1 < n0) v0 = scaled_coupling<FF_OP>(a0, c, sc, s[c + 1]);
+        else a0[c] = 0.0;
+        if (i1 + 1 < n1) v1 = scaled_coupling<FF_OP>(a1, c, sc, s[c + n0]);
+        else a1[c] = 0.0;
+        if (k + 1 < n2) v2 = scaled_coupling<FF_OP>(a2, c, sc, sb);
+        else a2[c] = 0.0;
+      }
       f0[c] = v0.h;
       f1[c] = v1.h;
       f2[c] = v2.h;
@@ -612,6 +635,7 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
         aprev = v2;
       }
       sc = sb;
+      scf = sbf;
     }
   }
 }

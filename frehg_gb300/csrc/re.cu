@@ -503,7 +503,9 @@ static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
       re->last_plain_ms = ms;
     }
     ++re->solves_since_probe;
-    if (!use_net || res->fallback) re->plain_its_ref = res->its;
+    // the reference count comes from network-free solves only (a fallback solve's count also
+    // holds the network's iterations)
+    if (!use_net) re->plain_its_ref = res->its;
   }
   if (!use_net) re->cnt.plain_ms += ms;
   if (res->fallback) re->cnt.fcg_fallbacks += 1;
