@@ -98,6 +98,9 @@ struct Stencil64 {
   double* s = nullptr;  // holds d before scale(), D^-1/2 after
   double* b = nullptr;  // right-hand side (unscaled)
   bool scaled = false;
+  // the float-float path's preparation left s = D^-1/2 in the mixed solver's FP64 vector r
+  // (as floats) and d itself in s
+  bool s_in_r = false;
   int alloc(int n0, int n1, int n2);
   void release();
 };
@@ -199,7 +202,8 @@ class KrylovSolver {
   // vertical-line preconditioner (FP32 factors and sweep scratch)
   int ensure_line(size_t n);
   // scaling of the operator for the mixed path (sq = D^1/2 into r, FP32 copy, line factors)
-  int prep_mixed(Stencil64& A, cudaStream_t st, bool line);
+  int prep_mixed(Stencil64& A, cudaStream_t st, bool line, const frehg_solver_config& cfg);
+  bool first_done = false;  // prep_mixed formed the first refinement residual and its state
   size_t cap_line = 0;
   float *lkf = nullptr, *dinvf = nullptr, *uf = nullptr;
   int g32_line = 0;

@@ -322,6 +322,7 @@ int Stencil64::alloc(int n0_, int n1_, int n2_) {
   FG_CUDA(cudaMalloc(&s, n * sizeof(double)));
   FG_CUDA(cudaMalloc(&b, n * sizeof(double)));
   scaled = false;
+  s_in_r = false;
   return FREHG_OK;
 }
 
@@ -403,6 +404,10 @@ int KrylovSolver::ensure(size_t n) {
 }
 
 int KrylovSolver::scale(Stencil64& A, cudaStream_t st) {
+  if (A.scaled && A.s_in_r) {
+    set_error("operator prepared for the float-float mixed-precision solve; reassemble it");
+    return FREHG_ERR_STATE;
+  }
   if (A.scaled) return FREHG_OK;
   const int nb = reduction_blocks(A.n, 256, 4);
   const double n = (double)A.n;
@@ -435,7 +440,7 @@ int KrylovSolver::solve(Stencil64& A, double* x_out, const frehg_solver_config& 
                         cudaStream_t st, CgResult* res) {
   FG_TRY(ensure(A.n));
   if (cfg.precision == 1) {
-    FG_TRY(prep_mixed(A, st, !strcmp(cfg.pc_type, "line")));
+    FG_TRY(prep_mixed(A, st, !strcmp(cfg.pc_type, "line"), cfg));
     return solve_mixed(A, x_out, cfg, st, res);
   }
   FG_TRY(scale(A, st));
@@ -532,7 +537,7 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
 
 int KrylovSolver::finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResult* res, int nb) {
   FG_LAUNCH(prof, st, "k_unscale", 24.0 * (double)A.n,
-            k_unscale<<<nb, 256, 0, st>>>(A.s, x, x_out, A.n));
+            k_unscale<<<nb, 256, 0, st>>>(A.s_in_r ? r : A.s, x, x_out, A.n));
   FG_CUDA(cudaGetLastError());
   res->its = hst->its;
   res->reason = hst->status;

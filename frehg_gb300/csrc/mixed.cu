@@ -32,7 +32,7 @@ namespace fg {
 // the stencil product in FP64: the residual is a difference of nearly equal terms, and the
 // refinement converges only as far as this product is accurate (a float-float form, 2^-48,
 // was both slower here and short of 1e-12 on ill-conditioned systems).
-template <bool FIRST>
+template <bool FIRST, bool INV_S = false>
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ s, const double* __restrict__ sq, const double* __restrict__ b,
@@ -85,7 +85,9 @@ __global__ void __launch_bounds__(256) k_ir_residual(
         rres[c] = r;
         ef[c] = 0.0f;
         const float rf = ff_hi_of(r);
-        const float q0 = rf * sig0, q1 = rf * ff_hi_of(sq[c]) * sig1;  // sq r~ = r~ / s
+        // sq r~ = r~ / s (INV_S: s holds floats and sq is not stored)
+        const float sqc = INV_S ? __frcp_rn(ff_hi_of(s[c])) : ff_hi_of(sq[c]);
+        const float q0 = rf * sig0, q1 = rf * sqc * sig1;
         k0.add(q0 * q0);
         k1.add(q1 * q1);
       }
@@ -517,51 +519,26 @@ int KrylovSolver::ensure32(size_t n) {
   return FREHG_OK;
 }
 
-// Scaling of a fresh operator for the mixed path in two passes: s = D^-1/2 with sq = 1/s (the
-// true-residual norm multiplies by it), then one pass per column that scales the couplings in
-// place (for the refinement residual), writes their FP32 copies and, with the line
-// preconditioner, the column factors.
-//
-// FF_OP (solves whose result is an update of an iterate): s is rounded to FP32.  The scaling is
-// a similarity transform (A~ = S A S, b~ = S b, x = S x~), so s_c s_n is then an exact float
-// product and the scaled couplings a s_c s_n cost one float-float product each instead of two
-// FP64 multiplications (GB300 runs FP64 at 1/73 of the FP32 rate).  The scaled diagonal d s^2
-// is then 1 only to FP32 precision while the refinement takes it as 1: the update changes in
-// its last digits, the iterate's fixed point does not.  Solves whose result is the solution
-// itself keep the FP64 s (d s^2 = 1 to rounding).
-template <bool FF_OP>
+// Scaling of a fresh operator for the mixed path in two passes (solves whose result is the
+// solution itself): s = D^-1/2 with sq = D^1/2 in FP64 (d s^2 = 1 to rounding, as the
+// refinement residual's unit diagonal assumes), then one pass per column that scales the
+// couplings in place (FP64, for the refinement residual), writes their FP32 copies (leading 24
+// bits, without a double->float conversion: GB300 runs those on the FP64 pipe) and, with the
+// line preconditioner, the column factors
+//   l_k = v2_{k-1} / d_{k-1},  d_k = 1 - l_k v2_{k-1}   (d_0 = 1)
+// in float-float, stored as floats.  The float-float path's update solves take k_prep_ff.
 __global__ void k_diag_rsqrt_sq(double* __restrict__ s, double* __restrict__ sq, size_t n) {
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
        c += (size_t)gridDim.x * blockDim.x) {
     const double d = s[c];
-    if (FF_OP) {
-      // PCJacobi replaces a zero diagonal entry by 1
-      const float df = (__double_as_longlong(d) << 1) == 0 ? 1.0f : ff_hi_of(d);
-      const float r = rsqrtf(df);
-      s[c] = (double)r;
-      sq[c] = (double)__frcp_rn(r);
-    } else {
-      const double dd = d == 0.0 ? 1.0 : d;
-      const double r = rsqrt(dd);
-      s[c] = r;
-      sq[c] = dd * r;
-    }
+    const double dd = d == 0.0 ? 1.0 : d;  // PCJacobi replaces a zero diagonal entry by 1
+    const double r = rsqrt(dd);
+    s[c] = r;
+    sq[c] = dd * r;
   }
 }
 
-// The scaled couplings v = a s_c s_n written back as doubles and as floats: in FP64 (two
-// multiplications; FF_OP false) or in float-float (FF_OP true: s_c s_n exact, a split from its
-// double, about 48 significant bits); the line factors
-//   l_k = v2_{k-1} / d_{k-1},  d_k = 1 - l_k v2_{k-1}   (d_0 = 1)
-// in float-float, stored as floats.  The FP32 copies are the leading 24 bits (no double->float
-// conversion, which runs on the FP64 pipe).
-template <bool FF_OP>
-__device__ __forceinline__ ff scaled_coupling(double* a, size_t c, double sc, double sn) {
-  if (FF_OP) {  // sc, sn hold floats
-    const ff v = ff_mul(ff_from_double(a[c]), two_prod(ff_hi_of(sc), ff_hi_of(sn)));
-    a[c] = ff_to_double(v);
-    return v;
-  }
+__device__ __forceinline__ ff scaled_coupling64(double* a, size_t c, double sc, double sn) {
   const double v = a[c] * sc * sn;
   a[c] = v;
   return ff_make(ff_hi_of(v));
@@ -579,7 +556,6 @@ __device__ __forceinline__ ff scaled_coupling_f(double* a, size_t c, float sc, f
   return v;
 }
 
-template <bool FF_OP>
 __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
                                                      double* __restrict__ a1,
                                                      double* __restrict__ a2,
@@ -599,26 +575,15 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
     ff inv_d = ff_make(1.0f), aprev = zero;
     size_t c = (size_t)col;
     double sc = s[c];
-    float scf = FF_OP ? ff_hi_of(sc) : 0.0f;
     for (int k = 0; k < n2; ++k, c += sk) {
       const double sb = (k + 1 < n2) ? s[c + sk] : 0.0;
-      const float sbf = FF_OP ? ff_hi_of(sb) : 0.0f;
       ff v0 = zero, v1 = zero, v2 = zero;
-      if (FF_OP) {
-        if (i0 + 1 < n0) v0 = scaled_coupling_f(a0, c, scf, ff_hi_of(s[c + 1]));
-        else a0[c] = 0.0;
-        if (i1 + 1 < n1) v1 = scaled_coupling_f(a1, c, scf, ff_hi_of(s[c + n0]));
-        else a1[c] = 0.0;
-        if (k + 1 < n2) v2 = scaled_coupling_f(a2, c, scf, sbf);
-        else a2[c] = 0.0;
-      } else {
-        if (i0 + 1 < n0) v0 = scaled_coupling<FF_OP>(a0, c, sc, s[c + 1]);
-        else a0[c] = 0.0;
-        if (i1 + 1 < n1) v1 = scaled_coupling<FF_OP>(a1, c, sc, s[c + n0]);
-        else a1[c] = 0.0;
-        if (k + 1 < n2) v2 = scaled_coupling<FF_OP>(a2, c, sc, sb);
-        else a2[c] = 0.0;
-      }
+      if (i0 + 1 < n0) v0 = scaled_coupling64(a0, c, sc, s[c + 1]);
+      else a0[c] = 0.0;
+      if (i1 + 1 < n1) v1 = scaled_coupling64(a1, c, sc, s[c + n0]);
+      else a1[c] = 0.0;
+      if (k + 1 < n2) v2 = scaled_coupling64(a2, c, sc, sb);
+      else a2[c] = 0.0;
       f0[c] = v0.h;
       f1[c] = v1.h;
       f2[c] = v2.h;
@@ -635,7 +600,90 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
         aprev = v2;
       }
       sc = sb;
-      scf = sbf;
+    }
+  }
+}
+
+// The float-float path's preparation in one pass per column (update solves, ff_operator): the
+// scale factors s = D^-1/2 rounded to FP32 (a similarity transform: any s applied consistently
+// gives the same solution, and FP32 s make s_c s_n an exact float product; d s^2 is then 1 only
+// to FP32 precision while the refinement takes it as 1, which perturbs the update, not the
+// iterate's fixed point), formed from the diagonal by each thread for itself and its neighbours
+// (the same rounding everywhere, so the diagonal stays in place) and written to s_out; the
+// scaled couplings a s_c s_n in float-float and their FP32 copies; the line factors as in
+// k_scale_mixed; and the first refinement sweep's residual r~ = s b with x~ = 0 (FP64), its
+// sums and test, as k_ir_residual<true>.  This replaces k_diag_rsqrt_sq, k_scale_mixed and the
+// first k_ir_residual: the diagonal, the couplings and b are read once.
+__device__ __forceinline__ float scale_of(double d) {
+  return rsqrtf((__double_as_longlong(d) << 1) == 0 ? 1.0f : ff_hi_of(d));
+}
+
+__global__ void __launch_bounds__(128) k_prep_ff(
+    double* __restrict__ a0, double* __restrict__ a1, double* __restrict__ a2,
+    const double* __restrict__ dg, const double* __restrict__ b, double* __restrict__ s_out,
+    double* __restrict__ x, double* __restrict__ rres, float* __restrict__ ef,
+    float* __restrict__ f0, float* __restrict__ f1, float* __restrict__ f2,
+    float* __restrict__ lk, float* __restrict__ dinv, int n0, int n1, int n2, int line,
+    CgDevState* ir, double* partials, double ir_rtol) {
+  const int ncol = n0 * n1;
+  const size_t sk = (size_t)ncol;
+  const ff zero = ff_make(0.0f);
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
+       col += gridDim.x * blockDim.x) {
+    const int i0 = col % n0, i1 = col / n0;
+    ff inv_d = ff_make(1.0f), aprev = zero;
+    size_t c = (size_t)col;
+    float sc = scale_of(dg[c]);
+    for (int k = 0; k < n2; ++k, c += sk) {
+      const float sb = (k + 1 < n2) ? scale_of(dg[c + sk]) : 0.0f;
+      s_out[c] = (double)sc;
+      ff v0 = zero, v1 = zero, v2 = zero;
+      if (i0 + 1 < n0) v0 = scaled_coupling_f(a0, c, sc, scale_of(dg[c + 1]));
+      else a0[c] = 0.0;
+      if (i1 + 1 < n1) v1 = scaled_coupling_f(a1, c, sc, scale_of(dg[c + n0]));
+      else a1[c] = 0.0;
+      if (k + 1 < n2) v2 = scaled_coupling_f(a2, c, sc, sb);
+      else a2[c] = 0.0;
+      f0[c] = v0.h;
+      f1[c] = v1.h;
+      f2[c] = v2.h;
+      if (line) {
+        ff l = zero;
+        if (k > 0) {
+          l = ff_mul(aprev, inv_d);
+          ff d = ff_add_f(ff_neg(ff_mul(l, aprev)), 1.0f);
+          if (!(d.h > 1e-30f)) d = ff_make(1.0f);  // not SPD: that row falls back to Jacobi
+          inv_d = ff_div(ff_make(1.0f), d);
+        }
+        lk[c] = l.h;
+        dinv[c] = inv_d.h;
+        aprev = v2;
+      }
+      // first sweep: x~ = 0, r~ = s b
+      const double bc = b[c];
+      const double r = (double)sc * bc;
+      x[c] = 0.0;
+      rres[c] = r;
+      ef[c] = 0.0f;
+      v[0] = fma(r, r, v[0]);
+      v[2] = fma(bc, bc, v[2]);
+      sc = sb;
+    }
+  }
+  v[1] = v[2];  // with x~ = 0 the true residual is b
+  double tot[3];
+  if (!grid_sum<3>(v, partials, &ir->arrive[0], tot)) return;
+  if (flat_tid() == 0) {
+    const double rn = sqrt(tot[1]);
+    ir->ir_bnorm = rn;
+    ir->ir_rnorm = rn;
+    ir->dp = rn;
+    ir->a = sqrt(tot[0]);
+    if (isnan(rn) || isinf(rn)) {
+      ir->status = kDivergedNanOrInf;
+    } else if (rn <= fmax(ir_rtol * ir->ir_bnorm, ir->atol) || tot[0] == 0.0) {
+      ir->status = rn < ir->atol ? kConvergedAtol : kConvergedRtol;
     }
   }
 }
@@ -647,7 +695,8 @@ __global__ void k_inv64(const double* __restrict__ s, double* __restrict__ sq, s
     sq[c] = 1.0 / s[c];
 }
 
-int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line) {
+int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
+                             const frehg_solver_config& cfg) {
   const size_t n = A.n;
   FG_TRY(ensure32(n));
   if (line) FG_TRY(ensure_line(n));
@@ -655,29 +704,38 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line) {
   const double dn = (double)n;
   const int ncol = A.n0 * A.n1;
   const int lb = (int)std::min<long>((ncol + 127) / 128, kMaxRedBlocks);
+  first_done = false;
   if (!A.scaled) {
-    if (ff_operator)
-      FG_LAUNCH(prof, st, "k_diag_rsqrt_sq", 24.0 * dn,
-                k_diag_rsqrt_sq<true><<<nb, 256, 0, st>>>(A.s, r, n));
-    else
-      FG_LAUNCH(prof, st, "k_diag_rsqrt_sq", 24.0 * dn,
-                k_diag_rsqrt_sq<false><<<nb, 256, 0, st>>>(A.s, r, n));
-    if (ff_operator)
-      FG_LAUNCH(prof, st, "k_scale_mixed", (56.0 + 12.0 + (line ? 8.0 : 0.0)) * dn,
-                k_scale_mixed<true><<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, op32.a0, op32.a1,
-                                                        op32.a2, lkf, dinvf, A.n0, A.n1, A.n2,
-                                                        line ? 1 : 0));
-    else
-      FG_LAUNCH(prof, st, "k_scale_mixed", (56.0 + 12.0 + (line ? 8.0 : 0.0)) * dn,
-                k_scale_mixed<false><<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, op32.a0,
-                                                         op32.a1, op32.a2, lkf, dinvf, A.n0,
-                                                         A.n1, A.n2, line ? 1 : 0));
+    if (ff_operator) {
+      // the refinement state, then one pass: scale factors, scaled operator, FP32 copy, line
+      // factors and the first sweep's residual
+      CgDevState ir0;
+      memset(&ir0, 0, sizeof(ir0));
+      ir0.atol = cfg.atol;
+      FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+      FG_LAUNCH(prof, st, "k_prep_ff", (8.0 + 48.0 + 12.0 + 8.0 + (line ? 8.0 : 0.0) + 36.0) * dn,
+                k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, A.b, r, x, rres, xf,
+                                              op32.a0, op32.a1, op32.a2, lkf, dinvf, A.n0, A.n1,
+                                              A.n2, line ? 1 : 0, dst, partials, cfg.ir_rtol));
+      FG_CUDA(cudaGetLastError());
+      A.scaled = true;
+      A.s_in_r = true;
+      first_done = true;
+      return FREHG_OK;
+    }
+    FG_LAUNCH(prof, st, "k_diag_rsqrt_sq", 24.0 * dn,
+              k_diag_rsqrt_sq<<<nb, 256, 0, st>>>(A.s, r, n));
+    FG_LAUNCH(prof, st, "k_scale_mixed", (56.0 + 12.0 + (line ? 8.0 : 0.0)) * dn,
+              k_scale_mixed<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, op32.a0, op32.a1,
+                                                op32.a2, lkf, dinvf, A.n0, A.n1, A.n2,
+                                                line ? 1 : 0));
     FG_CUDA(cudaGetLastError());
     A.scaled = true;
     return FREHG_OK;
   }
-  // an operator scaled by an earlier solve: derive sq, the FP32 copy and the factors from it
-  FG_LAUNCH(prof, st, "k_inv64", 16.0 * dn, k_inv64<<<nb, 256, 0, st>>>(A.s, r, n));
+  // an operator scaled by an earlier solve: derive sq (unless r holds s), the FP32 copy and
+  // the factors from it
+  if (!A.s_in_r) FG_LAUNCH(prof, st, "k_inv64", 16.0 * dn, k_inv64<<<nb, 256, 0, st>>>(A.s, r, n));
   FG_LAUNCH(prof, st, "k_to_f32", 36.0 * dn,
             k_to_f32<<<nb, 256, 0, st>>>(A.a0, A.a1, A.a2, op32.a0, op32.a1, op32.a2, n));
   if (line)
@@ -719,8 +777,14 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   memset(&in0, 0, sizeof(in0));
   ir0.atol = cfg.atol;
   in0.max_it = cfg.max_it;
-  FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+  // prep_mixed may have formed the first sweep's residual and its state already
+  const bool first_done_here = first_done;
+  first_done = false;
+  if (!first_done_here)
+    FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
   FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+  // where the scale factors are: A.s, or r (as floats) after the float-float preparation
+  const double* sv = A.s_in_r ? r : A.s;
 
   const int chunk = 32;
   const long shape_key = (long)A.n0 * 1000003L + A.n1;
@@ -785,16 +849,23 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   bool fcg_fallback = false;
   const bool dbg = getenv("FREHG_DEBUG_IR") != nullptr;
   for (;;) {
-    if (sweeps == 0)
-      FG_LAUNCH(prof, st, "k_ir_residual0", 40.0 * dn,
-                k_ir_residual<true><<<L.grid, L.block, 0, st>>>(
-                    A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
-                    L.tiles, dst, partials, cfg.ir_rtol));
-    else
+    if (sweeps == 0) {
+      if (!first_done_here)
+        FG_LAUNCH(prof, st, "k_ir_residual0", 40.0 * dn,
+                  k_ir_residual<true><<<L.grid, L.block, 0, st>>>(
+                      A.a0, A.a1, A.a2, sv, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                      L.tiles, dst, partials, cfg.ir_rtol));
+    } else if (A.s_in_r) {
+      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
+                (k_ir_residual<false, true><<<L.grid, L.block, 0, st>>>(
+                    A.a0, A.a1, A.a2, sv, sv, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                    L.tiles, dst, partials, cfg.ir_rtol)));
+    } else {
       FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
                 k_ir_residual<false><<<L.grid, L.block, 0, st>>>(
                     A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
                     L.tiles, dst, partials, cfg.ir_rtol));
+    }
     FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
               k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials, cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());

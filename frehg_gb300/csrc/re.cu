@@ -533,6 +533,7 @@ static int pca_step(frehg_re* re) {
   // groundwaterMatCoeff + groundwaterRhs + assembly
   const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
   re->A.scaled = false;
+  re->A.s_in_r = false;
   FG_LAUNCH(prof, st, "k_assemble", (72.0 + sb) * n,
             k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
                                                    re->A.b, L.planes, L.tiles));
@@ -633,6 +634,7 @@ static int picard_step(frehg_re* re) {
                   (k_constit_ff<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch,
                                                                 re->cap)));
       re->A.scaled = false;
+      re->A.s_in_r = false;
       if (re->p.picard_fp64)
         FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
                   k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
@@ -1333,6 +1335,7 @@ int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, int targ
   k_constit<false, true><<<nb, 256, 0, st>>>(a, a.h_old, re->kr, nullptr, re->cap);
   const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
   re->A.scaled = false;
+  re->A.s_in_r = false;
   k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b,
                                          L.planes, L.tiles);
   k_net_fields<<<nb, 256, 0, st>>>(a, lnk_out, cap_out);
