@@ -1,7 +1,7 @@
 // Float-float forms of the Picard assembly and of the conservative final update (not in
 // reference): the same faces, boundary closures, residual and update as k_pic_assemble /
 // k_pic_final (picard.cuh), with every FP64 operation replaced by float-float arithmetic on
-// the FP32 pipe (ff32.cuh; about 48 significant bits).  GB300 runs FP64 at 1/73 of the FP32
+// the FP32 pipe (ff32.cuh; about 48 significant bits), in one tiled kernel with two modes.  GB300 runs FP64 at 1/73 of the FP32
 // rate, and the FP64 forms of these kernels are bound by that pipe, not by memory.
 //
 // Doubles are read and split into float-float with integer operations; results are written
@@ -166,7 +166,12 @@ struct FfYPlane {
 // the next level as its own cell.  The level buffers alternate, so one
 // barrier per level suffices: a buffer is rewritten two levels later, after every thread has
 // passed the barrier that follows its last read.
-template <bool ISO>
+//
+// FINAL: the same faces at h^{n+1} with the last frozen K form the conservative update
+// th^{n+1} = th^n + (dt Q - V Ss (th^n/ths)(h^{n+1} - h^n)) / V (k_pic_final's job) instead of
+// the system, with the top / bottom / elastic volumes summed across the grid (FP64) and the
+// time advanced.
+template <bool ISO, bool FINAL = false>
 __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __restrict__ dg,
                                                            double* __restrict__ a0,
                                                            double* __restrict__ a1,
@@ -176,8 +181,13 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
   __shared__ FfYPlane ys[2];
   // the launch's constants in shared memory rather than in 20 registers per thread
   __shared__ FfConst K;
-  if (threadIdx.x == 0 && threadIdx.y == 0) K = ff_consts(a, a.sc->dt_used);
+  __shared__ ff inv_V;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    K = ff_consts(a, a.sc->dt_used);
+    inv_V = ff_div(ff_make(1.0f), K.V);
+  }
   __syncthreads();
+  double vol[3] = {0.0, 0.0, 0.0};  // FINAL: top, bottom, elastic volumes
   const int hm = a.face_mean;
   const int t0 = (a.nx + 31) / 32;
   const int lane = threadIdx.x, row = threadIdx.y;
@@ -250,9 +260,11 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
         if (a.soil.Ks) rb_ks = a.soil.Ks[cb];
         if (a.soil.cid) rb_id = a.soil.cid[a.soil.cid3d ? cb : col];
         r_wo = a.w_old[c];
-        r_wch = a.wch[c];
         r_ho = a.h_old[c];
-        r_cap = a.cap[c];
+        if (!FINAL) {
+          r_wch = a.wch[c];
+          r_cap = a.cap[c];
+        }
       }
       __syncthreads();
       // +x face from the next lane's cell (lane 31 loads its neighbour)
@@ -313,6 +325,7 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
           ff_top_face(a, K, cur, kc, c, col, &f, &t);
           q = ff_add_fast(q, f);
           tsum += t.h;
+          if (FINAL) vol[0] += ff_to_double(ff_mul(f, K.dt));
         }
         // face below, carried to the next level
         float tz = 0.0f;
@@ -345,11 +358,19 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
           ff_bottom_face<ISO>(a, K, cur, c, col, &f, &t);
           q = ff_add_fast(q, f);
           tsum += t.h;
+          if (FINAL && k + 1 == a.nz) vol[1] += ff_to_double(ff_mul(f, K.dt));
+        }
+        const ff wcn = ff_from_double(r_wo);
+        const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
+        if (FINAL) {
+          const ff el = ff_mul(ff_mul(K.V, st), ff_dif(cur.h, ff_from_double(r_ho)));
+          a.w_new[c] = ff_to_double(ff_add_fast(wcn, ff_mul(ff_dif(ff_mul(K.dt, q), el), inv_V)));
+          vol[2] += ff_to_double(el);
+          cur = below;
+          continue;
         }
         // diagonal V (C + Ss wcn/ths) + dt sum T and couplings -dt T (FP32), rhs -Rdt with
         // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q (float-float)
-        const ff wcn = ff_from_double(r_wo);
-        const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
         const float dtf = K.dt.h;
         dg[c] = (double)fmaf(dtf, tsum, K.V.h * (ff_hi_of(r_cap) + st.h));
         a0[c] = (double)(-dtf * tx);
@@ -364,94 +385,14 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
     }
     __syncthreads();  // the next tile restages both buffers
   }
-}
-
-// Net inflow of one cell with its top / bottom boundary parts (pic_row in float-float, each
-// face evaluated from the cells' own values, as pic_row does)
-struct FfRow {
-  ff q, top, bot;
-};
-
-__device__ __forceinline__ FfRow ff_pic_row(const ReArgs& a, const FfConst& K, size_t c,
-                                            size_t col, int i, int j, int k) {
-  const int hm = a.face_mean;
-  const FfCell cur = ff_cell(a, c, col);
-  FfRow r = {ff_make(0.0f), ff_make(0.0f), ff_make(0.0f)};
-  if (i > 0) {
-    const FfCell nb = ff_cell(a, c - 1, col - 1);
-    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.kx, cur.kx), K.cx), ff_dif(nb.h, cur.h)));
-  }
-  if (i + 1 < a.nx) {
-    const FfCell nb = ff_cell(a, c + 1, col + 1);
-    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.kx, nb.kx), K.cx), ff_dif(nb.h, cur.h)));
-  }
-  if (j > 0) {
-    const FfCell nb = ff_cell(a, c - a.nx, col - a.nx);
-    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, nb.ky, cur.ky), K.cy), ff_dif(nb.h, cur.h)));
-  }
-  if (j + 1 < a.ny) {
-    const FfCell nb = ff_cell(a, c + a.nx, col + a.nx);
-    r.q = ff_add_fast(r.q, ff_mul(ff_mul(ff_face_mean(hm, cur.ky, nb.ky), K.cy), ff_dif(nb.h, cur.h)));
-  }
-  if (k > 0) {
-    const FfCell nb = ff_cell(a, c - a.ncol, col);
-    const ff kf = ff_face_mean(hm, nb.kz, cur.kz);
-    r.q = ff_add_fast(r.q, ff_add_fast(ff_mul(ff_mul(kf, K.cz), ff_dif(nb.h, cur.h)), ff_mul(K.Az, kf)));
-  } else {
-    ff t;
-    ff_top_face(a, K, cur, class_of(a, c, col), c, col, &r.top, &t);
-    r.q = ff_add_fast(r.q, r.top);
-  }
-  if (k + 1 < a.nz) {
-    const FfCell nb = ff_cell(a, c + a.ncol, col);
-    const ff kf = ff_face_mean(hm, cur.kz, nb.kz);
-    r.q = ff_add_fast(r.q, ff_dif(ff_mul(ff_mul(kf, K.cz), ff_dif(nb.h, cur.h)), ff_mul(K.Az, kf)));
-  } else {
-    ff t;
-    ff_bottom_face(a, K, cur, c, col, &r.bot, &t);
-    r.q = ff_add_fast(r.q, r.bot);
-  }
-  return r;
-}
-
-// k_pic_final in float-float: th^{n+1} = th^n + (dt Q - V Ss (th^n/ths)(h^{n+1} - h^n)) / V,
-// boundary and elastic volumes (summed in FP64 across the grid) and time
-__global__ void __launch_bounds__(256, 3) k_pic_final_ff(ReArgs a, int planes, int tiles) {
-  const double dtd = a.sc->dt_used;
-  __shared__ FfConst K;  // the launch's constants in shared memory, not in registers
-  __shared__ ff inv_V;
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    K = ff_consts(a, dtd);
-    inv_V = ff_div(ff_make(1.0f), K.V);
-  }
-  __syncthreads();
-  double v[3] = {0.0, 0.0, 0.0};
-  const int t0 = (a.nx + 31) / 32;
-  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const int i = (tile % t0) * 32 + threadIdx.x;
-    const int j = (tile / t0) * 8 + threadIdx.y;
-    if (i >= a.nx || j >= a.ny) continue;
-    const size_t col = (size_t)i + (size_t)a.nx * j;
-    const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
-    for (int k = kb; k < ke; ++k) {
-      const size_t c = col + a.ncol * k;
-      const SoilClass& kc = class_of(a, c, col);
-      const ff wcn = ff_from_double(a.w_old[c]);
-      const FfRow r = ff_pic_row(a, K, c, col, i, j, k);
-      const ff dh = ff_dif(ff_from_double(a.h_new[c]), ff_from_double(a.h_old[c]));
-      const ff el = ff_mul(ff_mul(K.V, ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn)), dh);
-      a.w_new[c] = ff_to_double(ff_add_fast(wcn, ff_mul(ff_dif(ff_mul(K.dt, r.q), el), inv_V)));
-      if (k == 0) v[0] += ff_to_double(ff_mul(r.top, K.dt));
-      if (k + 1 == a.nz) v[1] += ff_to_double(ff_mul(r.bot, K.dt));
-      v[2] += ff_to_double(el);
+  if (FINAL) {
+    double tot[3];
+    if (grid_sum<3>(vol, a.partials, &a.sc->arrive[0], tot) && flat_tid() == 0) {
+      a.sc->vol_top += tot[0];
+      a.sc->vol_bot += tot[1];
+      a.sc->vol_elastic += tot[2];
+      a.sc->time += a.sc->dt_used;
     }
-  }
-  double tot[3];
-  if (grid_sum<3>(v, a.partials, &a.sc->arrive[0], tot) && flat_tid() == 0) {
-    a.sc->vol_top += tot[0];
-    a.sc->vol_bot += tot[1];
-    a.sc->vol_elastic += tot[2];
-    a.sc->time += dtd;
   }
 }
 

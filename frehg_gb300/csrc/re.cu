@@ -691,9 +691,14 @@ static int picard_step(frehg_re* re) {
   if (re->p.picard_fp64)
     FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n,
               k_pic_final<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
+  else if (iso)
+    FG_LAUNCH(prof, st, "k_pic_final_ff", (48.0 + sb) * n,
+              (k_pic_assemble_ff<true, true><<<PL.grid, PL.block, 0, st>>>(
+                  a, nullptr, nullptr, nullptr, nullptr, nullptr, PL.planes, PL.tiles)));
   else
     FG_LAUNCH(prof, st, "k_pic_final_ff", (48.0 + sb) * n,
-              k_pic_final_ff<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
+              (k_pic_assemble_ff<false, true><<<PL.grid, PL.block, 0, st>>>(
+                  a, nullptr, nullptr, nullptr, nullptr, nullptr, PL.planes, PL.tiles)));
   FG_CUDA(cudaGetLastError());
   re->cnt.last_picard_iterations = its;
   if (re->p.picard_dt_adapt) {
