@@ -198,6 +198,10 @@ class KrylovSolver {
   // solves whose result is an update of an iterate (Picard), where the operator's last bits
   // change the update, not the fixed point; solves whose result is the solution keep FP64
   bool ff_operator = false;
+  // leave the solution scaled: x_out is not written, the caller applies x = s x~ itself from
+  // x (x~) and scale_vector(A) (the Picard update fuses it into h += x)
+  bool keep_scaled = false;
+  const double* scale_vector(const Stencil64& A) const { return A.s_in_r ? r : A.s; }
   float* zf = nullptr;
   // vertical-line preconditioner (FP32 factors and sweep scratch)
   int ensure_line(size_t n);

@@ -536,9 +536,11 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
 }
 
 int KrylovSolver::finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResult* res, int nb) {
-  FG_LAUNCH(prof, st, "k_unscale", 24.0 * (double)A.n,
-            k_unscale<<<nb, 256, 0, st>>>(A.s_in_r ? r : A.s, x, x_out, A.n));
-  FG_CUDA(cudaGetLastError());
+  if (!keep_scaled) {
+    FG_LAUNCH(prof, st, "k_unscale", 24.0 * (double)A.n,
+              k_unscale<<<nb, 256, 0, st>>>(scale_vector(A), x, x_out, A.n));
+    FG_CUDA(cudaGetLastError());
+  }
   res->its = hst->its;
   res->reason = hst->status;
   res->rnorm = hst->dp;

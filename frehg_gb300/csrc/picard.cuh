@@ -267,14 +267,17 @@ __global__ void __launch_bounds__(256) k_pic_assemble(ReArgs a, double* __restri
 // maximum compare bit patterns (non-negative doubles order like their 64-bit integers), which
 // keeps them off the FP64 pipe; a NaN in d counts as an infinite change, which fails the
 // convergence test.
-__global__ void k_pic_update(ReArgs a, const double* __restrict__ d) {
+// SCALED: the solver left its solution scaled, d = s x~ is formed here (k_unscale fused)
+template <bool SCALED = false>
+__global__ void k_pic_update(ReArgs a, const double* __restrict__ d,
+                             const double* __restrict__ s = nullptr) {
   const long long kAbs = 0x7fffffffffffffffll;
   long long m = 0;
   const double lim = a.picard_dh_max;
   const long long lim_bits = lim > 0.0 ? __double_as_longlong(lim) : kAbs;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
        c += (size_t)gridDim.x * blockDim.x) {
-    double dc = d[c];
+    double dc = SCALED ? s[c] * d[c] : d[c];
     const long long b = __double_as_longlong(dc);
     long long ab = b & kAbs;
     if (ab > lim_bits) {

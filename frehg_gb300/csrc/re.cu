@@ -650,7 +650,9 @@ static int picard_step(frehg_re* re) {
                       a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b, PL.planes, PL.tiles));
       FG_CUDA(cudaGetLastError());
       CgResult res;
+      re->ksp.keep_scaled = true;  // the update below applies x = s x~
       const int rc = solve_system(re, re->scratch, &res);
+      re->ksp.keep_scaled = false;
       re->cnt.last_ksp_iterations = res.its;
       re->cnt.last_residual_norm = res.rnorm;
       re->cnt.ksp_iterations += res.its;
@@ -659,8 +661,9 @@ static int picard_step(frehg_re* re) {
         fail = rc;
         break;
       }
-      FG_LAUNCH(prof, st, "k_pic_update", 24.0 * n,
-                k_pic_update<<<nb, 256, 0, st>>>(a, re->scratch));
+      FG_LAUNCH(prof, st, "k_pic_update", 32.0 * n,
+                k_pic_update<true><<<nb, 256, 0, st>>>(a, re->ksp.x,
+                                                       re->ksp.scale_vector(re->A)));
       FG_CUDA(cudaGetLastError());
       FG_CUDA(cudaMemcpyAsync(&re->sc_host->dq_max, &re->sc->dq_max, sizeof(double),
                               cudaMemcpyDeviceToHost, st));
