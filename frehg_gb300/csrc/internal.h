@@ -122,6 +122,7 @@ struct CgDevState {
   int its, max_it, status, iter;
   unsigned int arrive[8];
   double ir_bnorm, ir_rnorm;  // refinement loop norms (mixed precision)
+  double rscale;              // the inner right-hand side is r~ / rscale (mixed precision)
   int ir_its, pad_;
 };
 

@@ -37,7 +37,8 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ s, const double* __restrict__ sq, const double* __restrict__ b,
     double* __restrict__ x, double* __restrict__ rres, float* __restrict__ ef, int n0,
-    int n1, int n2, int planes, int tiles, CgDevState* ir, double* partials, double ir_rtol) {
+    int n1, int n2, int planes, int tiles, CgDevState* ir, double* partials, double ir_rtol,
+    float* __restrict__ rfo = nullptr, CgDevState* in = nullptr, double inner_rtol = 0.0) {
   if (ir->status) return;
   const int t0 = (n0 + 31) / 32;
   const size_t s01 = (size_t)n0 * n1;
@@ -88,11 +89,12 @@ __global__ void __launch_bounds__(256) k_ir_residual(
         // sq r~ = r~ / s (INV_S: s holds floats and sq is not stored)
         const float sqc = INV_S ? __frcp_rn(ff_hi_of(s[c])) : ff_hi_of(sq[c]);
         const float q0 = rf * sig0, q1 = rf * sqc * sig1;
+        rfo[c] = q0;  // the next inner solve's right-hand side, r~ / rs0
         k0.add(q0 * q0);
         k1.add(q1 * q1);
       }
     }
-    v[0] = k0.value() * rs0 * rs0;
+    v[0] = k0.value();
     v[1] = k1.value() * rs1 * rs1;
   }
   double tot[3];
@@ -102,11 +104,24 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     if (ir->ir_its == 0) ir->ir_bnorm = sqrt(tot[2]);
     ir->ir_rnorm = rn;
     ir->dp = rn;
-    ir->a = sqrt(tot[0]);  // scale of the inner right-hand side
+    // ||r~||; later sweeps summed (r~ / rs0)^2, the FP32 right-hand side they wrote
+    const double rs0 = FIRST ? 1.0 : ir->a;
+    ir->a = sqrt(tot[0]) * rs0;
     if (isnan(rn) || isinf(rn)) {
       ir->status = kDivergedNanOrInf;
     } else if (rn <= fmax(ir_rtol * ir->ir_bnorm, ir->atol) || tot[0] == 0.0) {
       ir->status = rn < ir->atol ? kConvergedAtol : kConvergedRtol;
+    }
+    if (!FIRST && ir->status == 0) {
+      // the inner CG state, as k_ir_scale sets it, for the right-hand side r~ / rs0
+      ir->rscale = rs0;
+      in->beta = tot[0];
+      in->rnorm0 = sqrt(tot[0]);
+      in->ttol = inner_rtol * in->rnorm0;
+      in->iter = 0;
+      in->its = 0;
+      in->dpi = 0.0;
+      in->status = 0;
     }
   }
 }
@@ -114,7 +129,7 @@ __global__ void __launch_bounds__(256) k_ir_residual(
 // Inner right-hand side rf = fp32(r~ / ||r~||): unit norm, so FP32 products cannot underflow
 // however small the refinement residual is.  The last block initialises the inner CG state.
 __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ rf, size_t n,
-                           const CgDevState* ir, CgDevState* in, double* partials,
+                           CgDevState* ir, CgDevState* in, double* partials,
                            double inner_rtol) {
   if (ir->status) return;
   const float sig = (float)(1.0 / ir->a);
@@ -131,6 +146,7 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
   double tot[1];
   if (!grid_sum<1>(loc, partials, &in->arrive[0], tot)) return;
   if (flat_tid() == 0) {
+    ir->rscale = ir->a;
     in->beta = tot[0];
     in->rnorm0 = sqrt(tot[0]);
     in->ttol = inner_rtol * in->rnorm0;
@@ -410,10 +426,10 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
   }
 }
 
-// x~ += ||r~|| e (the inner system was solved for the unit-norm residual)
+// x~ += rscale e (the inner system was solved for the residual divided by rscale)
 __global__ void k_ir_update(double* __restrict__ x, const float* __restrict__ e, size_t n,
                             const CgDevState* ir) {
-  const double scale = ir->a;
+  const double scale = ir->rscale;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
        c += (size_t)gridDim.x * blockDim.x)
     x[c] = fma(scale, (double)e[c], x[c]);
@@ -856,18 +872,21 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
                       A.a0, A.a1, A.a2, sv, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
                       L.tiles, dst, partials, cfg.ir_rtol));
     } else if (A.s_in_r) {
-      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
+      FG_LAUNCH(prof, st, "k_ir_residual", 64.0 * dn,
                 (k_ir_residual<false, true><<<L.grid, L.block, 0, st>>>(
                     A.a0, A.a1, A.a2, sv, sv, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
-                    L.tiles, dst, partials, cfg.ir_rtol)));
+                    L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol)));
     } else {
-      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
+      FG_LAUNCH(prof, st, "k_ir_residual", 64.0 * dn,
                 k_ir_residual<false><<<L.grid, L.block, 0, st>>>(
                     A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
-                    L.tiles, dst, partials, cfg.ir_rtol));
+                    L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol));
     }
-    FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
-              k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials, cfg.inner_rtol));
+    // the first sweep's right-hand side (unit norm); later residual kernels write theirs
+    if (sweeps == 0)
+      FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
+                k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
+                                               cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());
     FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
