@@ -101,6 +101,10 @@ struct Stencil64 {
   // the float-float path's preparation left s = D^-1/2 in the mixed solver's FP64 vector r
   // (as floats) and d itself in s
   bool s_in_r = false;
+  // the float-float Picard assembly wrote the diagonal as floats into the first n floats of s
+  // and the couplings (unscaled, as floats) into the mixed solver's FP32 operator; only the
+  // float-float preparation (k_prep_ff) reads this form
+  bool f32_entries = false;
   int alloc(int n0, int n1, int n2);
   void release();
 };

@@ -409,6 +409,10 @@ int KrylovSolver::scale(Stencil64& A, cudaStream_t st) {
     return FREHG_ERR_STATE;
   }
   if (A.scaled) return FREHG_OK;
+  if (A.f32_entries) {
+    set_error("operator assembled in FP32 form for the mixed-precision solve (precision 1)");
+    return FREHG_ERR_STATE;
+  }
   const int nb = reduction_blocks(A.n, 256, 4);
   const double n = (double)A.n;
   FG_LAUNCH(prof, st, "k_diag_rsqrt", 16.0 * n, k_diag_rsqrt<<<nb, 256, 0, st>>>(A.s, A.n));

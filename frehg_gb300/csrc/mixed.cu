@@ -27,8 +27,9 @@ namespace fg {
 // r~ = s b - A~ x~ (FP64, kept in rres); e = 0; sums of r~^2 (scale of the inner system),
 // (r~/s)^2 = (sq r~)^2 for the true residual (sq = 1/s) and b^2 for ||b||.  The last block
 // runs the refinement test.
-// FIRST (the first sweep, x~ = 0): r~ = s b without the stencil product, x~ written as 0, and
-// the b^2 sum that ||b|| needs (with x~ = 0 the true residual is b itself).  Later sweeps form
+// FIRST (the first sweep, x~ = 0): r~ = s b without the stencil product (x~ is not read: the
+// first k_ir_update writes it), and the b^2 sum that ||b|| needs (with x~ = 0 the true
+// residual is b itself).  Later sweeps form
 // the stencil product in FP64: the residual is a difference of nearly equal terms, and the
 // refinement converges only as far as this product is accurate (a float-float form, 2^-48,
 // was both slower here and short of 1e-12 on ill-conditioned systems).
@@ -51,7 +52,6 @@ __global__ void __launch_bounds__(256) k_ir_residual(
       const int kb = blockIdx.y * planes, ke = min(n2, kb + planes);
       size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
       for (int k = kb; k < ke; ++k, c += s01) {
-        x[c] = 0.0;
         const double bc = b[c];
         const double r = s[c] * bc;
         rres[c] = r;
@@ -426,13 +426,15 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
   }
 }
 
-// x~ += rscale e (the inner system was solved for the residual divided by rscale)
+// x~ += rscale e (the inner system was solved for the residual divided by rscale); FIRST:
+// x~ = rscale e (x~ was 0 and is not read)
+template <bool FIRST>
 __global__ void k_ir_update(double* __restrict__ x, const float* __restrict__ e, size_t n,
                             const CgDevState* ir) {
   const double scale = ir->rscale;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
        c += (size_t)gridDim.x * blockDim.x)
-    x[c] = fma(scale, (double)e[c], x[c]);
+    x[c] = FIRST ? scale * (double)e[c] : fma(scale, (double)e[c], x[c]);
 }
 
 __global__ void k_to_f32(const double* __restrict__ a0, const double* __restrict__ a1,
@@ -562,12 +564,10 @@ __device__ __forceinline__ ff scaled_coupling64(double* a, size_t c, double sc, 
 
 // the float-float path's scale factors are floats, and so are the couplings the float-float
 // Picard assembly writes: a s_c s_n = a (p_h + p_l) with p = s_c s_n exact, one float-float by
-// float product; a coupling with more than 24 significant bits takes the float-float split
-__device__ __forceinline__ ff scaled_coupling_f(double* a, size_t c, float sc, float sn) {
-  const double ad = a[c];
-  const ff p = two_prod(sc, sn);
-  const ff v = ((unsigned)__double2loint(ad) & 0x1fffffffu) == 0u ? ff_mul_f(p, ff_hi_of(ad))
-                                                                 : ff_mul(ff_from_double(ad), p);
+// float product, stored in FP64 for the refinement residual
+__device__ __forceinline__ ff scaled_coupling_f(float af, double* a, size_t c, float sc,
+                                                float sn) {
+  const ff v = ff_mul_f(two_prod(sc, sn), af);
   a[c] = ff_to_double(v);
   return v;
 }
@@ -629,18 +629,18 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
 // scaled couplings a s_c s_n in float-float and their FP32 copies; the line factors as in
 // k_scale_mixed; and the first refinement sweep's residual r~ = s b with x~ = 0 (FP64), its
 // sums and test, as k_ir_residual<true>.  This replaces k_diag_rsqrt_sq, k_scale_mixed and the
-// first k_ir_residual: the diagonal, the couplings and b are read once.
-__device__ __forceinline__ float scale_of(double d) {
-  return rsqrtf((__double_as_longlong(d) << 1) == 0 ? 1.0f : ff_hi_of(d));
-}
+// first k_ir_residual: the diagonal, the couplings and b are read once.  The assembly wrote
+// the diagonal (dg) and the unscaled couplings (f0-f2) as floats; f0-f2 are overwritten in
+// place by the scaled FP32 copies, and the FP64 scaled couplings go to a0-a2.
+__device__ __forceinline__ float scale_of(float d) { return rsqrtf(d == 0.0f ? 1.0f : d); }
 
 __global__ void __launch_bounds__(128) k_prep_ff(
     double* __restrict__ a0, double* __restrict__ a1, double* __restrict__ a2,
-    const double* __restrict__ dg, const double* __restrict__ b, double* __restrict__ s_out,
-    double* __restrict__ x, double* __restrict__ rres, float* __restrict__ ef,
-    float* __restrict__ f0, float* __restrict__ f1, float* __restrict__ f2,
-    float* __restrict__ lk, float* __restrict__ dinv, int n0, int n1, int n2, int line,
-    CgDevState* ir, double* partials, double ir_rtol) {
+    const float* __restrict__ dg, const double* __restrict__ b, double* __restrict__ s_out,
+    double* __restrict__ rres, float* __restrict__ ef, float* __restrict__ f0,
+    float* __restrict__ f1, float* __restrict__ f2, float* __restrict__ lk,
+    float* __restrict__ dinv, int n0, int n1, int n2, int line, CgDevState* ir,
+    double* partials, double ir_rtol) {
   const int ncol = n0 * n1;
   const size_t sk = (size_t)ncol;
   const ff zero = ff_make(0.0f);
@@ -655,11 +655,11 @@ __global__ void __launch_bounds__(128) k_prep_ff(
       const float sb = (k + 1 < n2) ? scale_of(dg[c + sk]) : 0.0f;
       s_out[c] = (double)sc;
       ff v0 = zero, v1 = zero, v2 = zero;
-      if (i0 + 1 < n0) v0 = scaled_coupling_f(a0, c, sc, scale_of(dg[c + 1]));
+      if (i0 + 1 < n0) v0 = scaled_coupling_f(f0[c], a0, c, sc, scale_of(dg[c + 1]));
       else a0[c] = 0.0;
-      if (i1 + 1 < n1) v1 = scaled_coupling_f(a1, c, sc, scale_of(dg[c + n0]));
+      if (i1 + 1 < n1) v1 = scaled_coupling_f(f1[c], a1, c, sc, scale_of(dg[c + n0]));
       else a1[c] = 0.0;
-      if (k + 1 < n2) v2 = scaled_coupling_f(a2, c, sc, sb);
+      if (k + 1 < n2) v2 = scaled_coupling_f(f2[c], a2, c, sc, sb);
       else a2[c] = 0.0;
       f0[c] = v0.h;
       f1[c] = v1.h;
@@ -676,10 +676,9 @@ __global__ void __launch_bounds__(128) k_prep_ff(
         dinv[c] = inv_d.h;
         aprev = v2;
       }
-      // first sweep: x~ = 0, r~ = s b
+      // first sweep: x~ = 0 (the first k_ir_update writes x~ without reading it), r~ = s b
       const double bc = b[c];
       const double r = (double)sc * bc;
-      x[c] = 0.0;
       rres[c] = r;
       ef[c] = 0.0f;
       v[0] = fma(r, r, v[0]);
@@ -721,21 +720,32 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
   const int ncol = A.n0 * A.n1;
   const int lb = (int)std::min<long>((ncol + 127) / 128, kMaxRedBlocks);
   first_done = false;
+  if (A.f32_entries && (A.scaled || !ff_operator)) {
+    set_error("FP32-form operator outside the float-float preparation");
+    return FREHG_ERR_STATE;
+  }
   if (!A.scaled) {
     if (ff_operator) {
+      if (!A.f32_entries) {
+        set_error("the float-float preparation needs the assembly's FP32-form operator");
+        return FREHG_ERR_STATE;
+      }
       // the refinement state, then one pass: scale factors, scaled operator, FP32 copy, line
       // factors and the first sweep's residual
       CgDevState ir0;
       memset(&ir0, 0, sizeof(ir0));
       ir0.atol = cfg.atol;
       FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
-      FG_LAUNCH(prof, st, "k_prep_ff", (8.0 + 48.0 + 12.0 + 8.0 + (line ? 8.0 : 0.0) + 36.0) * dn,
-                k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, A.s, A.b, r, x, rres, xf,
-                                              op32.a0, op32.a1, op32.a2, lkf, dinvf, A.n0, A.n1,
-                                              A.n2, line ? 1 : 0, dst, partials, cfg.ir_rtol));
+      FG_LAUNCH(prof, st, "k_prep_ff",
+                (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 8.0 + 4.0 + (line ? 8.0 : 0.0)) * dn,
+                k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, reinterpret_cast<const float*>(A.s),
+                                              A.b, r, rres, xf, op32.a0, op32.a1, op32.a2, lkf,
+                                              dinvf, A.n0, A.n1, A.n2, line ? 1 : 0, dst,
+                                              partials, cfg.ir_rtol));
       FG_CUDA(cudaGetLastError());
       A.scaled = true;
       A.s_in_r = true;
+      A.f32_entries = false;
       first_done = true;
       return FREHG_OK;
     }
@@ -978,13 +988,20 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       fprintf(stderr, "ir sweep %d: true |r| %.3e / |b| %.3e ; inner its %d status %d |r0| %.3e -> %.3e\n",
               sweeps, hst->ir_rnorm, hst->ir_bnorm, hst32->its, hst32->status, hst32->rnorm0,
               hst32->dp);
-    FG_LAUNCH(prof, st, "k_ir_update", 20.0 * dn,
-              k_ir_update<<<nb, 256, 0, st>>>(x, xf, n, dst));
+    if (sweeps == 0)
+      FG_LAUNCH(prof, st, "k_ir_update", 12.0 * dn,
+                k_ir_update<true><<<nb, 256, 0, st>>>(x, xf, n, dst));
+    else
+      FG_LAUNCH(prof, st, "k_ir_update", 20.0 * dn,
+                k_ir_update<false><<<nb, 256, 0, st>>>(x, xf, n, dst));
     FG_CUDA(cudaGetLastError());
     ++sweeps;
     // next sweep's residual kernel re-arms the refinement bookkeeping
     FG_CUDA(cudaMemcpyAsync(&dst->ir_its, &sweeps, sizeof(int), cudaMemcpyHostToDevice, st));
   }
+  // stopped before the first update: x~ = 0
+  if (sweeps == 0)
+    FG_LAUNCH(prof, st, "k_zero64", 8.0 * dn, k_zero64<<<nb, 256, 0, st>>>(x, n));
   FG_TRY(finish64(A, x_out, st, res, nb));
   res->its = inner_total;
   res->inner_its = inner_total;

@@ -171,11 +171,13 @@ struct FfYPlane {
 // th^{n+1} = th^n + (dt Q - V Ss (th^n/ths)(h^{n+1} - h^n)) / V (k_pic_final's job) instead of
 // the system, with the top / bottom / elastic volumes summed across the grid (FP64) and the
 // time advanced.
-template <bool ISO, bool FINAL = false>
-__global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __restrict__ dg,
-                                                           double* __restrict__ a0,
-                                                           double* __restrict__ a1,
-                                                           double* __restrict__ a2,
+// T: the type of the diagonal and couplings written (FP32 values either way; float when the
+// mixed-precision solve's preparation reads them, which halves their traffic).
+template <bool ISO, bool FINAL = false, typename T = double>
+__global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restrict__ dg,
+                                                           T* __restrict__ a0,
+                                                           T* __restrict__ a1,
+                                                           T* __restrict__ a2,
                                                            double* __restrict__ bvec, int planes,
                                                            int tiles) {
   __shared__ FfYPlane ys[2];
@@ -372,10 +374,10 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, double* __
         // diagonal V (C + Ss wcn/ths) + dt sum T and couplings -dt T (FP32), rhs -Rdt with
         // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q (float-float)
         const float dtf = K.dt.h;
-        dg[c] = (double)fmaf(dtf, tsum, K.V.h * (ff_hi_of(r_cap) + st.h));
-        a0[c] = (double)(-dtf * tx);
-        a1[c] = (double)(-dtf * ty);
-        a2[c] = (double)(-dtf * tz);
+        dg[c] = (T)fmaf(dtf, tsum, K.V.h * (ff_hi_of(r_cap) + st.h));
+        a0[c] = (T)(-dtf * tx);
+        a1[c] = (T)(-dtf * ty);
+        a2[c] = (T)(-dtf * tz);
         const ff dth = ff_dif(ff_from_double(r_wch), wcn);
         const ff dh = ff_dif(cur.h, ff_from_double(r_ho));
         const ff rdt = ff_dif(ff_mul(K.V, ff_add_fast(dth, ff_mul(st, dh))), ff_mul(K.dt, q));

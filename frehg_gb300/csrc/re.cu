@@ -443,6 +443,11 @@ static int time_network(frehg_re* re) {
 // fallback), M = the vertical-line solve for "unet-line" (line-PCG fallback).  The first solve
 // runs the fallback method and sets the threshold (2x its inner iterations) beyond which a
 // solve switches to it.
+// whether solve_system takes the mixed-precision path (the learned preconditioners run in it)
+static bool mixed_solve(const frehg_re* re) {
+  return re->cfg.precision == 1 || !strncmp(re->cfg.pc_type, "unet", 4);
+}
+
 static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
   cudaStream_t st = re->stream;
   frehg_solver_config cfg = re->cfg;
@@ -534,6 +539,7 @@ static int pca_step(frehg_re* re) {
   const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
   re->A.scaled = false;
   re->A.s_in_r = false;
+  re->A.f32_entries = false;
   FG_LAUNCH(prof, st, "k_assemble", (72.0 + sb) * n,
             k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2,
                                                    re->A.b, L.planes, L.tiles));
@@ -616,6 +622,9 @@ static int picard_step(frehg_re* re) {
     iso = true;
     for (const SoilClass& k : re->cls_host) iso = iso && k.ks_iso;
   }
+  // a float-float assembly solved in mixed precision writes its matrix entries as floats
+  const bool f32 = !re->p.picard_fp64 && mixed_solve(re);
+  if (f32) FG_TRY(re->ksp.ensure32(re->n));
   int its = 0;
   for (;;) {
     FG_CUDA(cudaMemcpyAsync(&re->sc->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st));
@@ -635,12 +644,25 @@ static int picard_step(frehg_re* re) {
                                                                 re->cap)));
       re->A.scaled = false;
       re->A.s_in_r = false;
+      re->A.f32_entries = f32;
       if (re->p.picard_fp64)
         FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
                   k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
                                                                re->A.a2, re->A.b, PL.planes,
                                                                PL.tiles));
-      else if (iso)
+      else if (f32) {
+        // diagonal and couplings as floats (the float-float preparation's input)
+        float* dgf = reinterpret_cast<float*>(re->A.s);
+        const Stencil32& o = re->ksp.op32;
+        if (iso)
+          FG_LAUNCH(prof, st, "k_pic_assemble_ff", (48.0 + sb) * n,
+                    (k_pic_assemble_ff<true, false, float><<<PL.grid, PL.block, 0, st>>>(
+                        a, dgf, o.a0, o.a1, o.a2, re->A.b, PL.planes, PL.tiles)));
+        else
+          FG_LAUNCH(prof, st, "k_pic_assemble_ff", (48.0 + sb) * n,
+                    (k_pic_assemble_ff<false, false, float><<<PL.grid, PL.block, 0, st>>>(
+                        a, dgf, o.a0, o.a1, o.a2, re->A.b, PL.planes, PL.tiles)));
+      } else if (iso)
         FG_LAUNCH(prof, st, "k_pic_assemble_ff", (64.0 + sb) * n,
                   k_pic_assemble_ff<true><<<PL.grid, PL.block, 0, st>>>(
                       a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b, PL.planes, PL.tiles));
@@ -696,11 +718,11 @@ static int picard_step(frehg_re* re) {
               k_pic_final<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
   else if (iso)
     FG_LAUNCH(prof, st, "k_pic_final_ff", (48.0 + sb) * n,
-              (k_pic_assemble_ff<true, true><<<PL.grid, PL.block, 0, st>>>(
+              (k_pic_assemble_ff<true, true, double><<<PL.grid, PL.block, 0, st>>>(
                   a, nullptr, nullptr, nullptr, nullptr, nullptr, PL.planes, PL.tiles)));
   else
     FG_LAUNCH(prof, st, "k_pic_final_ff", (48.0 + sb) * n,
-              (k_pic_assemble_ff<false, true><<<PL.grid, PL.block, 0, st>>>(
+              (k_pic_assemble_ff<false, true, double><<<PL.grid, PL.block, 0, st>>>(
                   a, nullptr, nullptr, nullptr, nullptr, nullptr, PL.planes, PL.tiles)));
   FG_CUDA(cudaGetLastError());
   re->cnt.last_picard_iterations = its;
@@ -1344,6 +1366,7 @@ int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, int targ
   const StencilLaunch L = stencil_launch(re->nx, re->ny, re->nz);
   re->A.scaled = false;
   re->A.s_in_r = false;
+  re->A.f32_entries = false;
   k_assemble<<<L.grid, L.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b,
                                          L.planes, L.tiles);
   k_net_fields<<<nb, 256, 0, st>>>(a, lnk_out, cap_out);

@@ -270,6 +270,7 @@ int frehg_system_end_assembly(frehg_system* s) {
   FG_CUDA(cudaMemcpy(s->A.a2, s->up2.data(), s->n * sizeof(double), cudaMemcpyHostToDevice));
   s->A.scaled = false;
   s->A.s_in_r = false;
+  s->A.f32_entries = false;
   s->assembled = true;
   return FREHG_OK;
 }
