@@ -648,18 +648,36 @@ __global__ void __launch_bounds__(128) k_prep_ff(
   for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
        col += gridDim.x * blockDim.x) {
     const int i0 = col % n0, i1 = col / n0;
+    const bool hx = i0 + 1 < n0, hy = i1 + 1 < n1;
     ff inv_d = ff_make(1.0f), aprev = zero;
     size_t c = (size_t)col;
+    // level k's inputs are loaded one level ahead (two levels of loads in flight per thread)
     float sc = scale_of(dg[c]);
+    float q0 = f0[c], q1 = f1[c], q2 = f2[c];
+    float dx = hx ? dg[c + 1] : 1.0f, dy = hy ? dg[c + n0] : 1.0f;
+    float dz = n2 > 1 ? dg[c + sk] : 1.0f;
+    double bq = b[c];
     for (int k = 0; k < n2; ++k, c += sk) {
-      const float sb = (k + 1 < n2) ? scale_of(dg[c + sk]) : 0.0f;
+      const float e0 = q0, e1 = q1, e2 = q2, ex = dx, ey = dy, ez = dz;
+      const double bc = bq;
+      if (k + 1 < n2) {
+        const size_t cn = c + sk;
+        q0 = f0[cn];
+        q1 = f1[cn];
+        q2 = f2[cn];
+        dx = hx ? dg[cn + 1] : 1.0f;
+        dy = hy ? dg[cn + n0] : 1.0f;
+        dz = k + 2 < n2 ? dg[cn + sk] : 1.0f;
+        bq = b[cn];
+      }
+      const float sb = (k + 1 < n2) ? scale_of(ez) : 0.0f;
       s_out[c] = (double)sc;
       ff v0 = zero, v1 = zero, v2 = zero;
-      if (i0 + 1 < n0) v0 = scaled_coupling_f(f0[c], a0, c, sc, scale_of(dg[c + 1]));
+      if (hx) v0 = scaled_coupling_f(e0, a0, c, sc, scale_of(ex));
       else a0[c] = 0.0;
-      if (i1 + 1 < n1) v1 = scaled_coupling_f(f1[c], a1, c, sc, scale_of(dg[c + n0]));
+      if (hy) v1 = scaled_coupling_f(e1, a1, c, sc, scale_of(ey));
       else a1[c] = 0.0;
-      if (k + 1 < n2) v2 = scaled_coupling_f(f2[c], a2, c, sc, sb);
+      if (k + 1 < n2) v2 = scaled_coupling_f(e2, a2, c, sc, sb);
       else a2[c] = 0.0;
       f0[c] = v0.h;
       f1[c] = v1.h;
@@ -677,7 +695,6 @@ __global__ void __launch_bounds__(128) k_prep_ff(
         aprev = v2;
       }
       // first sweep: x~ = 0 (the first k_ir_update writes x~ without reading it), r~ = s b
-      const double bc = b[c];
       const double r = (double)sc * bc;
       rres[c] = r;
       ef[c] = 0.0f;
