@@ -64,6 +64,8 @@ __global__ void __launch_bounds__(128) k32_line_fwd(float* __restrict__ x, float
                                                     CgDevState* st, double* partials) {
   if (st->status) return;
   const float a = UPDATE ? (float)st->a : 0.0f;
+  // the first update writes x = alpha p (x is not initialised)
+  const bool xfirst = UPDATE && st->iter == 0;
   const size_t sk = (size_t)ncol;
   Kahan32 rz, rr;
   for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(128) k32_line_fwd(float* __restrict__ x, float
           lv[q] = lk[c];
           dv[q] = dinv[c];
           if (UPDATE) {
-            xv[q] = x[c];
+            xv[q] = xfirst ? 0.0f : x[c];
             pv[q] = p[c];
             wv[q] = w[c];
           }

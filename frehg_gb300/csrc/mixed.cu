@@ -24,21 +24,22 @@
 
 namespace fg {
 
-// r~ = s b - A~ x~ (FP64, kept in rres); e = 0; sums of r~^2 (scale of the inner system),
+// r~ = s b - A~ x~ (FP64, kept in rres); sums of r~^2 (scale of the inner system),
 // (r~/s)^2 = (sq r~)^2 for the true residual (sq = 1/s) and b^2 for ||b||.  The last block
-// runs the refinement test.
+// runs the refinement test.  The inner solution e needs no zeroing: the inner solve's first
+// update writes it.
 // FIRST (the first sweep, x~ = 0): r~ = s b without the stencil product (x~ is not read: the
 // first k_ir_update writes it), and the b^2 sum that ||b|| needs (with x~ = 0 the true
-// residual is b itself).  Later sweeps form
-// the stencil product in FP64: the residual is a difference of nearly equal terms, and the
-// refinement converges only as far as this product is accurate (a float-float form, 2^-48,
-// was both slower here and short of 1e-12 on ill-conditioned systems).
+// residual is b itself).  Later sweeps form the stencil product in FP64: the residual is a
+// difference of nearly equal terms, and the refinement converges only as far as this product
+// is accurate (a float-float form, 2^-48, was both slower here and short of 1e-12 on
+// ill-conditioned systems).
 template <bool FIRST, bool INV_S = false>
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ s, const double* __restrict__ sq, const double* __restrict__ b,
-    double* __restrict__ x, double* __restrict__ rres, float* __restrict__ ef, int n0,
-    int n1, int n2, int planes, int tiles, CgDevState* ir, double* partials, double ir_rtol,
+    double* __restrict__ x, double* __restrict__ rres, int n0, int n1, int n2, int planes,
+    int tiles, CgDevState* ir, double* partials, double ir_rtol,
     float* __restrict__ rfo = nullptr, CgDevState* in = nullptr, double inner_rtol = 0.0) {
   if (ir->status) return;
   const int t0 = (n0 + 31) / 32;
@@ -55,7 +56,6 @@ __global__ void __launch_bounds__(256) k_ir_residual(
         const double bc = b[c];
         const double r = s[c] * bc;
         rres[c] = r;
-        ef[c] = 0.0f;
         v[0] = fma(r, r, v[0]);
         v[2] = fma(bc, bc, v[2]);
       }
@@ -84,7 +84,6 @@ __global__ void __launch_bounds__(256) k_ir_residual(
         if (k + 1 < n2) ax = fma(a2[c], x[c + s01], ax);
         const double r = fma(s[c], b[c], -ax);
         rres[c] = r;
-        ef[c] = 0.0f;
         const float rf = ff_hi_of(r);
         // sq r~ = r~ / s (INV_S: s holds floats and sq is not stored)
         const float sqc = INV_S ? __frcp_rn(ff_hi_of(s[c])) : ff_hi_of(sq[c]);
@@ -134,10 +133,23 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
   if (ir->status) return;
   const float sig = (float)(1.0 / ir->a);
   Kahan32 acc;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
-       c += (size_t)gridDim.x * blockDim.x) {
-    // the FP32 right-hand side from the residual's leading 24 bits (integer split: GB300's
-    // double->float conversion runs on the FP64 pipe)
+  // the FP32 right-hand side from the residual's leading 24 bits (integer split: GB300's
+  // double->float conversion runs on the FP64 pipe); four cells per step, 16-byte accesses
+  const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const double2* r2 = reinterpret_cast<const double2*>(rres);
+  float4* f4 = reinterpret_cast<float4*>(rf);
+  for (size_t q = gid; q < n / 4; q += stride) {
+    const double2 lo = r2[2 * q], hi = r2[2 * q + 1];
+    const float4 v = make_float4(ff_hi_of(lo.x) * sig, ff_hi_of(lo.y) * sig,
+                                 ff_hi_of(hi.x) * sig, ff_hi_of(hi.y) * sig);
+    f4[q] = v;
+    acc.add(v.x * v.x);
+    acc.add(v.y * v.y);
+    acc.add(v.z * v.z);
+    acc.add(v.w * v.w);
+  }
+  for (size_t c = (n & ~(size_t)3) + gid; c < n; c += stride) {
     const float r32 = ff_hi_of(rres[c]) * sig;
     rf[c] = r32;
     acc.add(r32 * r32);
@@ -372,6 +384,8 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
                            CgDevState* st, double* partials) {
   if (st->status) return;
   const float a = (float)st->a;
+  // the first iteration writes e = a p (e is not initialised)
+  const bool first = st->iter == 0;
   Kahan32 acc;
   const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -380,7 +394,7 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
   const float4* p4 = reinterpret_cast<const float4*>(p);
   const float4* w4 = reinterpret_cast<const float4*>(w);
   for (size_t q = gid; q < n / 4; q += stride) {
-    float4 ev = e4[q], rv = r4[q];
+    float4 ev = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : e4[q], rv = r4[q];
     const float4 pv = p4[q], wv = w4[q];
     ev.x = fmaf(a, pv.x, ev.x);
     ev.y = fmaf(a, pv.y, ev.y);
@@ -399,7 +413,7 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
   }
   if (gid < (n & 3)) {
     const size_t c = (n & ~(size_t)3) + gid;
-    e[c] = fmaf(a, p[c], e[c]);
+    e[c] = fmaf(a, p[c], first ? 0.0f : e[c]);
     const float rc = fmaf(-a, w[c], r[c]);
     r[c] = rc;
     acc.add(rc * rc);
@@ -427,14 +441,44 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
 }
 
 // x~ += rscale e (the inner system was solved for the residual divided by rscale); FIRST:
-// x~ = rscale e (x~ was 0 and is not read)
+// x~ = rscale e (x~ was 0 and is not read).  The inner solve's first update writes e without
+// reading it, so e holds nothing before it: an inner solve that stopped before its first
+// iteration (in->iter == 0) contributes e = 0.  Four cells per step with 16-byte loads and
+// stores (the buffers are whole cudaMalloc allocations: 256-byte aligned).
+template <bool FIRST>
+__device__ __forceinline__ double ir_step(double scale, float e, double x) {
+  return FIRST ? scale * (double)e : fma(scale, (double)e, x);
+}
+
 template <bool FIRST>
 __global__ void k_ir_update(double* __restrict__ x, const float* __restrict__ e, size_t n,
-                            const CgDevState* ir) {
+                            const CgDevState* ir, const CgDevState* in) {
+  const size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if (in->iter == 0) {
+    if (FIRST)
+      for (size_t c = gid; c < n; c += stride) x[c] = 0.0;
+    return;
+  }
   const double scale = ir->rscale;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
-       c += (size_t)gridDim.x * blockDim.x)
-    x[c] = FIRST ? scale * (double)e[c] : fma(scale, (double)e[c], x[c]);
+  const float4* e4 = reinterpret_cast<const float4*>(e);
+  double2* x2 = reinterpret_cast<double2*>(x);
+  for (size_t q = gid; q < n / 4; q += stride) {
+    const float4 ev = e4[q];
+    double2 lo = make_double2(0.0, 0.0), hi = lo;
+    if (!FIRST) {
+      lo = x2[2 * q];
+      hi = x2[2 * q + 1];
+    }
+    lo.x = ir_step<FIRST>(scale, ev.x, lo.x);
+    lo.y = ir_step<FIRST>(scale, ev.y, lo.y);
+    hi.x = ir_step<FIRST>(scale, ev.z, hi.x);
+    hi.y = ir_step<FIRST>(scale, ev.w, hi.y);
+    x2[2 * q] = lo;
+    x2[2 * q + 1] = hi;
+  }
+  for (size_t c = (n & ~(size_t)3) + gid; c < n; c += stride)
+    x[c] = ir_step<FIRST>(scale, e[c], FIRST ? 0.0 : x[c]);
 }
 
 __global__ void k_to_f32(const double* __restrict__ a0, const double* __restrict__ a1,
@@ -637,7 +681,7 @@ __device__ __forceinline__ float scale_of(float d) { return rsqrtf(d == 0.0f ? 1
 __global__ void __launch_bounds__(128) k_prep_ff(
     double* __restrict__ a0, double* __restrict__ a1, double* __restrict__ a2,
     const float* __restrict__ dg, const double* __restrict__ b, double* __restrict__ s_out,
-    double* __restrict__ rres, float* __restrict__ ef, float* __restrict__ f0,
+    double* __restrict__ rres, float* __restrict__ f0,
     float* __restrict__ f1, float* __restrict__ f2, float* __restrict__ lk,
     float* __restrict__ dinv, int n0, int n1, int n2, int line, CgDevState* ir,
     double* partials, double ir_rtol) {
@@ -697,7 +741,6 @@ __global__ void __launch_bounds__(128) k_prep_ff(
       // first sweep: x~ = 0 (the first k_ir_update writes x~ without reading it), r~ = s b
       const double r = (double)sc * bc;
       rres[c] = r;
-      ef[c] = 0.0f;
       v[0] = fma(r, r, v[0]);
       v[2] = fma(bc, bc, v[2]);
       sc = sb;
@@ -754,9 +797,9 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
       ir0.atol = cfg.atol;
       FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
       FG_LAUNCH(prof, st, "k_prep_ff",
-                (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 8.0 + 4.0 + (line ? 8.0 : 0.0)) * dn,
+                (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 8.0 + (line ? 8.0 : 0.0)) * dn,
                 k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, reinterpret_cast<const float*>(A.s),
-                                              A.b, r, rres, xf, op32.a0, op32.a1, op32.a2, lkf,
+                                              A.b, r, rres, op32.a0, op32.a1, op32.a2, lkf,
                                               dinvf, A.n0, A.n1, A.n2, line ? 1 : 0, dst,
                                               partials, cfg.ir_rtol));
       FG_CUDA(cudaGetLastError());
@@ -894,19 +937,19 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   for (;;) {
     if (sweeps == 0) {
       if (!first_done_here)
-        FG_LAUNCH(prof, st, "k_ir_residual0", 40.0 * dn,
+        FG_LAUNCH(prof, st, "k_ir_residual0", 24.0 * dn,
                   k_ir_residual<true><<<L.grid, L.block, 0, st>>>(
-                      A.a0, A.a1, A.a2, sv, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                      A.a0, A.a1, A.a2, sv, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                       L.tiles, dst, partials, cfg.ir_rtol));
     } else if (A.s_in_r) {
-      FG_LAUNCH(prof, st, "k_ir_residual", 64.0 * dn,
+      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
                 (k_ir_residual<false, true><<<L.grid, L.block, 0, st>>>(
-                    A.a0, A.a1, A.a2, sv, sv, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                    A.a0, A.a1, A.a2, sv, sv, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                     L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol)));
     } else {
-      FG_LAUNCH(prof, st, "k_ir_residual", 64.0 * dn,
+      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
                 k_ir_residual<false><<<L.grid, L.block, 0, st>>>(
-                    A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, xf, A.n0, A.n1, A.n2, L.planes,
+                    A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                     L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol));
     }
     // the first sweep's right-hand side (unit norm); later residual kernels write theirs
@@ -1007,10 +1050,10 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
               hst32->dp);
     if (sweeps == 0)
       FG_LAUNCH(prof, st, "k_ir_update", 12.0 * dn,
-                k_ir_update<true><<<nb, 256, 0, st>>>(x, xf, n, dst));
+                k_ir_update<true><<<nb, 256, 0, st>>>(x, xf, n, dst, dst32));
     else
       FG_LAUNCH(prof, st, "k_ir_update", 20.0 * dn,
-                k_ir_update<false><<<nb, 256, 0, st>>>(x, xf, n, dst));
+                k_ir_update<false><<<nb, 256, 0, st>>>(x, xf, n, dst, dst32));
     FG_CUDA(cudaGetLastError());
     ++sweeps;
     // next sweep's residual kernel re-arms the refinement bookkeeping
