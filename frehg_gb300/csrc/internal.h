@@ -127,7 +127,8 @@ struct CgDevState {
   unsigned int arrive[8];
   double ir_bnorm, ir_rnorm;  // refinement loop norms (mixed precision)
   double rscale;              // the inner right-hand side is r~ / rscale (mixed precision)
-  int ir_its, pad_;
+  int ir_its;
+  int rhs_rescale;  // k_prep_ff: its power-of-two scaled right-hand side needs k_ir_scale instead
 };
 
 // KSPConvergedReason values
@@ -213,6 +214,7 @@ class KrylovSolver {
   // scaling of the operator for the mixed path (sq = D^1/2 into r, FP32 copy, line factors)
   int prep_mixed(Stencil64& A, cudaStream_t st, bool line, const frehg_solver_config& cfg);
   bool first_done = false;  // prep_mixed formed the first refinement residual and its state
+  double first_rnorm = 0.0;  // the last solve's first residual norm (scale of the next one's)
   size_t cap_line = 0;
   float *lkf = nullptr, *dinvf = nullptr, *uf = nullptr;
   int g32_line = 0;

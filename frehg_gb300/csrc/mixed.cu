@@ -17,6 +17,7 @@
 #include "line.cuh"
 #include "reduce.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -24,13 +25,14 @@
 
 namespace fg {
 
-// r~ = s b - A~ x~ (FP64, kept in rres); sums of r~^2 (scale of the inner system),
+// r~ = s b - A~ x~ (FP64); sums of r~^2 (scale of the inner system),
 // (r~/s)^2 = (sq r~)^2 for the true residual (sq = 1/s) and b^2 for ||b||.  The last block
 // runs the refinement test.  The inner solution e needs no zeroing: the inner solve's first
 // update writes it.
-// FIRST (the first sweep, x~ = 0): r~ = s b without the stencil product (x~ is not read: the
-// first k_ir_update writes it), and the b^2 sum that ||b|| needs (with x~ = 0 the true
-// residual is b itself).  Later sweeps form the stencil product in FP64: the residual is a
+// FIRST (the first sweep, x~ = 0): r~ = s b without the stencil product, kept in rres for
+// k_ir_scale (x~ is not read: the first k_ir_update writes it), and the b^2 sum that ||b||
+// needs (with x~ = 0 the true residual is b itself).  Later sweeps write the next inner
+// right-hand side themselves and form the stencil product in FP64: the residual is a
 // difference of nearly equal terms, and the refinement converges only as far as this product
 // is accurate (a float-float form, 2^-48, was both slower here and short of 1e-12 on
 // ill-conditioned systems).
@@ -83,7 +85,6 @@ __global__ void __launch_bounds__(256) k_ir_residual(
         if (k > 0) ax = fma(a2[c - s01], x[c - s01], ax);
         if (k + 1 < n2) ax = fma(a2[c], x[c + s01], ax);
         const double r = fma(s[c], b[c], -ax);
-        rres[c] = r;
         const float rf = ff_hi_of(r);
         // sq r~ = r~ / s (INV_S: s holds floats and sq is not stored)
         const float sqc = INV_S ? __frcp_rn(ff_hi_of(s[c])) : ff_hi_of(sq[c]);
@@ -127,9 +128,11 @@ __global__ void __launch_bounds__(256) k_ir_residual(
 
 // Inner right-hand side rf = fp32(r~ / ||r~||): unit norm, so FP32 products cannot underflow
 // however small the refinement residual is.  The last block initialises the inner CG state.
+// SB: r~ = s b is formed here from the scale factors and b (rres = s, sb = b) instead of read.
+template <bool SB = false>
 __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ rf, size_t n,
                            CgDevState* ir, CgDevState* in, double* partials,
-                           double inner_rtol) {
+                           double inner_rtol, const double* __restrict__ sb = nullptr) {
   if (ir->status) return;
   const float sig = (float)(1.0 / ir->a);
   Kahan32 acc;
@@ -139,8 +142,16 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   const double2* r2 = reinterpret_cast<const double2*>(rres);
   float4* f4 = reinterpret_cast<float4*>(rf);
+  const double2* b2 = reinterpret_cast<const double2*>(sb);
   for (size_t q = gid; q < n / 4; q += stride) {
-    const double2 lo = r2[2 * q], hi = r2[2 * q + 1];
+    double2 lo = r2[2 * q], hi = r2[2 * q + 1];
+    if (SB) {
+      const double2 blo = b2[2 * q], bhi = b2[2 * q + 1];
+      lo.x *= blo.x;
+      lo.y *= blo.y;
+      hi.x *= bhi.x;
+      hi.y *= bhi.y;
+    }
     const float4 v = make_float4(ff_hi_of(lo.x) * sig, ff_hi_of(lo.y) * sig,
                                  ff_hi_of(hi.x) * sig, ff_hi_of(hi.y) * sig);
     f4[q] = v;
@@ -150,7 +161,7 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
     acc.add(v.w * v.w);
   }
   for (size_t c = (n & ~(size_t)3) + gid; c < n; c += stride) {
-    const float r32 = ff_hi_of(rres[c]) * sig;
+    const float r32 = ff_hi_of(SB ? rres[c] * sb[c] : rres[c]) * sig;
     rf[c] = r32;
     acc.add(r32 * r32);
   }
@@ -672,8 +683,15 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
 // (the same rounding everywhere, so the diagonal stays in place) and written to s_out; the
 // scaled couplings a s_c s_n in float-float and their FP32 copies; the line factors as in
 // k_scale_mixed; and the first refinement sweep's residual r~ = s b with x~ = 0 (FP64), its
-// sums and test, as k_ir_residual<true>.  This replaces k_diag_rsqrt_sq, k_scale_mixed and the
-// first k_ir_residual: the diagonal, the couplings and b are read once.  The assembly wrote
+// sums and test, as k_ir_residual<true>, and the first inner right-hand side r~ 2^-e with its
+// inner CG state, as k_ir_scale, but scaled by a power of two from the previous solve's first
+// residual (so that the FP32 values and their squares stay far from the range limits; a power
+// of two changes no rounding, so the inner iterates are those of the unit-norm form up to
+// that factor).  When the scaled sum of squares leaves [2^-60, 2^60] (the first solve, a
+// jump in scale) the last block sets ir->rhs_rescale and the host runs k_ir_scale<true>
+// instead.
+// This replaces k_diag_rsqrt_sq, k_scale_mixed, the first k_ir_residual and k_ir_scale: the
+// diagonal, the couplings and b are read once.  The assembly wrote
 // the diagonal (dg) and the unscaled couplings (f0-f2) as floats; f0-f2 are overwritten in
 // place by the scaled FP32 copies, and the FP64 scaled couplings go to a0-a2.
 __device__ __forceinline__ float scale_of(float d) { return rsqrtf(d == 0.0f ? 1.0f : d); }
@@ -681,14 +699,16 @@ __device__ __forceinline__ float scale_of(float d) { return rsqrtf(d == 0.0f ? 1
 __global__ void __launch_bounds__(128) k_prep_ff(
     double* __restrict__ a0, double* __restrict__ a1, double* __restrict__ a2,
     const float* __restrict__ dg, const double* __restrict__ b, double* __restrict__ s_out,
-    double* __restrict__ rres, float* __restrict__ f0,
+    float* __restrict__ f0,
     float* __restrict__ f1, float* __restrict__ f2, float* __restrict__ lk,
     float* __restrict__ dinv, int n0, int n1, int n2, int line, CgDevState* ir,
-    double* partials, double ir_rtol) {
+    double* partials, double ir_rtol, float* __restrict__ rf, CgDevState* in, float sig,
+    double inner_rtol) {
   const int ncol = n0 * n1;
   const size_t sk = (size_t)ncol;
   const ff zero = ff_make(0.0f);
-  double v[3] = {0.0, 0.0, 0.0};
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  Kahan32 kq;
   for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
        col += gridDim.x * blockDim.x) {
     const int i0 = col % n0, i1 = col / n0;
@@ -740,15 +760,18 @@ __global__ void __launch_bounds__(128) k_prep_ff(
       }
       // first sweep: x~ = 0 (the first k_ir_update writes x~ without reading it), r~ = s b
       const double r = (double)sc * bc;
-      rres[c] = r;
+      const float q = ff_hi_of(r) * sig;
+      rf[c] = q;
+      kq.add(q * q);
       v[0] = fma(r, r, v[0]);
       v[2] = fma(bc, bc, v[2]);
       sc = sb;
     }
   }
   v[1] = v[2];  // with x~ = 0 the true residual is b
-  double tot[3];
-  if (!grid_sum<3>(v, partials, &ir->arrive[0], tot)) return;
+  v[3] = kq.value();
+  double tot[4];
+  if (!grid_sum<4>(v, partials, &ir->arrive[0], tot)) return;
   if (flat_tid() == 0) {
     const double rn = sqrt(tot[1]);
     ir->ir_bnorm = rn;
@@ -759,6 +782,21 @@ __global__ void __launch_bounds__(128) k_prep_ff(
       ir->status = kDivergedNanOrInf;
     } else if (rn <= fmax(ir_rtol * ir->ir_bnorm, ir->atol) || tot[0] == 0.0) {
       ir->status = rn < ir->atol ? kConvergedAtol : kConvergedRtol;
+    }
+    ir->rhs_rescale = 0;
+    if (ir->status == 0) {
+      if (tot[3] >= 0x1p-60 && tot[3] <= 0x1p60) {
+        ir->rscale = 1.0 / (double)sig;
+        in->beta = tot[3];
+        in->rnorm0 = sqrt(tot[3]);
+        in->ttol = inner_rtol * in->rnorm0;
+        in->iter = 0;
+        in->its = 0;
+        in->dpi = 0.0;
+        in->status = 0;
+      } else {
+        ir->rhs_rescale = 1;  // rescale: k_ir_scale<true> forms the right-hand side
+      }
     }
   }
 }
@@ -792,16 +830,27 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
       }
       // the refinement state, then one pass: scale factors, scaled operator, FP32 copy, line
       // factors and the first sweep's residual
-      CgDevState ir0;
+      CgDevState ir0, in0;
       memset(&ir0, 0, sizeof(ir0));
+      memset(&in0, 0, sizeof(in0));
       ir0.atol = cfg.atol;
+      in0.max_it = cfg.max_it;
       FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+      FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+      // the first inner right-hand side's scale: 2^-e with 2^(e-1) <= the previous solve's
+      // first residual norm < 2^e
+      float sig = 1.0f;
+      if (first_rnorm > 0.0 && std::isfinite(first_rnorm)) {
+        int e = 0;
+        std::frexp(first_rnorm, &e);
+        sig = std::ldexp(1.0f, -std::max(-120, std::min(120, e)));
+      }
       FG_LAUNCH(prof, st, "k_prep_ff",
-                (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 8.0 + (line ? 8.0 : 0.0)) * dn,
+                (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 4.0 + (line ? 8.0 : 0.0)) * dn,
                 k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, reinterpret_cast<const float*>(A.s),
-                                              A.b, r, rres, op32.a0, op32.a1, op32.a2, lkf,
-                                              dinvf, A.n0, A.n1, A.n2, line ? 1 : 0, dst,
-                                              partials, cfg.ir_rtol));
+                                              A.b, r, op32.a0, op32.a1, op32.a2, lkf, dinvf,
+                                              A.n0, A.n1, A.n2, line ? 1 : 0, dst, partials,
+                                              cfg.ir_rtol, rf, dst32, sig, cfg.inner_rtol));
       FG_CUDA(cudaGetLastError());
       A.scaled = true;
       A.s_in_r = true;
@@ -866,9 +915,10 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   // prep_mixed may have formed the first sweep's residual and its state already
   const bool first_done_here = first_done;
   first_done = false;
-  if (!first_done_here)
+  if (!first_done_here) {
     FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
-  FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
+  }
   // where the scale factors are: A.s, or r (as floats) after the float-float preparation
   const double* sv = A.s_in_r ? r : A.s;
 
@@ -952,17 +1002,26 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
                     A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                     L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol));
     }
-    // the first sweep's right-hand side (unit norm); later residual kernels write theirs
-    if (sweeps == 0)
+    // the first sweep's right-hand side (unit norm; k_prep_ff wrote it already); later
+    // residual kernels write theirs
+    if (sweeps == 0 && !first_done_here)
       FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
-                k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
-                                               cfg.inner_rtol));
+                k_ir_scale<false><<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
+                                                      cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());
     FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (prof && prof->on) FG_TRY(prof->flush());
+    if (sweeps == 0 && hst->a > 0.0 && std::isfinite(hst->a)) first_rnorm = hst->a;
     if (hst->status != 0) break;
     if (sweeps >= max_sweeps) break;
+    if (sweeps == 0 && first_done_here && hst->rhs_rescale) {
+      // k_prep_ff's power-of-two scale left the FP32 range margin: unit norm from s b
+      FG_LAUNCH(prof, st, "k_ir_scale", 20.0 * dn,
+                k_ir_scale<true><<<nb, 256, 0, st>>>(sv, rf, n, dst, dst32, partials,
+                                                     cfg.inner_rtol, A.b));
+      FG_CUDA(cudaGetLastError());
+    }
     // inner FP32 solve: flexible CG with the learned preconditioner, or Jacobi CG
     FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
