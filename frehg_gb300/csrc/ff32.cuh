@@ -145,10 +145,6 @@ __device__ __forceinline__ ff ff_from_double(double x) {
   return fast_two_sum(h, l);
 }
 
-// float-float -> double without an FP64 addition: the two significands are added as integers
-// (a.l shifted to the double's last place, truncated there), so the result is within an ulp of
-// the double nearest to a.h + a.l.  Zero, subnormal, infinite and NaN a.h take the conversion
-// instructions.
 // x rounded to a float (to nearest, ties away from zero) without a double->float conversion:
 // the significand's leading 24 bits plus the first dropped bit, added as an integer (a carry
 // moves into the exponent).  |x| below the normal float range gives a signed zero; huge, inf and
@@ -164,6 +160,10 @@ __device__ __forceinline__ float ff_hi_of(double x) {
                         (int)((lx >> 28) & 1u));
 }
 
+// float-float -> double without an FP64 addition: the two significands are added as integers
+// (a.l shifted to the double's last place, truncated there), so the result is within an ulp of
+// the double nearest to a.h + a.l.  Zero, subnormal, infinite and NaN a.h take the conversion
+// instructions.
 __device__ __forceinline__ double ff_to_double(ff a) {
   const int bh = __float_as_int(a.h);
   const int eh = (bh >> 23) & 0xff;
@@ -187,6 +187,58 @@ __device__ __forceinline__ double ff_to_double(ff a) {
   const unsigned long long bits = ((unsigned long long)((unsigned)bh & 0x80000000u) << 32) |
                                   ((unsigned long long)e << 52) | (M & ((1ull << 52) - 1));
   return __longlong_as_double((long long)bits);
+}
+
+static __device__ __noinline__ double f2d_scaled_rare(float f, int k) {
+  return ldexp((double)f, k);
+}
+
+// (double)f * 2^k exactly, without the FP64 pipe (GB300 converts float -> double there): the
+// float's exponent re-biased by 1023 - 127 + k, its significand moved to the top of the double's.
+// Zero gives a signed zero; subnormal, infinite and NaN f, and results outside the normal
+// double range, take the conversion instruction.
+__device__ __forceinline__ double f2d_scaled(float f, int k) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+  if ((b << 1) == 0u) return __longlong_as_double((long long)sign);
+  const int e = (int)((b >> 23) & 0xffu);
+  const int E = e + (1023 - 127) + k;
+  if (e == 0 || e == 0xff || E <= 0 || E >= 0x7ff) return f2d_scaled_rare(f, k);
+  return __longlong_as_double((long long)(sign | ((unsigned long long)E << 52) |
+                                          ((unsigned long long)(b & 0x007fffffu) << 29)));
+}
+
+// k with 2^(k-1) <= v < 2^k for a positive normal double v (0 otherwise), clamped to
+// [-120, 120] so that 2^-k is a normal float
+__device__ __host__ __forceinline__ int pow2_above(double v) {
+  union {
+    double d;
+    unsigned long long u;
+  } w;
+  w.d = v;
+  const unsigned long long b = w.u;
+  const int E = (int)((b >> 52) & 0x7ffu);
+  if ((b >> 63) || E == 0 || E == 0x7ff) return 0;
+  const int k = E - 1022;
+  return k < -120 ? -120 : (k > 120 ? 120 : k);
+}
+
+// 2^k as a double and as a float (|k| <= 120)
+__device__ __host__ __forceinline__ double pow2d(int k) {
+  union {
+    unsigned long long u;
+    double d;
+  } w;
+  w.u = (unsigned long long)(k + 1023) << 52;
+  return w.d;
+}
+__device__ __host__ __forceinline__ float pow2f_of(int k) {
+  union {
+    unsigned u;
+    float f;
+  } w;
+  w.u = (unsigned)(k + 127) << 23;
+  return w.f;
 }
 
 // a >= 1 (a normalised)

@@ -67,8 +67,10 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     // the sums of squares in FP32 (compensated), after scaling by the previous sweep's norms,
     // which keeps the terms far from the FP32 range limits: they only set the inner scale and
     // the stopping test, and the FP64 pipe stays with the stencil product
-    const double rs0 = ir->a, rs1 = ir->ir_rnorm;
-    const float sig0 = (float)(1.0 / rs0), sig1 = (float)(1.0 / rs1);
+    // the right-hand side's scale a power of two (2^(k-1) <= previous ||r~|| < 2^k)
+    const float sig0 = pow2f_of(-pow2_above(ir->a));
+    const double rs1 = ir->ir_rnorm;
+    const float sig1 = (float)(1.0 / rs1);
     Kahan32 k0, k1;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
       const int i0 = (tile % t0) * 32 + threadIdx.x;
@@ -105,7 +107,7 @@ __global__ void __launch_bounds__(256) k_ir_residual(
     ir->ir_rnorm = rn;
     ir->dp = rn;
     // ||r~||; later sweeps summed (r~ / rs0)^2, the FP32 right-hand side they wrote
-    const double rs0 = FIRST ? 1.0 : ir->a;
+    const double rs0 = FIRST ? 1.0 : pow2d(pow2_above(ir->a));
     ir->a = sqrt(tot[0]) * rs0;
     if (isnan(rn) || isinf(rn)) {
       ir->status = kDivergedNanOrInf;
@@ -126,15 +128,17 @@ __global__ void __launch_bounds__(256) k_ir_residual(
   }
 }
 
-// Inner right-hand side rf = fp32(r~ / ||r~||): unit norm, so FP32 products cannot underflow
-// however small the refinement residual is.  The last block initialises the inner CG state.
-// SB: r~ = s b is formed here from the scale factors and b (rres = s, sb = b) instead of read.
-template <bool SB = false>
+// Inner right-hand side rf = fp32(r~ 2^-k), 2^(k-1) <= ||r~|| < 2^k: norm in [1/2, 1), so FP32
+// products cannot underflow however small the refinement residual is.  The last block
+// initialises the inner CG state.
 __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ rf, size_t n,
                            CgDevState* ir, CgDevState* in, double* partials,
-                           double inner_rtol, const double* __restrict__ sb = nullptr) {
+                           double inner_rtol) {
   if (ir->status) return;
-  const float sig = (float)(1.0 / ir->a);
+  // 2^-k with 2^(k-1) <= ||r~|| < 2^k: the right-hand side's norm in [1/2, 1), and the scale
+  // a power of two (exact, and the refinement update forms rscale e without FP64 arithmetic)
+  const int k = pow2_above(ir->a);
+  const float sig = pow2f_of(-k);
   Kahan32 acc;
   // the FP32 right-hand side from the residual's leading 24 bits (integer split: GB300's
   // double->float conversion runs on the FP64 pipe); four cells per step, 16-byte accesses
@@ -142,16 +146,8 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   const double2* r2 = reinterpret_cast<const double2*>(rres);
   float4* f4 = reinterpret_cast<float4*>(rf);
-  const double2* b2 = reinterpret_cast<const double2*>(sb);
   for (size_t q = gid; q < n / 4; q += stride) {
-    double2 lo = r2[2 * q], hi = r2[2 * q + 1];
-    if (SB) {
-      const double2 blo = b2[2 * q], bhi = b2[2 * q + 1];
-      lo.x *= blo.x;
-      lo.y *= blo.y;
-      hi.x *= bhi.x;
-      hi.y *= bhi.y;
-    }
+    const double2 lo = r2[2 * q], hi = r2[2 * q + 1];
     const float4 v = make_float4(ff_hi_of(lo.x) * sig, ff_hi_of(lo.y) * sig,
                                  ff_hi_of(hi.x) * sig, ff_hi_of(hi.y) * sig);
     f4[q] = v;
@@ -161,7 +157,7 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
     acc.add(v.w * v.w);
   }
   for (size_t c = (n & ~(size_t)3) + gid; c < n; c += stride) {
-    const float r32 = ff_hi_of(SB ? rres[c] * sb[c] : rres[c]) * sig;
+    const float r32 = ff_hi_of(rres[c]) * sig;
     rf[c] = r32;
     acc.add(r32 * r32);
   }
@@ -169,7 +165,7 @@ __global__ void k_ir_scale(const double* __restrict__ rres, float* __restrict__ 
   double tot[1];
   if (!grid_sum<1>(loc, partials, &in->arrive[0], tot)) return;
   if (flat_tid() == 0) {
-    ir->rscale = ir->a;
+    ir->rscale = pow2d(k);
     in->beta = tot[0];
     in->rnorm0 = sqrt(tot[0]);
     in->ttol = inner_rtol * in->rnorm0;
@@ -456,9 +452,12 @@ __global__ void k32_update(float* __restrict__ e, float* __restrict__ r,
 // reading it, so e holds nothing before it: an inner solve that stopped before its first
 // iteration (in->iter == 0) contributes e = 0.  Four cells per step with 16-byte loads and
 // stores (the buffers are whole cudaMalloc allocations: 256-byte aligned).
+// rscale is a power of two 2^k: rscale e is formed by integer operations (f2d_scaled), which
+// leaves FIRST without FP64 instructions and the others with one addition per cell.
 template <bool FIRST>
-__device__ __forceinline__ double ir_step(double scale, float e, double x) {
-  return FIRST ? scale * (double)e : fma(scale, (double)e, x);
+__device__ __forceinline__ double ir_step(int k, float e, double x) {
+  const double v = f2d_scaled(e, k);
+  return FIRST ? v : x + v;
 }
 
 template <bool FIRST>
@@ -471,7 +470,13 @@ __global__ void k_ir_update(double* __restrict__ x, const float* __restrict__ e,
       for (size_t c = gid; c < n; c += stride) x[c] = 0.0;
     return;
   }
-  const double scale = ir->rscale;
+  const double rs = ir->rscale;
+  const int scale = pow2_above(rs) - 1;  // rscale = 2^scale
+  if (rs != pow2d(scale)) {  // not a power of two (no path sets one): FP64 arithmetic
+    for (size_t c = gid; c < n; c += stride)
+      x[c] = FIRST ? rs * (double)e[c] : fma(rs, (double)e[c], x[c]);
+    return;
+  }
   const float4* e4 = reinterpret_cast<const float4*>(e);
   double2* x2 = reinterpret_cast<double2*>(x);
   for (size_t q = gid; q < n / 4; q += stride) {
@@ -682,14 +687,14 @@ __global__ void __launch_bounds__(128) k_scale_mixed(double* __restrict__ a0,
 // iterate's fixed point), formed from the diagonal by each thread for itself and its neighbours
 // (the same rounding everywhere, so the diagonal stays in place) and written to s_out; the
 // scaled couplings a s_c s_n in float-float and their FP32 copies; the line factors as in
-// k_scale_mixed; and the first refinement sweep's residual r~ = s b with x~ = 0 (FP64), its
-// sums and test, as k_ir_residual<true>, and the first inner right-hand side r~ 2^-e with its
-// inner CG state, as k_ir_scale, but scaled by a power of two from the previous solve's first
-// residual (so that the FP32 values and their squares stay far from the range limits; a power
-// of two changes no rounding, so the inner iterates are those of the unit-norm form up to
-// that factor).  When the scaled sum of squares leaves [2^-60, 2^60] (the first solve, a
-// jump in scale) the last block sets ir->rhs_rescale and the host runs k_ir_scale<true>
-// instead.
+// k_scale_mixed; and the first refinement sweep (x~ = 0): the inner right-hand side
+// fp32(s b) 2^-e with its CG state (k_ir_scale's job) and the norms ||s b||, ||b|| and the
+// stopping test (k_ir_residual<true>'s), all in FP32 arithmetic: the scale 2^-e comes from the
+// previous solve's first residual, which keeps the scaled values and their squares far from
+// the FP32 range limits (a power of two changes no rounding).  When a scaled sum of squares
+// leaves [2^-60, 2^60] (the first solve, a jump in scale) the last block sets
+// ir->rhs_rescale and the host runs k_ir_residual<true> and k_ir_scale instead (FP64).  The
+// kernel has no FP64 arithmetic: GB300's FP64 pipe would bound it.
 // This replaces k_diag_rsqrt_sq, k_scale_mixed, the first k_ir_residual and k_ir_scale: the
 // diagonal, the couplings and b are read once.  The assembly wrote
 // the diagonal (dg) and the unscaled couplings (f0-f2) as floats; f0-f2 are overwritten in
@@ -702,13 +707,13 @@ __global__ void __launch_bounds__(128) k_prep_ff(
     float* __restrict__ f0,
     float* __restrict__ f1, float* __restrict__ f2, float* __restrict__ lk,
     float* __restrict__ dinv, int n0, int n1, int n2, int line, CgDevState* ir,
-    double* partials, double ir_rtol, float* __restrict__ rf, CgDevState* in, float sig,
+    double* partials, double ir_rtol, float* __restrict__ rf, CgDevState* in, int sig_exp,
     double inner_rtol) {
   const int ncol = n0 * n1;
   const size_t sk = (size_t)ncol;
   const ff zero = ff_make(0.0f);
-  double v[4] = {0.0, 0.0, 0.0, 0.0};
-  Kahan32 kq;
+  const float sig = pow2f_of(-sig_exp);
+  Kahan32 kq, kb;
   for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
        col += gridDim.x * blockDim.x) {
     const int i0 = col % n0, i1 = col / n0;
@@ -735,7 +740,7 @@ __global__ void __launch_bounds__(128) k_prep_ff(
         bq = b[cn];
       }
       const float sb = (k + 1 < n2) ? scale_of(ez) : 0.0f;
-      s_out[c] = (double)sc;
+      s_out[c] = f2d_scaled(sc, 0);
       ff v0 = zero, v1 = zero, v2 = zero;
       if (hx) v0 = scaled_coupling_f(e0, a0, c, sc, scale_of(ex));
       else a0[c] = 0.0;
@@ -758,45 +763,45 @@ __global__ void __launch_bounds__(128) k_prep_ff(
         dinv[c] = inv_d.h;
         aprev = v2;
       }
-      // first sweep: x~ = 0 (the first k_ir_update writes x~ without reading it), r~ = s b
-      const double r = (double)sc * bc;
-      const float q = ff_hi_of(r) * sig;
+      // first sweep: x~ = 0 (the first k_ir_update writes x~ without reading it), r~ = s b,
+      // kept only as its FP32 form r~ 2^-e (the inner right-hand side), with the sums of
+      // squares of r~ 2^-e and b 2^-e (with x~ = 0 the true residual is b) compensated in FP32
+      const float qb = ff_hi_of(bc) * sig;
+      const float q = sc * qb;
       rf[c] = q;
       kq.add(q * q);
-      v[0] = fma(r, r, v[0]);
-      v[2] = fma(bc, bc, v[2]);
+      kb.add(qb * qb);
       sc = sb;
     }
   }
-  v[1] = v[2];  // with x~ = 0 the true residual is b
-  v[3] = kq.value();
-  double tot[4];
-  if (!grid_sum<4>(v, partials, &ir->arrive[0], tot)) return;
+  double v[2] = {kq.value(), kb.value()};
+  double tot[2];
+  if (!grid_sum<2>(v, partials, &ir->arrive[0], tot)) return;
   if (flat_tid() == 0) {
-    const double rn = sqrt(tot[1]);
+    ir->rhs_rescale = 0;
+    if (!(tot[0] >= 0x1p-60 && tot[0] <= 0x1p60 && tot[1] >= 0x1p-60 && tot[1] <= 0x1p60)) {
+      // the scaled sums left the FP32 margin (or are 0, inf, NaN): the host recomputes this
+      // sweep's residual, norms and test in FP64 (k_ir_residual<true>, k_ir_scale)
+      ir->rhs_rescale = 1;
+      return;
+    }
+    const double inv_sig = pow2d(sig_exp);
+    const double rn = sqrt(tot[1]) * inv_sig;
     ir->ir_bnorm = rn;
     ir->ir_rnorm = rn;
     ir->dp = rn;
-    ir->a = sqrt(tot[0]);
-    if (isnan(rn) || isinf(rn)) {
-      ir->status = kDivergedNanOrInf;
-    } else if (rn <= fmax(ir_rtol * ir->ir_bnorm, ir->atol) || tot[0] == 0.0) {
+    ir->a = sqrt(tot[0]) * inv_sig;
+    if (rn <= fmax(ir_rtol * ir->ir_bnorm, ir->atol))
       ir->status = rn < ir->atol ? kConvergedAtol : kConvergedRtol;
-    }
-    ir->rhs_rescale = 0;
     if (ir->status == 0) {
-      if (tot[3] >= 0x1p-60 && tot[3] <= 0x1p60) {
-        ir->rscale = 1.0 / (double)sig;
-        in->beta = tot[3];
-        in->rnorm0 = sqrt(tot[3]);
-        in->ttol = inner_rtol * in->rnorm0;
-        in->iter = 0;
-        in->its = 0;
-        in->dpi = 0.0;
-        in->status = 0;
-      } else {
-        ir->rhs_rescale = 1;  // rescale: k_ir_scale<true> forms the right-hand side
-      }
+      ir->rscale = inv_sig;
+      in->beta = tot[0];
+      in->rnorm0 = sqrt(tot[0]);
+      in->ttol = inner_rtol * in->rnorm0;
+      in->iter = 0;
+      in->its = 0;
+      in->dpi = 0.0;
+      in->status = 0;
     }
   }
 }
@@ -839,18 +844,13 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
       FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
       // the first inner right-hand side's scale: 2^-e with 2^(e-1) <= the previous solve's
       // first residual norm < 2^e
-      float sig = 1.0f;
-      if (first_rnorm > 0.0 && std::isfinite(first_rnorm)) {
-        int e = 0;
-        std::frexp(first_rnorm, &e);
-        sig = std::ldexp(1.0f, -std::max(-120, std::min(120, e)));
-      }
+      const int sig_exp = pow2_above(first_rnorm);
       FG_LAUNCH(prof, st, "k_prep_ff",
                 (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 4.0 + (line ? 8.0 : 0.0)) * dn,
                 k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, reinterpret_cast<const float*>(A.s),
                                               A.b, r, op32.a0, op32.a1, op32.a2, lkf, dinvf,
                                               A.n0, A.n1, A.n2, line ? 1 : 0, dst, partials,
-                                              cfg.ir_rtol, rf, dst32, sig, cfg.inner_rtol));
+                                              cfg.ir_rtol, rf, dst32, sig_exp, cfg.inner_rtol));
       FG_CUDA(cudaGetLastError());
       A.scaled = true;
       A.s_in_r = true;
@@ -1006,22 +1006,29 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     // residual kernels write theirs
     if (sweeps == 0 && !first_done_here)
       FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
-                k_ir_scale<false><<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
-                                                      cfg.inner_rtol));
+                k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
+                                               cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());
     FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (prof && prof->on) FG_TRY(prof->flush());
+    if (sweeps == 0 && first_done_here && hst->rhs_rescale) {
+      // k_prep_ff's scale left the FP32 margin: this sweep's residual, norms and test in FP64
+      FG_LAUNCH(prof, st, "k_ir_residual0", 24.0 * dn,
+                k_ir_residual<true><<<L.grid, L.block, 0, st>>>(
+                    A.a0, A.a1, A.a2, sv, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
+                    L.tiles, dst, partials, cfg.ir_rtol));
+      FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
+                k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
+                                               cfg.inner_rtol));
+      FG_CUDA(cudaGetLastError());
+      FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaStreamSynchronize(st));
+      if (prof && prof->on) FG_TRY(prof->flush());
+    }
     if (sweeps == 0 && hst->a > 0.0 && std::isfinite(hst->a)) first_rnorm = hst->a;
     if (hst->status != 0) break;
     if (sweeps >= max_sweeps) break;
-    if (sweeps == 0 && first_done_here && hst->rhs_rescale) {
-      // k_prep_ff's power-of-two scale left the FP32 range margin: unit norm from s b
-      FG_LAUNCH(prof, st, "k_ir_scale", 20.0 * dn,
-                k_ir_scale<true><<<nb, 256, 0, st>>>(sv, rf, n, dst, dst32, partials,
-                                                     cfg.inner_rtol, A.b));
-      FG_CUDA(cudaGetLastError());
-    }
     // inner FP32 solve: flexible CG with the learned preconditioner, or Jacobi CG
     FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
