@@ -214,6 +214,7 @@ class KrylovSolver {
   // scaling of the operator for the mixed path (sq = D^1/2 into r, FP32 copy, line factors)
   int prep_mixed(Stencil64& A, cudaStream_t st, bool line, const frehg_solver_config& cfg);
   bool first_done = false;  // prep_mixed formed the first refinement residual and its state
+  bool first_line_done = false;  // ... and the line preconditioner's first application
   double first_rnorm = 0.0;  // the last solve's first residual norm (scale of the next one's)
   size_t cap_line = 0;
   float *lkf = nullptr, *dinvf = nullptr, *uf = nullptr;

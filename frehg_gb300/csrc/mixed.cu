@@ -25,6 +25,14 @@
 
 namespace fg {
 
+// The inner state after the line preconditioner's first application, z0 = M^-1 r0, as
+// k32_line_fwd<false> leaves it: beta = r0 . z0, no direction yet.
+__device__ __forceinline__ void line_first_state(CgDevState* in, double rz) {
+  in->beta = rz;
+  in->bcoef = 0.0;
+  if (!(rz > 0.0)) in->status = rz == 0.0 ? kConvergedAtol : kDivergedIndefinitePc;
+}
+
 // r~ = s b - A~ x~ (FP64); sums of r~^2 (scale of the inner system),
 // (r~/s)^2 = (sq r~)^2 for the true residual (sq = 1/s) and b^2 for ||b||.  The last block
 // runs the refinement test.  The inner solution e needs no zeroing: the inner solve's first
@@ -36,6 +44,9 @@ namespace fg {
 // difference of nearly equal terms, and the refinement converges only as far as this product
 // is accurate (a float-float form, 2^-48, was both slower here and short of 1e-12 on
 // ill-conditioned systems).
+// (Applying the line preconditioner to the new right-hand side in the same column march, as
+// k_prep_ff does for the first sweep, made this kernel slower by more than the separate
+// k32_line_fwd<false> takes.)
 template <bool FIRST, bool INV_S = false>
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
@@ -708,17 +719,18 @@ __global__ void __launch_bounds__(128) k_prep_ff(
     float* __restrict__ f1, float* __restrict__ f2, float* __restrict__ lk,
     float* __restrict__ dinv, int n0, int n1, int n2, int line, CgDevState* ir,
     double* partials, double ir_rtol, float* __restrict__ rf, CgDevState* in, int sig_exp,
-    double inner_rtol) {
+    double inner_rtol, float* __restrict__ u) {
   const int ncol = n0 * n1;
   const size_t sk = (size_t)ncol;
   const ff zero = ff_make(0.0f);
   const float sig = pow2f_of(-sig_exp);
-  Kahan32 kq, kb;
+  Kahan32 kq, kb, kz;
   for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
        col += gridDim.x * blockDim.x) {
     const int i0 = col % n0, i1 = col / n0;
     const bool hx = i0 + 1 < n0, hy = i1 + 1 < n1;
     ff inv_d = ff_make(1.0f), aprev = zero;
+    float y = 0.0f;  // u != nullptr: forward substitution of the first right-hand side
     size_t c = (size_t)col;
     // level k's inputs are loaded one level ahead (two levels of loads in flight per thread)
     float sc = scale_of(dg[c]);
@@ -751,8 +763,8 @@ __global__ void __launch_bounds__(128) k_prep_ff(
       f0[c] = v0.h;
       f1[c] = v1.h;
       f2[c] = v2.h;
+      ff l = zero;
       if (line) {
-        ff l = zero;
         if (k > 0) {
           l = ff_mul(aprev, inv_d);
           ff d = ff_add_f(ff_neg(ff_mul(l, aprev)), 1.0f);
@@ -771,12 +783,18 @@ __global__ void __launch_bounds__(128) k_prep_ff(
       rf[c] = q;
       kq.add(q * q);
       kb.add(qb * qb);
+      if (u) {  // the line preconditioner's first application (k32_line_fwd<false>)
+        y = fmaf(-l.h, y, q);
+        const float uk = y * inv_d.h;
+        u[c] = uk;
+        kz.add(y * uk);
+      }
       sc = sb;
     }
   }
-  double v[2] = {kq.value(), kb.value()};
-  double tot[2];
-  if (!grid_sum<2>(v, partials, &ir->arrive[0], tot)) return;
+  double v[3] = {kq.value(), kb.value(), kz.value()};
+  double tot[3];
+  if (!grid_sum<3>(v, partials, &ir->arrive[0], tot)) return;
   if (flat_tid() == 0) {
     ir->rhs_rescale = 0;
     if (!(tot[0] >= 0x1p-60 && tot[0] <= 0x1p60 && tot[1] >= 0x1p-60 && tot[1] <= 0x1p60)) {
@@ -802,6 +820,7 @@ __global__ void __launch_bounds__(128) k_prep_ff(
       in->its = 0;
       in->dpi = 0.0;
       in->status = 0;
+      if (u) line_first_state(in, tot[2]);
     }
   }
 }
@@ -823,6 +842,7 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
   const int ncol = A.n0 * A.n1;
   const int lb = (int)std::min<long>((ncol + 127) / 128, kMaxRedBlocks);
   first_done = false;
+  first_line_done = false;
   if (A.f32_entries && (A.scaled || !ff_operator)) {
     set_error("FP32-form operator outside the float-float preparation");
     return FREHG_ERR_STATE;
@@ -845,13 +865,17 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
       // the first inner right-hand side's scale: 2^-e with 2^(e-1) <= the previous solve's
       // first residual norm < 2^e
       const int sig_exp = pow2_above(first_rnorm);
+      // the line preconditioner's first application as well, unless the network runs
+      const bool first_line = line && net.net == nullptr;
       FG_LAUNCH(prof, st, "k_prep_ff",
                 (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 4.0 + (line ? 8.0 : 0.0)) * dn,
                 k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, reinterpret_cast<const float*>(A.s),
                                               A.b, r, op32.a0, op32.a1, op32.a2, lkf, dinvf,
                                               A.n0, A.n1, A.n2, line ? 1 : 0, dst, partials,
-                                              cfg.ir_rtol, rf, dst32, sig_exp, cfg.inner_rtol));
+                                              cfg.ir_rtol, rf, dst32, sig_exp, cfg.inner_rtol,
+                                              first_line ? uf : nullptr));
       FG_CUDA(cudaGetLastError());
+      first_line_done = first_line;
       A.scaled = true;
       A.s_in_r = true;
       A.f32_entries = false;
@@ -912,9 +936,12 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   memset(&in0, 0, sizeof(in0));
   ir0.atol = cfg.atol;
   in0.max_it = cfg.max_it;
-  // prep_mixed may have formed the first sweep's residual and its state already
+  // prep_mixed may have formed the first sweep's residual and its state already, and the
+  // line preconditioner's first application to it
   const bool first_done_here = first_done;
+  const bool first_line_here = first_line_done;
   first_done = false;
+  first_line_done = false;
   if (!first_done_here) {
     FG_CUDA(cudaMemcpyAsync(dst, &ir0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
     FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
@@ -985,12 +1012,17 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
   bool fcg_fallback = false;
   const bool dbg = getenv("FREHG_DEBUG_IR") != nullptr;
   for (;;) {
+    // whether this sweep's right-hand side producer also applied the line preconditioner
+    // once (k32_line_fwd<false>): k_prep_ff does in the first sweep
+    bool fwd0_done = false;
     if (sweeps == 0) {
       if (!first_done_here)
         FG_LAUNCH(prof, st, "k_ir_residual0", 24.0 * dn,
                   k_ir_residual<true><<<L.grid, L.block, 0, st>>>(
                       A.a0, A.a1, A.a2, sv, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                       L.tiles, dst, partials, cfg.ir_rtol));
+      else
+        fwd0_done = first_line_here;
     } else if (A.s_in_r) {
       FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
                 (k_ir_residual<false, true><<<L.grid, L.block, 0, st>>>(
@@ -1014,6 +1046,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     if (prof && prof->on) FG_TRY(prof->flush());
     if (sweeps == 0 && first_done_here && hst->rhs_rescale) {
       // k_prep_ff's scale left the FP32 margin: this sweep's residual, norms and test in FP64
+      fwd0_done = false;
       FG_LAUNCH(prof, st, "k_ir_residual0", 24.0 * dn,
                 k_ir_residual<true><<<L.grid, L.block, 0, st>>>(
                     A.a0, A.a1, A.a2, sv, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
@@ -1073,10 +1106,11 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       if (prof && prof->on) FG_TRY(prof->flush());
     }
     if (!use_net && line) {
-      // z0 = M^-1 r0, r0.z0 and p0 = z0
-      FG_LAUNCH(prof, st, "k32_line_fwd0", 16.0 * dn,
-                (k32_line_fwd<false><<<lb, 128, 0, st>>>(xf, rf, pf, wf, lkf, dinvf, uf, ncol,
-                                                         nzl, dst32, partials)));
+      // z0 = M^-1 r0, r0.z0 (unless the right-hand side's producer formed them) and p0 = z0
+      if (!fwd0_done)
+        FG_LAUNCH(prof, st, "k32_line_fwd0", 16.0 * dn,
+                  (k32_line_fwd<false><<<lb, 128, 0, st>>>(xf, rf, pf, wf, lkf, dinvf, uf, ncol,
+                                                           nzl, dst32, partials)));
       FG_LAUNCH(prof, st, "k32_line_bwd", 12.0 * dn,
                 k32_line_bwd<<<lb, 128, 0, st>>>(uf, lkf, pf, ncol, nzl, dst32));
       FG_CUDA(cudaGetLastError());
