@@ -215,7 +215,11 @@ class KrylovSolver {
   int prep_mixed(Stencil64& A, cudaStream_t st, bool line, const frehg_solver_config& cfg);
   bool first_done = false;  // prep_mixed formed the first refinement residual and its state
   bool first_line_done = false;  // ... and the line preconditioner's first application
-  double first_rnorm = 0.0;  // the last solve's first residual norm (scale of the next one's)
+  // first residual norms of earlier solves, the scale of the next one's: slot 0 for the first
+  // solve of a time step (its residual is orders of magnitude above the previous step's last
+  // one), slot 1 for the later (Picard) solves; the caller picks the slot
+  double first_rnorm[2] = {0.0, 0.0};
+  int rnorm_slot = 1;
   size_t cap_line = 0;
   float *lkf = nullptr, *dinvf = nullptr, *uf = nullptr;
   int g32_line = 0;

@@ -864,7 +864,7 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
       FG_CUDA(cudaMemcpyAsync(dst32, &in0, sizeof(CgDevState), cudaMemcpyHostToDevice, st));
       // the first inner right-hand side's scale: 2^-e with 2^(e-1) <= the previous solve's
       // first residual norm < 2^e
-      const int sig_exp = pow2_above(first_rnorm);
+      const int sig_exp = pow2_above(first_rnorm[rnorm_slot & 1]);
       // the line preconditioner's first application as well, unless the network runs
       const bool first_line = line && net.net == nullptr;
       FG_LAUNCH(prof, st, "k_prep_ff",
@@ -1059,7 +1059,8 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       FG_CUDA(cudaStreamSynchronize(st));
       if (prof && prof->on) FG_TRY(prof->flush());
     }
-    if (sweeps == 0 && hst->a > 0.0 && std::isfinite(hst->a)) first_rnorm = hst->a;
+    if (sweeps == 0 && hst->a > 0.0 && std::isfinite(hst->a))
+      first_rnorm[rnorm_slot & 1] = hst->a;
     if (hst->status != 0) break;
     if (sweeps >= max_sweeps) break;
     // inner FP32 solve: flexible CG with the learned preconditioner, or Jacobi CG

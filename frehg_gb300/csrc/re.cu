@@ -673,8 +673,10 @@ static int picard_step(frehg_re* re) {
       FG_CUDA(cudaGetLastError());
       CgResult res;
       re->ksp.keep_scaled = true;  // the update below applies x = s x~
+      re->ksp.rnorm_slot = its == 0 ? 0 : 1;
       const int rc = solve_system(re, re->scratch, &res);
       re->ksp.keep_scaled = false;
+      re->ksp.rnorm_slot = 1;
       re->cnt.last_ksp_iterations = res.its;
       re->cnt.last_residual_norm = res.rnorm;
       re->cnt.ksp_iterations += res.its;
