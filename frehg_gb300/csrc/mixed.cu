@@ -868,7 +868,8 @@ int KrylovSolver::prep_mixed(Stencil64& A, cudaStream_t st, bool line,
       // the line preconditioner's first application as well, unless the network runs
       const bool first_line = line && net.net == nullptr;
       FG_LAUNCH(prof, st, "k_prep_ff",
-                (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 4.0 + (line ? 8.0 : 0.0)) * dn,
+                (4.0 + 12.0 + 8.0 + 24.0 + 12.0 + 8.0 + 4.0 + (line ? 8.0 : 0.0) +
+                 (first_line ? 4.0 : 0.0)) * dn,
                 k_prep_ff<<<lb, 128, 0, st>>>(A.a0, A.a1, A.a2, reinterpret_cast<const float*>(A.s),
                                               A.b, r, op32.a0, op32.a1, op32.a2, lkf, dinvf,
                                               A.n0, A.n1, A.n2, line ? 1 : 0, dst, partials,
@@ -1024,12 +1025,12 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       else
         fwd0_done = first_line_here;
     } else if (A.s_in_r) {
-      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
+      FG_LAUNCH(prof, st, "k_ir_residual", 52.0 * dn,
                 (k_ir_residual<false, true><<<L.grid, L.block, 0, st>>>(
                     A.a0, A.a1, A.a2, sv, sv, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                     L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol)));
     } else {
-      FG_LAUNCH(prof, st, "k_ir_residual", 60.0 * dn,
+      FG_LAUNCH(prof, st, "k_ir_residual", 52.0 * dn,
                 k_ir_residual<false><<<L.grid, L.block, 0, st>>>(
                     A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                     L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol));
