@@ -5,9 +5,10 @@
 // b~ = D^-1/2 b); its couplings are rounded once to FP32.  Each refinement sweep
 //   1. forms the true residual r~ = b~ - A~ x~ in FP64 (FP64 couplings) and its unscaled norm
 //      ||b - A x|| = ||r~ / s||; stops when ||b - A x|| <= ir_rtol * ||b||;
-//   2. solves A~32 e = fp32(r~) with FP32 CG to a relative reduction inner_rtol (dot products
-//      in FP32 with Kahan compensation per thread, combined in FP64 across threads/blocks);
-//   3. updates x~ += e in FP64.
+//   2. solves A~32 e = fp32(r~ 2^-k) with FP32 CG to a relative reduction inner_rtol (dot
+//      products in FP32 with Kahan compensation per thread, combined in FP64 across
+//      threads/blocks; 2^-k, a power of two near 1/||r~||, keeps FP32 away from underflow);
+//   3. updates x~ += 2^k e in FP64.
 // The FP32 inner iteration moves 56 B/cell (vs 120 B/cell in FP64) and leaves the FP64 pipe,
 // the limiter of the FP64 path on GB300, idle.  Convergence is always to the FP64 true
 // residual, so the inner precision changes the iteration count, not the accuracy.
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(256) k_ir_residual(
         // sq r~ = r~ / s (INV_S: s holds floats and sq is not stored)
         const float sqc = INV_S ? __frcp_rn(ff_hi_of(s[c])) : ff_hi_of(sq[c]);
         const float q0 = rf * sig0, q1 = rf * sqc * sig1;
-        rfo[c] = q0;  // the next inner solve's right-hand side, r~ / rs0
+        rfo[c] = q0;  // the next inner solve's right-hand side, r~ / rs0 (rs0 = 2^k)
         k0.add(q0 * q0);
         k1.add(q1 * q1);
       }
@@ -1035,7 +1036,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
                     A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
                     L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol));
     }
-    // the first sweep's right-hand side (unit norm; k_prep_ff wrote it already); later
+    // the first sweep's right-hand side (norm in [1/2, 1); k_prep_ff wrote it already); later
     // residual kernels write theirs
     if (sweeps == 0 && !first_done_here)
       FG_LAUNCH(prof, st, "k_ir_scale", 12.0 * dn,
