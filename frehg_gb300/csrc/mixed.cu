@@ -569,12 +569,6 @@ __global__ void k_add_f32(float* __restrict__ z, const float* __restrict__ r, si
     z[c] += r[c];
 }
 
-__global__ void k_cast_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
-       c += (size_t)gridDim.x * blockDim.x)
-    b[c] = (float)a[c];
-}
-
 // ------------------------------------------------------------------------------------------
 
 int KrylovSolver::ensure32(size_t n) {
