@@ -52,7 +52,7 @@ class Workload:
     def apply(self, s):
         """Configure a solver (GPU ReSolver or oracle) following the reference call order."""
         if self.classes is not None:
-            if hasattr(s, "set_soil_map") and s.__class__.__name__ == "OracleRe":
+            if hasattr(s, "set_soil_map") and s.__class__.__name__ in ("OracleRe", "RefRe"):
                 s.set_soil_map(self.classes, self.class_index, self.class3d)
             else:
                 from .re_solver import SoilMap

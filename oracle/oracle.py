@@ -27,7 +27,7 @@ def build(force: bool = False) -> str:
         t = os.path.getmtime(LIB_PATH)
         if all(os.path.getmtime(d) <= t for d in DEPS):
             return LIB_PATH
-    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-Wall", "-o", LIB_PATH] + SOURCES + ["-lm"]
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall", "-o", LIB_PATH] + SOURCES + ["-lm"]
     subprocess.run(cmd, check=True)
     return LIB_PATH
 
