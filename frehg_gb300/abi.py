@@ -21,6 +21,8 @@ FREHG_ERR_NONFINITE = 4
 FREHG_ERR_STATE = 5
 FREHG_ERR_UNSUPPORTED = 6
 FREHG_ERR_NO_DEVICE = 7
+# doubles of a checkpoint's state block (frehg_re_checkpoint, include/frehg_gb300.h)
+CHECKPOINT_SCALARS = 10
 
 STATUS_NAMES = {
     0: "FREHG_OK",

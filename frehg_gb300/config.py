@@ -333,11 +333,10 @@ def solver_config(cfg):
     prec = opts.get("precision", "fp64")
     if prec not in ("fp64", "mixed"):
         raise ConfigError(f"precision '{prec}' (fp64, mixed)")
-    # The reference's default pc_type is "sor" (PETSc PCSOR, a sequential lexicographic sweep).
-    # This backend has no SOR; an unset pc_type therefore means Jacobi here, and an explicit
-    # "sor" is passed through so that attachSolver rejects it loudly.
+    # An unset pc_type is "sor" (PETSc PCSOR, local symmetric sweep), the reference's
+    # groundwater default (Orchestrator.cpp:489); the GPU realises it in FP64.
     return SolverConfig(ksp_type=str(opts.get("ksp_type", "cg")),
-                        pc_type=str(opts.get("pc_type", "jacobi")),
+                        pc_type=str(opts.get("pc_type", "sor")),
                         rtol=float(opts.get("rtol", 1e-10)),
                         atol=float(opts.get("atol", 1e-50)),
                         max_it=int(opts.get("max_it", 10000)),

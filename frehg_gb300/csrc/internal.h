@@ -105,6 +105,10 @@ struct Stencil64 {
   // and the couplings (unscaled, as floats) into the mixed solver's FP32 operator; only the
   // float-float preparation (k_prep_ff) reads this form
   bool f32_entries = false;
+  // axes from the slowest to the fastest of the reference's row order (Decomp3D: j, i, k);
+  // PCSOR subtracts its neighbour terms in that order.  RE handles store (i, j, k) as axes
+  // (0, 1, 2), the linear seam stores owned order (k, i, j)
+  int ref_order[3] = {1, 0, 2};
   int alloc(int n0, int n1, int n2);
   void release();
 };
@@ -222,6 +226,15 @@ class KrylovSolver {
   int rnorm_slot = 1;
   size_t cap_line = 0;
   float *lkf = nullptr, *dinvf = nullptr, *uf = nullptr;
+  // PCSOR (pc_type "sor", precision 0): 1/d, the preconditioned residual, iteration graph
+  int ensure_sor(size_t n);
+  size_t cap_sor = 0;
+  double *invd = nullptr, *zs = nullptr;
+  cudaGraphExec_t gsor = nullptr;
+  const void* gsor_key = nullptr;
+  const void* gsor_key2 = nullptr;
+  cudaStream_t gsor_stream = nullptr;
+  size_t gsor_n = 0;
   int g32_line = 0;
   const void* g32_key = nullptr;
   cudaStream_t g_stream = nullptr;
@@ -232,6 +245,9 @@ class KrylovSolver {
               CgResult* res);
   int solve_mixed(Stencil64& A, double* x_out, const frehg_solver_config& cfg, cudaStream_t st,
                   CgResult* res);
+  // CG + PCSOR on the unscaled operator; the solution is left in x and copied to x_out
+  int solve_sor(Stencil64& A, double* x_out, const frehg_solver_config& cfg, cudaStream_t st,
+                CgResult* res);
   int run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk);
   int finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResult* res, int nb);
 };

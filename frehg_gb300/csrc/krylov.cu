@@ -44,12 +44,9 @@ StencilLaunch stencil_launch(int n0, int n1, int n2) {
   L.block = dim3(32, 8, 1);
   const int t0 = (n0 + 31) / 32, t1 = (n1 + 7) / 8;
   const long tiles = (long)t0 * t1;
-  static const long waves = [] {
-    const char* e = getenv("FREHG_STENCIL_WAVES");
-    const long v = e ? atol(e) : 2;
-    return v < 1 ? 1L : v;
-  }();
-  const long target = (long)kNumSMs * 8 * waves;
+  // about two waves of 8 resident (32 x 8)-thread blocks per SM; the launch shape, and with
+  // it the summation tree of the reductions, depends on the grid sizes only
+  const long target = (long)kNumSMs * 8 * 2;
   long z = target / (tiles > 0 ? tiles : 1);
   if (z < 1) z = 1;
   if (z > n2) z = n2;
@@ -357,6 +354,9 @@ KrylovSolver::~KrylovSolver() {
   if (g64) cudaGraphExecDestroy(g64);
   if (g32) cudaGraphExecDestroy(g32);
   if (g32s) cudaGraphExecDestroy(g32s);
+  if (gsor) cudaGraphExecDestroy(gsor);
+  cudaFree(invd);
+  cudaFree(zs);
   cudaFree(x);
   cudaFree(r);
   cudaFree(p);
@@ -443,6 +443,17 @@ int KrylovSolver::run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int
 int KrylovSolver::solve(Stencil64& A, double* x_out, const frehg_solver_config& cfg,
                         cudaStream_t st, CgResult* res) {
   FG_TRY(ensure(A.n));
+  if (!strcmp(cfg.pc_type, "sor")) {
+    if (cfg.precision != 0) {
+      set_error("pc_type 'sor' runs in FP64 (precision 0)");
+      return FREHG_ERR_UNSUPPORTED;
+    }
+    if (keep_scaled) {
+      set_error("pc_type 'sor' returns the unscaled solution");
+      return FREHG_ERR_STATE;
+    }
+    return solve_sor(A, x_out, cfg, st, res);
+  }
   if (cfg.precision == 1) {
     FG_TRY(prep_mixed(A, st, !strcmp(cfg.pc_type, "line"), cfg));
     return solve_mixed(A, x_out, cfg, st, res);

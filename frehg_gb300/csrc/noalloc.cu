@@ -13,9 +13,12 @@
 //  * Size limit: at most kNoAllocMaxCells unknowns.  Larger systems are refused with
 //    FREHG_ERR_BAD_ARG; use frehg_cg_solve for them.
 //  * The array exists once per GPU that loads this library and stays reserved until the
-//    process exits (8 x kNoAllocMaxCells doubles + reduction slots: about 16.1 MB).
-//  * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
-//    with that device current; make that first call before any stream capture on the device.
+//    process exits: 8 x kNoAllocMaxCells doubles + 2 x 32,768 reduction slots + the scalar
+//    state = 17,302,016 bytes (about 17.3 MB, 16.5 MiB).
+//  * Every call looks up the array's device address (cudaGetSymbolAddress, which allocates
+//    nothing) on the device that is current, so the address stays right after a device reset
+//    reloads the module.  The first call on a device loads the module there; make that first
+//    call before any stream capture on the device.
 //  * Every call on a device shares the one array and overwrites what the previous call left
 //    there; the scalar state is reset at the start of each call.  Calls that overlap on the GPU
 //    (two streams, or two host threads on one device) race on the array and corrupt each
@@ -25,7 +28,6 @@
 #include "krylov_kernels.cuh"
 
 #include <cstring>
-#include <mutex>
 
 namespace {
 
@@ -38,30 +40,19 @@ static_assert(sizeof(fg::CgDevState) <= kStateDoubles * sizeof(double), "state s
 // the work space: s, a0, a1, a2 (scaled operator copy), x~, r, p, w, partials, state
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_addr[kMaxDevices] = {nullptr};
-
-// Device address of the work space on the current device (looked up once per device).
+// Device address of the work space on the current device.  In host code the array's name is
+// only a host-side stand-in; kernels must be given this address.
 int scratch_address(double** out) {
   int dev = -1;
   FG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    fg::set_error("frehg_cg_solve_noalloc: device ordinal %d outside [0,%d)", dev, kMaxDevices);
-    return FREHG_ERR_BAD_ARG;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    fg::set_error("frehg_cg_solve_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
+                  cudaGetErrorString(e));
+    return FREHG_ERR_CUDA;
   }
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      fg::set_error("frehg_cg_solve_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
-                    cudaGetErrorString(e));
-      return FREHG_ERR_CUDA;
-    }
-    g_addr[dev] = static_cast<double*>(p);
-  }
-  *out = g_addr[dev];
+  *out = static_cast<double*>(p);
   return FREHG_OK;
 }
 

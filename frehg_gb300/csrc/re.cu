@@ -672,7 +672,9 @@ static int picard_step(frehg_re* re) {
                       a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b, PL.planes, PL.tiles));
       FG_CUDA(cudaGetLastError());
       CgResult res;
-      re->ksp.keep_scaled = true;  // the update below applies x = s x~
+      // the update below applies x = s x~ (PCSOR solves the unscaled system into scratch)
+      const bool sor = !strcmp(re->cfg.pc_type, "sor");
+      re->ksp.keep_scaled = !sor;
       re->ksp.rnorm_slot = its == 0 ? 0 : 1;
       const int rc = solve_system(re, re->scratch, &res);
       re->ksp.keep_scaled = false;
@@ -685,9 +687,13 @@ static int picard_step(frehg_re* re) {
         fail = rc;
         break;
       }
-      FG_LAUNCH(prof, st, "k_pic_update", 32.0 * n,
-                k_pic_update<true><<<nb, 256, 0, st>>>(a, re->ksp.x,
-                                                       re->ksp.scale_vector(re->A)));
+      if (sor)
+        FG_LAUNCH(prof, st, "k_pic_update", 24.0 * n,
+                  k_pic_update<false><<<nb, 256, 0, st>>>(a, re->scratch));
+      else
+        FG_LAUNCH(prof, st, "k_pic_update", 32.0 * n,
+                  k_pic_update<true><<<nb, 256, 0, st>>>(a, re->ksp.x,
+                                                         re->ksp.scale_vector(re->A)));
       FG_CUDA(cudaGetLastError());
       FG_CUDA(cudaMemcpyAsync(&re->sc_host->dq_max, &re->sc->dq_max, sizeof(double),
                               cudaMemcpyDeviceToHost, st));
@@ -930,12 +936,16 @@ int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg) {
     set_error("ksp_type '%s' is not available (cg, fcg)", cfg->ksp_type);
     return FREHG_ERR_UNSUPPORTED;
   }
-  const char* pcs[] = {"jacobi", "line", "unet", "unet-line"};
+  const char* pcs[] = {"jacobi", "sor", "line", "unet", "unet-line"};
   bool known = false;
   for (const char* q : pcs) known = known || !strcmp(cfg->pc_type, q);
   if (!known) {
-    set_error("pc_type '%s' is not available on the GPU path (jacobi, line, unet, unet-line)",
-              cfg->pc_type);
+    set_error("pc_type '%s' is not available on the GPU path (jacobi, sor, line, unet, "
+              "unet-line)", cfg->pc_type);
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  if (!strcmp(cfg->pc_type, "sor") && cfg->precision != 0) {
+    set_error("pc_type 'sor' runs in FP64 (precision 0)");
     return FREHG_ERR_UNSUPPORTED;
   }
   FG_ARG(cfg->rtol > 0 && cfg->max_it > 0, "rtol and max_it must be positive");
@@ -1003,6 +1013,9 @@ int frehg_re_finalize_initial_state(frehg_re* re) {
   FG_CUDA(cudaMemcpy(re->sc, re->sc_host, sizeof(ReScalars), cudaMemcpyHostToDevice));
   re->ghosts_valid = false;
   re->top_ghost_stale = false;
+  // the refinement's right-hand-side scales carried from solve to solve start afresh
+  re->ksp.first_rnorm[0] = re->ksp.first_rnorm[1] = 0.0;
+  re->ksp.first_done = false;
   re->finalized = true;
   return FREHG_OK;
 }
@@ -1134,6 +1147,11 @@ int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state) {
   clear_error();
   FG_ARG(re && h && wc && state, "null argument");
   FG_ARG(re->finalized, "checkpoint of a handle without a finalized state");
+  if (re->top_ghost_stale) {
+    set_error("checkpoint between a surface exchange and the next step: the top layer's "
+              "pre-exchange ghost copies are not part of the state");
+    return FREHG_ERR_STATE;
+  }
   FG_CUDA(cudaStreamSynchronize(re->stream));
   FG_CUDA(cudaMemcpy(h, re->H[re->cur], re->n * sizeof(double), cudaMemcpyDeviceToHost));
   FG_CUDA(cudaMemcpy(wc, re->W[re->cur], re->n * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1141,7 +1159,8 @@ int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state) {
   const ReScalars& s = *re->sc_host;
   const double v[FREHG_CHECKPOINT_SCALARS] = {s.time,    s.dt,      s.dtn,
                                               s.dt_used, s.vol_top, s.vol_bot,
-                                              s.vol_elastic, re->ghosts_valid ? 1.0 : 0.0};
+                                              s.vol_elastic, re->ghosts_valid ? 1.0 : 0.0,
+                                              re->ksp.first_rnorm[0], re->ksp.first_rnorm[1]};
   memcpy(state, v, sizeof(v));
   return FREHG_OK;
 }
@@ -1165,6 +1184,9 @@ int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const doub
   FG_CUDA(cudaMemcpy(re->sc, re->sc_host, sizeof(ReScalars), cudaMemcpyHostToDevice));
   re->p.dt = state[1];
   re->ghosts_valid = state[7] != 0.0;
+  re->ksp.first_rnorm[0] = state[8];
+  re->ksp.first_rnorm[1] = state[9];
+  re->ksp.first_done = false;
   re->top_ghost_stale = false;
   re->have_state = true;
   re->finalized = true;

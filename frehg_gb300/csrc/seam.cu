@@ -120,9 +120,13 @@ int frehg_cg_create(const frehg_solver_config* cfg, frehg_cg** out) {
               cfg->ksp_type);
     return FREHG_ERR_UNSUPPORTED;
   }
-  if (strcmp(cfg->pc_type, "jacobi") != 0) {
-    set_error("makeLinearSolver: pc_type '%s' is not available on the gb300 backend (jacobi)",
+  if (strcmp(cfg->pc_type, "jacobi") != 0 && strcmp(cfg->pc_type, "sor") != 0) {
+    set_error("makeLinearSolver: pc_type '%s' is not available on the gb300 backend (jacobi, sor)",
               cfg->pc_type);
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  if (!strcmp(cfg->pc_type, "sor") && cfg->precision != 0) {
+    set_error("makeLinearSolver: pc_type 'sor' runs in FP64 (precision 0)");
     return FREHG_ERR_UNSUPPORTED;
   }
   FG_ARG(cfg->rtol > 0 && cfg->max_it > 0, "rtol and max_it must be positive");
@@ -168,6 +172,10 @@ int frehg_system_create(frehg_cg* cg, int nx, int ny, int nz, frehg_system** out
     set_error("device allocation for the system failed");
     return FREHG_ERR_CUDA;
   }
+  // owned order (k, i, j) on axes (0, 1, 2): the reference's row order is j slowest, then i, k
+  s->A.ref_order[0] = 2;
+  s->A.ref_order[1] = 1;
+  s->A.ref_order[2] = 0;
   *out = s;
   return FREHG_OK;
 }
@@ -303,6 +311,8 @@ int frehg_cg_setup(frehg_cg* cg, frehg_system* s) {
     return FREHG_ERR_STATE;
   }
   FG_TRY(cg->ksp.ensure(s->n));
+  // PCSOR works on the unscaled operator (D and L); Jacobi-PCG on D^-1/2 A D^-1/2
+  if (!strcmp(cg->cfg.pc_type, "sor")) return FREHG_OK;
   return cg->ksp.scale(s->A, cg->stream);
 }
 

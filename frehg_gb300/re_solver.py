@@ -10,8 +10,8 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import (KernelStat, ReCounters, ReParams, SoilParams, SolverConfig, check, dptr,
-                  load_library)
+from .abi import (CHECKPOINT_SCALARS, KernelStat, ReCounters, ReParams, SoilParams,
+                  SolverConfig, check, dptr, load_library)
 
 
 class Grid:
@@ -204,7 +204,7 @@ class ReSolver:
     def checkpoint(self) -> dict:
         """The step state (h, wc in interior order, time, dt state, budgets, ghost flag)."""
         n = self.grid.nx * self.grid.ny * self.grid.nz
-        h, wc, st = np.empty(n), np.empty(n), np.empty(8)
+        h, wc, st = np.empty(n), np.empty(n), np.empty(CHECKPOINT_SCALARS)
         check(self._lib.frehg_re_checkpoint(self._h, dptr(h), dptr(wc), dptr(st)), "checkpoint")
         return {"h": h, "wc": wc, "state": st}
 

@@ -335,9 +335,11 @@ int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, int targ
  * of each row with its k+1, i+1, j+1 neighbour, 0 where that neighbour is absent), b and x.
  * The solver's work space is one fixed device array inside the library, so:
  *   - at most 262,144 unknowns (nx*ny*nz); larger systems get FREHG_ERR_BAD_ARG;
- *   - every GPU that loads the library keeps that array (about 16 MB) until the process ends;
- *   - the first call on a device looks up the array's address with that device current --
- *     make it before any stream capture on the device;
+ *   - every GPU that loads the library keeps that array (17,302,016 bytes, about 17.3 MB or
+ *     16.5 MiB) until the process ends;
+ *   - each call looks up the array's address on the current device; the first call on a
+ *     device loads the library's device code there -- make it before any stream capture on
+ *     the device;
  *   - all calls share the array: calls that overlap on the GPU race; serialise them;
  *   - no cudaMalloc, cudaFree or other allocating routine is called.
  * stream: cudaStream_t as void* (NULL = the legacy default stream).  Same stopping rule,
@@ -365,11 +367,13 @@ int frehg_re_surface_exchange(frehg_re* re, double* eta, const double* bottom, d
  * primeAdaptiveDt).  h and wc are host arrays of nx*ny*nz values in interior order (the only
  * fields the next step reads; every other device array is recomputed by the step);
  * state[FREHG_CHECKPOINT_SCALARS] = {time, dt, dtn, dt_used, top inflow volume, bottom inflow
- * volume, elastic volume, ghosts written (1/0)}.  A handle with the same parameters, soil,
- * solver and top flux field restarted from a checkpoint steps exactly like the run that wrote
- * it (bit for bit).  Checkpoint between steps, not between a surface exchange and the next
- * step (the top layer's pre-exchange ghost copies are not part of the state). */
-#define FREHG_CHECKPOINT_SCALARS 8
+ * volume, elastic volume, ghosts written (1/0), the mixed-precision refinement's first residual
+ * norms of the last first and later solves (the next solves' right-hand-side scales)}.  A
+ * handle with the same parameters, soil, solver and top flux field restarted from a checkpoint
+ * steps exactly like the run that wrote it (bit for bit).  Checkpoint between steps: between a
+ * surface exchange and the next step the top layer's pre-exchange ghost copies are not part of
+ * the state, and the checkpoint returns FREHG_ERR_STATE. */
+#define FREHG_CHECKPOINT_SCALARS 10
 int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state);
 int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const double* state);
 

@@ -38,7 +38,7 @@ inline void check(int rc, const char* what) {
 // struct SolverConfig (SolverConfig.hpp:14-20) plus the precision keys of this backend.
 struct SolverConfig {
   std::string ksp_type = "cg";      // cg | fcg
-  std::string pc_type = "jacobi";   // jacobi | line | unet | unet-line
+  std::string pc_type = "jacobi";   // jacobi | sor (fp64) | line | unet | unet-line
   real rtol = 1e-8;
   real atol = 1e-50;
   int max_it = 10000;

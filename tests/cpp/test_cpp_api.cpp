@@ -67,11 +67,12 @@ static std::vector<double> apply_laplacian(const std::vector<double>& x, const g
   return y;
 }
 
-static void seam(const char* precision) {
+static void seam(const char* precision, const char* pc = "jacobi") {
   g::Decomp3D d(12, 10, 8);
   g::SolverConfig cfg;
   cfg.rtol = 1e-12;
   cfg.precision = precision;
+  cfg.pc_type = pc;
   cfg.ir_rtol = 1e-13;
   auto ls = g::makeLinearSolver("gb300", cfg);
   auto A = ls->createSystem(d);
@@ -92,14 +93,14 @@ static void seam(const char* precision) {
     n2 += xe[q] * xe[q];
   }
   const double rel = std::sqrt(e2 / n2);
-  EXPECT(rel < 1e-9, "seam %s: manufactured Laplacian relative L2 error %.3e (%d iterations)",
-         precision, rel, ls->getIterationCount());
+  EXPECT(rel < 1e-9, "seam %s %s: manufactured Laplacian relative L2 error %.3e (%d iterations)",
+         precision, pc, rel, ls->getIterationCount());
   // getSolution returns the last solve's x
   std::vector<double> x2;
   A->getSolution(x2);
   double d2 = 0.0;
   for (size_t q = 0; q < x.size(); ++q) d2 = std::fmax(d2, std::fabs(x2[q] - x[q]));
-  EXPECT(d2 == 0.0, "seam %s: getSolution equals the solve's x", precision);
+  EXPECT(d2 == 0.0, "seam %s %s: getSolution equals the solve's x", precision, pc);
 }
 
 static void errors() {
@@ -113,12 +114,12 @@ static void errors() {
   thrown = false;
   try {
     g::SolverConfig c;
-    c.pc_type = "sor";
+    c.pc_type = "gamg";
     g::makeLinearSolver("gb300", c);
   } catch (const std::invalid_argument&) {
     thrown = true;
   }
-  EXPECT(thrown, "pc_type sor is rejected (std::invalid_argument)");
+  EXPECT(thrown, "pc_type gamg is rejected (std::invalid_argument)");
   thrown = false;
   try {
     auto ls = g::makeLinearSolver("gb300", g::SolverConfig());
@@ -199,6 +200,7 @@ int main() {
   try {
     seam("fp64");
     seam("mixed");
+    seam("fp64", "sor");
     errors();
     closed_box();
   } catch (const std::exception& e) {

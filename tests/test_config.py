@@ -97,7 +97,8 @@ def test_parameter_mapping():
     assert p.soil.Ss == 1e-5 and p.soil.use_vg == 1 and p.soil.air_entry == -0.02
     assert p.scheme == 0 and p.face_mean == 0
     k = cf.solver_config(d)
-    assert (k.ksp_type, k.pc_type, k.rtol, k.precision) == (b"cg", b"jacobi", 1e-10, 0)
+    # an unset pc_type is PCSOR, the reference default (Orchestrator.cpp:489)
+    assert (k.ksp_type, k.pc_type, k.rtol, k.precision) == (b"cg", b"sor", 1e-10, 0)
     # mapping form of groundwater.solver (Orchestrator.cpp:487-490) + precision extension
     d["groundwater"]["solver"] = {"ksp_type": "cg", "pc_type": "jacobi", "rtol": 1e-8}
     d["groundwater"]["solver_options"] = {"precision": "mixed", "ir_rtol": 1e-12}

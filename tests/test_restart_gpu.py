@@ -53,3 +53,26 @@ def test_restart_picard_rain_mixed(gpu_lib):
     w = W.config4(nx=16, ny=12, nz=96, steps=20, precision=1, pc="line")
     w.params.rain_until = 200.0
     continuous_vs_restart(w, 10, 10)
+
+
+def test_restart_mixed_tiny_first_residual(gpu_lib):
+    """A near-equilibrium Picard run whose first refinement residual is below 2^-30: the first
+    solves' right-hand-side scale comes from the previous solve, which the checkpoint carries,
+    so the restarted handle takes the same scaling path as the continuous run."""
+    w = W.config1("picard", nx=16, ny=12, nz=24, steps=6, precision=1)
+    w.solver.pc_type = b"line"
+    w.params.qtop = -1e-12
+    continuous_vs_restart(w, 3, 3)
+
+
+def test_checkpoint_refused_after_surface_exchange(gpu_lib):
+    from frehg_gb300.abi import FREHG_ERR_STATE, FrehgError
+    w = W.config1("pca", nx=8, ny=6, nz=10, steps=2)
+    g = new(w)
+    g.advance_step()
+    g.surface_exchange(np.full(w.nx * w.ny, 0.01), np.zeros(w.nx * w.ny), 1.0)
+    with pytest.raises(FrehgError) as e:
+        g.checkpoint()
+    assert e.value.code == FREHG_ERR_STATE
+    g.advance_step()
+    g.checkpoint()  # between steps again
