@@ -47,8 +47,15 @@ DEFAULTS = {
     "c1": dict(scheme="picard", precision="fp64", pc="jacobi", steps=20, window=64),
     "c2": dict(scheme="picard", precision="mixed", pc="jacobi", steps=10, window=64),
     "c3": dict(scheme="picard", precision="mixed", pc="unet-line", steps=10, window=64),
-    "c4": dict(scheme="picard", precision="mixed", pc="unet-line", steps=20, window=64),
+    "c4": dict(scheme="picard", precision="mixed", pc="line", steps=20, window=64),
 }
+
+# algorithmic bytes per cell of one launch as the hot-path scope table states them (the
+# roofline's `achieved`): the fused Picard / PCA assembly 72 (read h, theta^n, ln Ks, ln alpha;
+# write the four operator entries and the right-hand side), the Picard update 32, the step-start
+# copy 16.  Kernels without such a figure use their own compulsory bytes (the library's labels).
+SCOPE_BYTES_PER_CELL = {"k_pic_assemble_ff": 72.0, "k_pic_assemble": 72.0, "k_assemble": 72.0,
+                        "k_pic_update": 32.0, "k_copy64": 16.0}
 
 
 def parse():
@@ -78,6 +85,8 @@ def parse():
     ap.add_argument("--picard-fp64", action="store_true",
                     help="Picard kernels in native FP64 instead of float-float on the FP32 pipe")
     ap.add_argument("--profile-steps", type=int, default=1)
+    ap.add_argument("--learned-window", type=int, default=128,
+                    help="columns per side of the learned-preconditioner record (0: skip)")
     ap.add_argument("--nx", type=int, default=None, help="window of the workload (smaller case)")
     ap.add_argument("--ny", type=int, default=None)
     a = ap.parse_args()
@@ -131,6 +140,12 @@ def window(args, side, **kw):
     side = min(side, full, fully)
     w = workload(args, nx=side, ny=side, **kw)
     return w.name.replace(f"{side}x{side}x", f"{full}x{fully}x", 1), w
+
+
+def workload_config(args, name, cells):
+    """The `config` both arms print: what the workload is, nothing about the solver that ran."""
+    return {"workload": name, "cells": int(cells), "scheme": args.scheme,
+            "l2": "working set larger than the 129 MB L2 (no flush needed)"}
 
 
 def dist_env():
@@ -300,6 +315,8 @@ def run_reference(args):
     from oracle import oracle
     oracle.build()
     full_name, w = window(args, args.ref_window, precision="fp64", pc="jacobi")
+    full_cells = (args.nx or FULL_COLUMNS[args.config]) * (args.ny or args.nx or
+                                                           FULL_COLUMNS[args.config]) * w.nz
     o = oracle.OracleRe(w.nx, w.ny, w.nz, w.params)
     w.apply(o)
     for _ in range(args.warmup):
@@ -320,8 +337,9 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded soil fields)",
-        "config": {"workload": full_name, "sample_window": f"{w.nx}x{w.ny}x{w.nz}",
-                   "scheme": args.scheme, "precision": "fp64", "solver": "cg+jacobi rtol 1e-12"},
+        "config": workload_config(args, full_name, full_cells),
+        "arm": {"sample_window": f"{w.nx}x{w.ny}x{w.nz}", "precision": "fp64",
+                "solver": "cg+jacobi rtol 1e-12"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -361,6 +379,54 @@ def trained_net(args):
             "note": "bounded training budget for the benchmark run"}
     del data
     return net, info
+
+
+def learned_record(args, stream, net, info):
+    """The learned preconditioner forced on for every solve, beside the same refinement without
+    it (line-PCG), on a window of the learned-preconditioner configuration: three-layer soil,
+    Picard steps, FP32 Krylov under FP64 refinement to a true relative residual of 1e-12.
+    Reports per arm the inner (FP32) iterations, the time of the solves and of the steps (CUDA
+    events), the network applications and fallbacks, and the head difference between the arms."""
+    import torch
+    import numpy as np
+    from frehg_gb300 import workloads as W
+    from frehg_gb300.abi import check
+    from frehg_gb300.re_solver import Grid, ReSolver
+    n = args.learned_window
+    steps = 3
+    out, heads = {}, {}
+    for pc in ("line", "unet-line"):
+        w = W.config3("picard", nx=n, ny=n, nz=128, steps=steps, pc=pc)
+        s = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
+        s.set_stream(stream.cuda_stream)
+        w.apply(s)
+        if pc != "line":
+            check(s._lib.frehg_re_attach_unet(s._h, net.handle), "attach_unet")
+            check(s._lib.frehg_re_set_learned_policy(s._h, 0, 1e9), "policy")
+        its, c0 = [], s.counters()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            a = s.counters()
+            s.advance_step()
+            its.append(int(s.counters().ksp_iterations - a.ksp_iterations))
+        e1.record(stream)
+        stream.synchronize()
+        c1 = s.counters()
+        heads[pc] = s.interior("h").copy()
+        out[pc] = {"inner_iterations_per_step": its,
+                   "picard_iterations": int(c1.picard_iterations - c0.picard_iterations),
+                   "ms_steps": round(e0.elapsed_time(e1), 2),
+                   "ms_solves": round((c1.net_ms + c1.plain_ms) - (c0.net_ms + c0.plain_ms), 2),
+                   "network_solves": int(c1.net_solves - c0.net_solves),
+                   "fallbacks": int(c1.fcg_fallbacks - c0.fcg_fallbacks)}
+        del s
+    dh = np.abs(heads["line"] - heads["unet-line"])
+    return {"workload": f"c3-picard-{n}x{n}x128 window, {steps} steps",
+            "network": info, "line": out["line"], "learned_forced_on": out["unet-line"],
+            "head_difference_m": float(dh.max()),
+            "solve_time_ratio_learned_over_line": round(
+                out["unet-line"]["ms_solves"] / max(out["line"]["ms_solves"], 1e-9), 3)}
 
 
 def time_arm(args, w, net, stream, barrier, steps, warmup):
@@ -484,14 +550,21 @@ def run_gpu(args):
     tot = sum(st["total_ms"] for st in stats) or 1.0
     dom = max(stats, key=lambda st: st["total_ms"])
     per_launch_ms = dom["total_ms"] / dom["launches"]
-    achieved = dom["bytes_per_launch"] / (per_launch_ms / 1000.0) / 1e9
+    scope_bpc = SCOPE_BYTES_PER_CELL.get(dom["name"])
+    alg_bytes = scope_bpc * w.cells if scope_bpc else dom["bytes_per_launch"]
+    achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
     tr, limiter = ncu_traffic(dom["name"])
     roofline = {
         "bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": peak_kind, "limiter": limiter,
         "traffic": None if tr is None else tr * w.cells,
-        "bytes_per_launch": dom["bytes_per_launch"], "ms_per_launch": per_launch_ms,
+        "bytes_per_launch": alg_bytes,
+        "bytes_per_cell": alg_bytes / w.cells,
+        "bytes_per_cell_source": ("hot-path scope table" if scope_bpc else
+                                  "kernel's compulsory bytes"),
+        "kernel_compulsory_bytes_per_cell": dom["bytes_per_launch"] / w.cells,
+        "ms_per_launch": per_launch_ms,
         "share_of_step": dom["total_ms"] / tot,
         "kernels": {st["name"]: {"launches": st["launches"], "ms": round(st["total_ms"], 4),
                                  "share": round(st["total_ms"] / tot, 4),
@@ -501,7 +574,16 @@ def run_gpu(args):
                     for st in stats},
     }
 
-    net_roof = network_roofline(net, w, stream) if learned else None
+    # the network: its tensor-pipe roofline on this grid, and the forced-on record
+    lnet, linfo = net, net_info
+    want_rec = args.learned_window > 0 and rank == 0 and args.scheme == "picard"
+    if lnet is None and want_rec:
+        lnet, linfo = trained_net(argparse.Namespace(**dict(vars(args), pc="unet-line")))
+    net_roof = network_roofline(lnet, w, stream) if lnet is not None else None
+    learned_rec = None
+    if want_rec:
+        torch.cuda.empty_cache()
+        learned_rec = learned_record(args, stream, lnet, linfo)
 
     # the plain FP64 GPU path on the same inputs and steps (FP64 Jacobi-PCG, native FP64
     # Picard kernels): throughput and head error
@@ -548,29 +630,30 @@ def run_gpu(args):
         "dtype": ("f64" if args.precision == "fp64" else "f64+f32" + ("+bf16" if learned else ""))
                  + ("+ff" if args.scheme == "picard" and not w.params.picard_fp64 else ""),
         "data": "synthetic (seeded soil fields)",
-        "config": {"workload": w.name, "cells": w.cells, "scheme": args.scheme,
-                   "precision": args.precision, "pc": args.pc, "solver": solver,
-                   "parallelism": f"replicas x{world}",
-                   "picard_arith": ("native fp64" if args.scheme != "picard" or w.params.picard_fp64
-                                    else "float-float (two fp32, ~48-bit significand) for the "
-                                         "constitutive relations, assembly and final update; "
-                                         "refinement residual fp64"),
-                   "l2": "working set > 1 GB, larger than the 129 MB L2 (no flush needed)",
-                   "picard_iterations": cnt["picard_iterations"],
-                   "cg_iterations": cnt["ksp_iterations"], "ir_sweeps": cnt["ir_sweeps"],
-                   "mass_error_rel": cnt["mass_error_rel"]},
+        "config": workload_config(args, w.name, w.cells),
+        "arm": {"precision": args.precision, "pc": args.pc, "solver": solver,
+                "parallelism": f"replicas x{world}",
+                "picard_arith": ("native fp64" if args.scheme != "picard" or w.params.picard_fp64
+                                 else "float-float (two fp32, ~48-bit significand) for the "
+                                      "constitutive relations, face fluxes and final update; "
+                                      "Picard residual's storage difference and combination, "
+                                      "refinement residual and mass sums fp64"),
+                "picard_iterations": cnt["picard_iterations"],
+                "cg_iterations": cnt["ksp_iterations"], "ir_sweeps": cnt["ir_sweeps"],
+                "mass_error_rel": cnt["mass_error_rel"]},
         "comparison": comparison,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(q_host.numel() * 8),
                 "d2h_bytes_per_step": int(h_host.numel() * 8 + wc_host.numel() * 8)},
         "roofline": roofline,
         "roofline_network": net_roof,
+        "learned": learned_rec,
         "cpu_baseline": cpu,
         "gpu_launches": int(cnt["kernel_launches"]),
         "clocks": clk,
     }
     if learned:
-        line["config"]["learned"] = dict(net_info, net_solves=cnt["net_solves"],
+        line["arm"]["learned"] = dict(net_info, net_solves=cnt["net_solves"],
                                          net_skipped=cnt["net_skipped"],
                                          fcg_fallbacks=cnt["fcg_fallbacks"],
                                          net_solve_ms=round(cnt["net_ms"], 2),

@@ -5,7 +5,8 @@
 // rate, and the FP64 forms of these kernels are bound by that pipe, not by memory.
 //
 // Doubles are read and split into float-float with integer operations; results are written
-// back as doubles.  The matrix (diagonal and couplings) is formed from the leading floats of
+// back as doubles.  The Picard residual's storage difference (theta(h^m) - theta^n of the two
+// stored doubles) and its final combination stay in FP64.  The matrix (diagonal and couplings) is formed from the leading floats of
 // the float-float transmissibilities: it shapes each Picard update, not the fixed point the
 // iteration converges to, and the mixed-precision solve rounds it to FP32 anyway.  Sums use
 // the double-word addition whose error is a few 2^-48 of the operands (not of the result): the
@@ -378,10 +379,13 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
         a0[c] = (T)(-dtf * tx);
         a1[c] = (T)(-dtf * ty);
         a2[c] = (T)(-dtf * tz);
-        const ff dth = ff_dif(ff_from_double(r_wch), wcn);
+        // the storage difference wch - wcn of the two stored doubles and the residual's last
+        // combination in FP64 (the difference is exact where the values are close, Sterbenz);
+        // the elastic term and the face-flux sum in float-float
+        const double dth = r_wch - r_wo;
         const ff dh = ff_dif(cur.h, ff_from_double(r_ho));
-        const ff rdt = ff_dif(ff_mul(K.V, ff_add_fast(dth, ff_mul(st, dh))), ff_mul(K.dt, q));
-        bvec[c] = -ff_to_double(rdt);
+        const ff rest = ff_dif(ff_mul(K.V, ff_mul(st, dh)), ff_mul(K.dt, q));
+        bvec[c] = -fma(a.vol_cell, dth, ff_to_double(rest));
       }
       cur = below;
     }

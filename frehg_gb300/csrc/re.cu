@@ -190,6 +190,7 @@ static ReArgs make_args(frehg_re* re) {
     a.inv_Ax = 1.0 / (dy * dz);
     a.inv_Ay = 1.0 / (dx * dz);
     a.inv_Az = 1.0 / (dx * dy);
+    a.vol_cell = dx * dy * dz;
   }
   a.soil.cls = re->cls;
   a.soil.cid = re->cid;
@@ -646,7 +647,7 @@ static int picard_step(frehg_re* re) {
       re->A.s_in_r = false;
       re->A.f32_entries = f32;
       if (re->p.picard_fp64)
-        FG_LAUNCH(prof, st, "k_pic_assemble", (64.0 + sb) * n,
+        FG_LAUNCH(prof, st, "k_pic_assemble", (88.0 + sb) * n,
                   k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
                                                                re->A.a2, re->A.b, PL.planes,
                                                                PL.tiles));
@@ -655,19 +656,19 @@ static int picard_step(frehg_re* re) {
         float* dgf = reinterpret_cast<float*>(re->A.s);
         const Stencil32& o = re->ksp.op32;
         if (iso)
-          FG_LAUNCH(prof, st, "k_pic_assemble_ff", (48.0 + sb) * n,
+          FG_LAUNCH(prof, st, "k_pic_assemble_ff", (72.0 + sb) * n,
                     (k_pic_assemble_ff<true, false, float><<<PL.grid, PL.block, 0, st>>>(
                         a, dgf, o.a0, o.a1, o.a2, re->A.b, PL.planes, PL.tiles)));
         else
-          FG_LAUNCH(prof, st, "k_pic_assemble_ff", (48.0 + sb) * n,
+          FG_LAUNCH(prof, st, "k_pic_assemble_ff", (72.0 + sb) * n,
                     (k_pic_assemble_ff<false, false, float><<<PL.grid, PL.block, 0, st>>>(
                         a, dgf, o.a0, o.a1, o.a2, re->A.b, PL.planes, PL.tiles)));
       } else if (iso)
-        FG_LAUNCH(prof, st, "k_pic_assemble_ff", (64.0 + sb) * n,
+        FG_LAUNCH(prof, st, "k_pic_assemble_ff", (88.0 + sb) * n,
                   k_pic_assemble_ff<true><<<PL.grid, PL.block, 0, st>>>(
                       a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b, PL.planes, PL.tiles));
       else
-        FG_LAUNCH(prof, st, "k_pic_assemble_ff", (64.0 + sb) * n,
+        FG_LAUNCH(prof, st, "k_pic_assemble_ff", (88.0 + sb) * n,
                   k_pic_assemble_ff<false><<<PL.grid, PL.block, 0, st>>>(
                       a, re->A.s, re->A.a0, re->A.a1, re->A.a2, re->A.b, PL.planes, PL.tiles));
       FG_CUDA(cudaGetLastError());
@@ -722,14 +723,14 @@ static int picard_step(frehg_re* re) {
     dt = fmax(0.5 * dt, dt_floor);
   }
   if (re->p.picard_fp64)
-    FG_LAUNCH(prof, st, "k_pic_final", (48.0 + sb) * n,
+    FG_LAUNCH(prof, st, "k_pic_final", (40.0 + sb) * n,
               k_pic_final<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
   else if (iso)
-    FG_LAUNCH(prof, st, "k_pic_final_ff", (48.0 + sb) * n,
+    FG_LAUNCH(prof, st, "k_pic_final_ff", (40.0 + sb) * n,
               (k_pic_assemble_ff<true, true, double><<<PL.grid, PL.block, 0, st>>>(
                   a, nullptr, nullptr, nullptr, nullptr, nullptr, PL.planes, PL.tiles)));
   else
-    FG_LAUNCH(prof, st, "k_pic_final_ff", (48.0 + sb) * n,
+    FG_LAUNCH(prof, st, "k_pic_final_ff", (40.0 + sb) * n,
               (k_pic_assemble_ff<false, true, double><<<PL.grid, PL.block, 0, st>>>(
                   a, nullptr, nullptr, nullptr, nullptr, nullptr, PL.planes, PL.tiles)));
   FG_CUDA(cudaGetLastError());

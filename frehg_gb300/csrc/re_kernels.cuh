@@ -69,6 +69,7 @@ struct ReArgs {
   const double* gh_top_w;
   // geometric factors: 1/dx, 1/dy, 1/dz; Ax/dx, Ay/dy, Az/dz; V/dz; 1/Ax, 1/Ay, 1/Az
   double inv_dx, inv_dy, inv_dz, cx, cy, cz, v_dz, inv_Ax, inv_Ay, inv_Az;
+  double vol_cell;  // dx * dy * dz
   SoilView soil;
   const double* h_old;  // h^n (and hn)
   const double* w_old;  // wc^n (and wcn)

@@ -1230,6 +1230,14 @@ int or_re_get_field(const or_re* s, const char* name, double* out) {
   return FREHG_ERR_BAD_ARG;
 }
 
+/* The last linear system the step assembled (7 coefficients per owned row, C W E S N Up Down,
+ * and the right-hand side), for preconditioner studies in the tests. */
+void or_re_last_system(const or_re* s, double* coef, double* b) {
+  const long n = (long)s->nx * s->ny * s->nz;
+  if (coef) memcpy(coef, s->coef, sizeof(double) * 7 * (size_t)n);
+  if (b) memcpy(b, s->b_owned, sizeof(double) * (size_t)n);
+}
+
 /* ======================= modified Picard (not in reference) ====================== */
 #include "frehg_oracle_picard.inc"
 

@@ -50,6 +50,8 @@ void or_re_prime_adaptive_dt(or_re* st, double dt);
  * unknown name. */
 int or_re_get_field(const or_re* st, const char* name, double* out_halo);
 int or_re_last_ksp_its(const or_re* st);
+/* the last assembled system: coef[7 n] (owned order, slots C W E S N Up Down) and b[n] */
+void or_re_last_system(const or_re* st, double* coef, double* b);
 int or_re_last_picard_its(const or_re* st);
 double or_re_last_rnorm(const or_re* st);
 long long or_re_total_ksp_its(const or_re* st);

@@ -64,6 +64,7 @@ def lib():
             "or_re_prime_adaptive_dt": (None, [_VP, C.c_double]),
             "or_re_get_field": (C.c_int, [_VP, C.c_char_p, _PD]),
             "or_re_last_ksp_its": (C.c_int, [_VP]),
+            "or_re_last_system": (None, [_VP, _PD, _PD]),
             "or_re_last_picard_its": (C.c_int, [_VP]),
             "or_re_last_rnorm": (C.c_double, [_VP]),
             "or_re_total_ksp_its": (C.c_longlong, [_VP]),
@@ -180,6 +181,14 @@ class OracleRe:
 
     def last_ksp_its(self):
         return lib().or_re_last_ksp_its(self.h)
+
+    def last_system(self):
+        """(coef (n, 7) in owned order with slots C W E S N Up Down, b (n,)) of the last
+        assembled linear system"""
+        n = self.nx * self.ny * self.nz
+        coef, b = np.empty(7 * n), np.empty(n)
+        lib().or_re_last_system(self.h, coef.ctypes.data_as(_PD), b.ctypes.data_as(_PD))
+        return coef.reshape(n, 7), b
 
     def last_picard_its(self):
         return lib().or_re_last_picard_its(self.h)
