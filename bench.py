@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--picard-fp64", action="store_true",
                     help="Picard kernels in native FP64 instead of float-float on the FP32 pipe")
     ap.add_argument("--profile-steps", type=int, default=1)
+    ap.add_argument("--staged-assembly", action="store_true",
+                    help="stage the Picard assembly's inputs through TMA (same results)")
     ap.add_argument("--learned-window", type=int, default=128,
                     help="columns per side of the learned-preconditioner record (0: skip)")
     ap.add_argument("--nx", type=int, default=None, help="window of the workload (smaller case)")
@@ -437,6 +439,8 @@ def time_arm(args, w, net, stream, barrier, steps, warmup):
     from frehg_gb300.re_solver import Grid, ReSolver
     s = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
     s.set_stream(stream.cuda_stream)
+    if getattr(args, "staged_assembly", False):
+        s.set_assembly_staging(True)
 
     def reset():
         s.set_params(w.params)
@@ -632,6 +636,7 @@ def run_gpu(args):
         "data": "synthetic (seeded soil fields)",
         "config": workload_config(args, w.name, w.cells),
         "arm": {"precision": args.precision, "pc": args.pc, "solver": solver,
+                "staged_assembly": bool(args.staged_assembly),
                 "parallelism": f"replicas x{world}",
                 "picard_arith": ("native fp64" if args.scheme != "picard" or w.params.picard_fp64
                                  else "float-float (two fp32, ~48-bit significand) for the "

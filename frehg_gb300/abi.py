@@ -261,6 +261,7 @@ SIGNATURES = {
     "frehg_unet_flops": (C.c_int, [C.c_int, C.c_int, C.c_int, _PD]),
     "frehg_re_attach_unet": (C.c_int, [_VP, _VP]),
     "frehg_re_set_learned_policy": (C.c_int, [_VP, C.c_int, C.c_double]),
+    "frehg_re_set_assembly_staging": (C.c_int, [_VP, C.c_int]),
     "frehg_re_training_pairs": (C.c_int, [_VP, C.c_int, _PI, C.c_int, _VP, _VP, _VP, _VP]),
     "frehg_build_arch": (C.c_int, []),
     "frehg_re_checkpoint": (C.c_int, [_VP, _VP, _VP, _VP]),
@@ -269,6 +270,7 @@ SIGNATURES = {
     "frehg_re_restart": (C.c_int, [_VP, _VP, _VP, _VP]),
     "frehg_fastmath_eval": (C.c_int, [C.c_int, _VP, _VP, C.c_int64]),
     "frehg_constit_eval": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_int64, _VP, _VP, _VP]),
+    "frehg_re_check_staged_assembly": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
 }
 
 _lib = None

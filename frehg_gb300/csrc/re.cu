@@ -5,8 +5,10 @@
 #include "re_kernels.cuh"
 #include "picard.cuh"
 #include "picard_ff.cuh"
+#include "picard_tma.cuh"
 #include "krylov_kernels.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <chrono>
 #include <cstring>
@@ -41,6 +43,7 @@ struct frehg_re {
   bool has_qtop = false;
   uint8_t* flags = nullptr;
   double* scratch = nullptr;  // n doubles for exports / Picard increments
+  bool staged = false;        // Picard assembly staged through TMA (frehg_re_set_assembly_staging)
   ReScalars* sc = nullptr;
   ReScalars* sc_host = nullptr;
   double* partials = nullptr;
@@ -598,6 +601,83 @@ static int pca_step(frehg_re* re) {
   return FREHG_OK;
 }
 
+// ------------------------------------------------------------------------------------------
+// Tensor maps of the staged (TMA) Picard assembly: cuTensorMapEncodeTiled through the runtime's
+// driver entry point (the library does not link libcuda).
+
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return static_cast<EncodeTiledFn>(nullptr);
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// an nx x ny x nz FP64 array (x fastest), boxes of bx x by x 1; out-of-range elements read 0
+bool encode_box(CUtensorMap* m, const double* base, int nx, int ny, int nz, int bx, int by) {
+  const EncodeTiledFn f = encode_tiled();
+  if (!f || (reinterpret_cast<uintptr_t>(base) & 15u)) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * 8u, (cuuint64_t)nx * ny * 8u};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1u};
+  const cuuint32_t es[3] = {1u, 1u, 1u};
+  return f(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dims, strides, box,
+           es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the staged arrays' tensor maps; false when the layout does not qualify (the row stride of nx
+// doubles must be a multiple of 16 bytes)
+bool pic_tma_maps(const ReArgs& a, const double* ks, PicTmaMaps* m) {
+  if (!ks || (a.nx & 1)) return false;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  return encode_box(&m->h, a.h_new, nx, ny, nz, kPtWideX, kPtWideY) &&
+         encode_box(&m->kr, a.kr, nx, ny, nz, kPtWideX, kPtWideY) &&
+         encode_box(&m->ks, ks, nx, ny, nz, kPtWideX, kPtWideY) &&
+         encode_box(&m->wo, a.w_old, nx, ny, nz, 32, 8) &&
+         encode_box(&m->ho, a.h_old, nx, ny, nz, 32, 8) &&
+         encode_box(&m->wch, a.wch, nx, ny, nz, 32, 8) &&
+         encode_box(&m->cap, a.cap, nx, ny, nz, 32, 8);
+}
+}  // namespace
+
+// Launch the staged assembly (mixed-precision form: float matrix entries).  *launched stays
+// false when the handle's layout does not qualify; the caller then launches k_pic_assemble_ff.
+static int launch_staged_assembly(frehg_re* re, const ReArgs& a, const StencilLaunch& PL,
+                                  float* dgf, const Stencil32& o, double* b, bool* launched) {
+  *launched = false;
+  PicTmaMaps maps;
+  if (!pic_tma_maps(a, re->fKs, &maps)) return FREHG_OK;
+  static bool attr_set = false;
+  if (!attr_set) {
+    FG_CUDA(cudaFuncSetAttribute(k_pic_assemble_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kPtSmemBytes + 128));
+    attr_set = true;
+  }
+  const double n = (double)re->n;
+  // persistent: three blocks per SM stride over the tiles, so each block's copy pipeline runs on
+  // from one tile into the next
+  const long per_slab = (long)kNumSMs * 3 / (long)PL.grid.y;
+  const dim3 grid((unsigned)std::max(1L, std::min((long)PL.tiles, per_slab)), PL.grid.y, 1);
+  FG_LAUNCH(&re->prof, re->stream, "k_pic_assemble_ff", (72.0 + soil_bytes(re)) * n,
+            (k_pic_assemble_tma<<<grid, dim3(32, 9), kPtSmemBytes + 128, re->stream>>>(
+                a, maps, dgf, o.a0, o.a1, o.a2, b, PL.planes, PL.tiles, &re->sc->stage_err)));
+  FG_CUDA(cudaGetLastError());
+  *launched = true;
+  return FREHG_OK;
+}
+
 static int read_scalars(const frehg_re* re) {
   FG_CUDA(cudaStreamSynchronize(re->stream));
   FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
@@ -655,7 +735,10 @@ static int picard_step(frehg_re* re) {
         // diagonal and couplings as floats (the float-float preparation's input)
         float* dgf = reinterpret_cast<float*>(re->A.s);
         const Stencil32& o = re->ksp.op32;
-        if (iso)
+        bool staged = false;
+        if (iso && re->staged) FG_TRY(launch_staged_assembly(re, a, PL, dgf, o, re->A.b, &staged));
+        if (staged) {
+        } else if (iso)
           FG_LAUNCH(prof, st, "k_pic_assemble_ff", (72.0 + sb) * n,
                     (k_pic_assemble_ff<true, false, float><<<PL.grid, PL.block, 0, st>>>(
                         a, dgf, o.a0, o.a1, o.a2, re->A.b, PL.planes, PL.tiles)));
@@ -698,7 +781,14 @@ static int picard_step(frehg_re* re) {
       FG_CUDA(cudaGetLastError());
       FG_CUDA(cudaMemcpyAsync(&re->sc_host->dq_max, &re->sc->dq_max, sizeof(double),
                               cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaMemcpyAsync(&re->sc_host->stage_err, &re->sc->stage_err, sizeof(int),
+                              cudaMemcpyDeviceToHost, st));
       FG_CUDA(cudaStreamSynchronize(st));
+      if (re->sc_host->stage_err) {
+        set_error("staged Picard assembly: a bounded wait on its copy pipeline ran out (%d)",
+                  re->sc_host->stage_err);
+        return FREHG_ERR_CUDA;
+      }
       if (prof->on) FG_TRY(prof->flush());
       re->cnt.picard_iterations += 1;
       if (re->sc_host->dq_max < re->p.picard_tol) {
@@ -1324,6 +1414,86 @@ int frehg_re_get_field(frehg_re* re, const char* name, double* out_halo) {
   return FREHG_OK;
 }
 
+int frehg_re_check_staged_assembly(frehg_re* re, int64_t* mismatches) {
+  clear_error();
+  FG_ARG(re && mismatches, "null argument");
+  FG_ARG(re->finalized, "check before a finalized state");
+  const ReArgs a = make_args(re);
+  if (re->p.scheme != 1 || re->p.picard_fp64 || !mixed_solve(re) || !re->fKs || (re->nx & 1)) {
+    set_error("the staged assembly serves Picard handles in mixed precision with a per-cell Ks "
+              "field and an even nx");
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  const size_t n = re->n;
+  const StencilLaunch PL = stencil_launch(re->nx, re->ny, re->nz);
+  cudaStream_t st = re->stream;
+  float* f[2][4] = {{nullptr}};
+  double* b[2] = {nullptr, nullptr};
+  int rc = FREHG_OK;
+  for (int v = 0; v < 2 && rc == FREHG_OK; ++v) {
+    for (int q = 0; q < 4; ++q)
+      if (cudaMalloc(&f[v][q], n * sizeof(float)) != cudaSuccess) rc = FREHG_ERR_CUDA;
+    if (cudaMalloc(&b[v], n * sizeof(double)) != cudaSuccess) rc = FREHG_ERR_CUDA;
+  }
+  if (rc != FREHG_OK) set_error("self-check allocation failed");
+  if (rc == FREHG_OK) {
+    Stencil32 o;
+    o.n = n;
+    o.a0 = f[0][1];
+    o.a1 = f[0][2];
+    o.a2 = f[0][3];
+    bool staged = false;
+    rc = launch_staged_assembly(re, a, PL, f[0][0], o, b[0], &staged);
+    o.a0 = o.a1 = o.a2 = nullptr;  // not owned
+    if (rc == FREHG_OK && !staged) {
+      set_error("tensor maps of the staged assembly could not be encoded");
+      rc = FREHG_ERR_UNSUPPORTED;
+    }
+    if (rc == FREHG_OK) {
+      k_pic_assemble_ff<true, false, float><<<PL.grid, PL.block, 0, st>>>(
+          a, f[1][0], f[1][1], f[1][2], f[1][3], b[1], PL.planes, PL.tiles);
+      if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error("assembly self-check launch failed");
+        rc = FREHG_ERR_CUDA;
+      }
+    }
+    if (rc == FREHG_OK) {
+      int64_t bad = 0;
+      std::vector<uint32_t> x(n), y(n);
+      for (int q = 0; q < 4 && rc == FREHG_OK; ++q) {
+        if (cudaMemcpy(x.data(), f[0][q], n * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(y.data(), f[1][q], n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+          set_error("self-check copy failed");
+          rc = FREHG_ERR_CUDA;
+        }
+        for (size_t c = 0; c < n && rc == FREHG_OK; ++c) bad += x[c] != y[c];
+      }
+      std::vector<uint64_t> u(n), w(n);
+      if (rc == FREHG_OK &&
+          (cudaMemcpy(u.data(), b[0], n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+           cudaMemcpy(w.data(), b[1], n * 8, cudaMemcpyDeviceToHost) != cudaSuccess)) {
+        set_error("self-check copy failed");
+        rc = FREHG_ERR_CUDA;
+      }
+      if (rc == FREHG_OK)
+        for (size_t c = 0; c < n; ++c) bad += u[c] != w[c];
+      *mismatches = bad;
+      ReScalars sh;
+      if (rc == FREHG_OK &&
+          cudaMemcpy(&sh, re->sc, sizeof(sh), cudaMemcpyDeviceToHost) == cudaSuccess &&
+          sh.stage_err) {
+        set_error("staged Picard assembly: a bounded wait ran out (%d)", sh.stage_err);
+        rc = FREHG_ERR_CUDA;
+      }
+    }
+  }
+  for (int v = 0; v < 2; ++v) {
+    for (int q = 0; q < 4; ++q) cudaFree(f[v][q]);
+    cudaFree(b[v]);
+  }
+  return rc;
+}
+
 int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c) {
   clear_error();
   FG_ARG(re && c, "null argument");
@@ -1352,6 +1522,13 @@ int frehg_re_attach_unet(frehg_re* re, frehg_unet* net) {
   re->probe_pending = true;
   re->solves_since_probe = 0;
   re->last_plain_ms = 0.0;
+  return FREHG_OK;
+}
+
+int frehg_re_set_assembly_staging(frehg_re* re, int on) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  re->staged = on != 0;
   return FREHG_OK;
 }
 

@@ -47,7 +47,7 @@ struct ReScalars {
   double vol_bot;   // cumulative bottom-face inflow volume
   double vol_elastic;
   int changed;      // reallocation sweep changed a flag
-  int pad_;
+  int stage_err;    // staged (TMA) assembly: nonzero when one of its bounded waits ran out
   unsigned int arrive[8];
 };
 

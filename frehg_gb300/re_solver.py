@@ -258,6 +258,11 @@ class ReSolver:
         """Cumulative specific-storage volume of the Picard step (not in reference)."""
         return self.counters().elastic_volume
 
+    def set_assembly_staging(self, on: bool):
+        """Stage the Picard assembly's inputs through the Tensor Memory Accelerator (same bits;
+        not in reference)."""
+        check(self._lib.frehg_re_set_assembly_staging(self._h, int(bool(on))), "setAssemblyStaging")
+
     def set_profiling(self, on: bool):
         check(self._lib.frehg_re_set_profiling(self._h, int(bool(on))), "setProfiling")
 

@@ -318,6 +318,13 @@ int frehg_re_attach_unet(frehg_re* re, frehg_unet* net);
  * than max_ratio times the last network-free solve.  probe_every = 0 applies the network on
  * every solve (no time policy).  Defaults: 32, 1.0. */
 int frehg_re_set_learned_policy(frehg_re* re, int probe_every, double max_ratio);
+/* Picard assembly staged through the Tensor Memory Accelerator (not in reference): on = 1
+ * stages the float-float assembly's inputs with cp.async.bulk.tensor into a shared-memory ring
+ * (mixed-precision Picard handles with a per-cell Ks field and an even nx; other cases keep the
+ * unstaged kernel).  Both kernels write the same bits; the unstaged one is the default because
+ * the assembly is bound by float-float instruction issue, not by memory (the staged kernel moves
+ * fewer DRAM bytes but runs about 5 % longer on GB300). */
+int frehg_re_set_assembly_staging(frehg_re* re, int on);
 /* Training pairs from the plain solver: assembles the next PCA step's system at the current
  * state (nothing advances), solves it with FP64 Jacobi-PCG, re-runs the iteration from zero and
  * at each iteration number iters[q] (increasing) stores the scaled residual r~ and a target
@@ -394,6 +401,14 @@ int frehg_fastmath_eval(int fn, const double* x, double* y, int64_t n);
  * Picard scheme does. */
 int frehg_constit_eval(const frehg_soil_params* soil, int arith, int continuous_theta,
                        const double* h, int64_t n, double* kr, double* wc, double* cap);
+
+/* Self-check of the TMA-staged Picard assembly (not in reference): on the handle's current
+ * state (a Picard handle in mixed precision, soil with a per-cell Ks field, even nx -- the case
+ * the step stages through the Tensor Memory Accelerator), assembles the system once with the
+ * staged kernel and once with the unstaged float-float kernel and stores the number of matrix
+ * and right-hand-side entries whose bits differ in *mismatches (0: identical).  Returns
+ * FREHG_ERR_UNSUPPORTED when the handle's case does not take the staged kernel. */
+int frehg_re_check_staged_assembly(frehg_re* re, int64_t* mismatches);
 
 #ifdef __cplusplus
 }

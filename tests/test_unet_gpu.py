@@ -43,7 +43,11 @@ def test_forward_and_gradients_match_reference(gpu_lib, shape):
                                       y.data_ptr(), None) == 0
     yref, _, rms = U.forward(params, r, lnk, cap)
     yg = y.cpu().numpy()
-    assert np.abs(yg - yref * rms).max() <= 2e-2 * np.abs(yref * rms).max()
+    err = np.abs(yg - yref * rms).max() / np.abs(yref * rms).max()
+    print(f"\n  forward {shape}: max error {err:.2e} of the output's maximum")
+    # the statement rounds to BF16 where the GPU stores BF16; what remains is the order of the
+    # FP32 accumulations and BF16 ties (a few BF16 ulps, 2^-8 each, of a layer's inputs)
+    assert err <= 8e-3
     loss = C.c_double()
     g = np.zeros(params.size, dtype=np.float32)
     assert gpu_lib.frehg_unet_loss_grad(h, nx, ny, nz, tr.data_ptr(), tk.data_ptr(),
@@ -81,6 +85,43 @@ def test_adam_lowers_the_loss(gpu_lib):
         losses.append(loss.value)
         assert gpu_lib.frehg_unet_adam_step(h, 1e-3, 0.9, 0.999, 1e-8, None) == 0
     assert losses[-1] < 0.5 * losses[0], losses[::10]
+    gpu_lib.frehg_unet_destroy(h)
+
+
+def test_adam_matches_numpy(gpu_lib):
+    """Three Adam steps on the GPU's own gradients against the same update in numpy (FP32):
+    m = b1 m + (1-b1) g, v = b2 v + (1-b2) g^2, w -= lr (m/(1-b1^t)) / (sqrt(v/(1-b2^t)) + eps)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(4)
+    shape = (8, 16, 16)
+    r = rng.standard_normal(shape).astype(np.float32)
+    lnk = rng.standard_normal(shape).astype(np.float32)
+    cap = rng.uniform(0, 1, shape).astype(np.float32)
+    tgt = rng.standard_normal(shape).astype(np.float32)
+    params = U.init_params(8).astype(np.float32)
+    h = net_with(gpu_lib, params)
+    tr, tk, tc, tt = dev(torch, r), dev(torch, lnk), dev(torch, cap), dev(torch, tgt)
+    lr, b1, b2, eps = np.float32(1e-3), np.float32(0.9), np.float32(0.999), np.float32(1e-8)
+    w = params.copy()
+    m = np.zeros_like(w)
+    v = np.zeros_like(w)
+    for t in range(1, 4):
+        loss = C.c_double()
+        g = np.zeros(w.size, dtype=np.float32)
+        assert gpu_lib.frehg_unet_loss_grad(h, 16, 16, 8, tr.data_ptr(), tk.data_ptr(),
+                                            tc.data_ptr(), tt.data_ptr(), C.byref(loss),
+                                            g.ctypes.data_as(C.POINTER(C.c_float)), None) == 0
+        assert gpu_lib.frehg_unet_adam_step(h, float(lr), float(b1), float(b2), float(eps),
+                                            None) == 0
+        m = b1 * m + (np.float32(1) - b1) * g
+        v = b2 * v + (np.float32(1) - b2) * g * g
+        c1 = np.float32(1) - np.float32(b1 ** t)
+        c2 = np.float32(1) - np.float32(b2 ** t)
+        w = w - lr * (m / c1) / (np.sqrt(v / c2) + eps)
+        got = np.empty_like(w)
+        assert gpu_lib.frehg_unet_get_params(h, got.ctypes.data_as(C.POINTER(C.c_float))) == 0
+        step = np.abs(w - params).max()
+        assert np.abs(got - w).max() <= 1e-3 * step + 1e-9, (t, np.abs(got - w).max(), step)
     gpu_lib.frehg_unet_destroy(h)
 
 
