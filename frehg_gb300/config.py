@@ -418,6 +418,19 @@ def recharge_field(cfg, nx, ny, dx, dy):
     return np.where(inside, rate, 0.0).ravel()
 
 
+def constant_head_ic(ic):
+    """A head IC given as a formula that is a plain number (`h: {type: formula, formula: "-500"}`,
+    dispatched as a head field like the reference's formula ICs, src/ic/ICApply.cpp:211-224);
+    None for any other form."""
+    h = ic.get("h") if isinstance(ic, dict) else None
+    if isinstance(h, dict) and h.get("type") == "formula":
+        try:
+            return float(str(h.get("formula")).strip())
+        except ValueError:
+            return None
+    return None
+
+
 def build_groundwater(cfg, base_dir="."):
     """Validate, then build and initialise a GPU ReSolver from a parsed v2 config."""
     import numpy as np
@@ -438,13 +451,17 @@ def build_groundwater(cfg, base_dir="."):
     # content initialises every cell; its default is theta_r of soil class 0; a constant head
     # is not used.
     ic = get(cfg, "initial_conditions.groundwater", {}) or {}
-    if ic.get("h_from_file") or ic.get("wc_from_file") or isinstance(ic.get("h"), dict) or \
-            isinstance(ic.get("wc"), dict):
-        raise ConfigError("raster / formula / polygon initial conditions belong to the IC "
-                          "builder, which is not built here (constant wc only)")
-    wc0 = ic.get("wc")
-    wc0 = p.soil.theta_r if wc0 is None else float(wc0)
-    s.set_initial_water_content(np.full(nx * ny * nz, wc0))
+    h0 = constant_head_ic(ic)
+    if h0 is not None:
+        s.set_initial_head(np.full(nx * ny * nz, h0))
+    else:
+        if ic.get("h_from_file") or ic.get("wc_from_file") or isinstance(ic.get("h"), dict) or \
+                isinstance(ic.get("wc"), dict):
+            raise ConfigError("raster / polygon / non-constant formula initial conditions belong "
+                              "to the IC builder, which is not built here (constant wc or head)")
+        wc0 = ic.get("wc")
+        wc0 = p.soil.theta_r if wc0 is None else float(wc0)
+        s.set_initial_water_content(np.full(nx * ny * nz, wc0))
     s.finalize_initial_state()
     s.attach_solver(solver_config(cfg))
     return s

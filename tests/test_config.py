@@ -198,3 +198,11 @@ def test_recharge_polygon():
     assert np.all(cf.recharge_field(d, 6, 4, 1.0, 1.0) == 2e-7)
     del d["groundwater"]["recharge"]
     assert cf.recharge_field(d, 6, 4, 1.0, 1.0) is None
+
+
+def test_constant_formula_head_ic():
+    """initial_conditions.groundwater.h as a formula that is a number is a uniform head (the
+    reference dispatches formula ICs as head fields); other forms are not constant heads."""
+    assert cf.constant_head_ic({"h": {"type": "formula", "formula": "-500"}}) == -500.0
+    assert cf.constant_head_ic({"h": {"type": "formula", "formula": "-2*z"}}) is None
+    assert cf.constant_head_ic({"wc": 0.1}) is None

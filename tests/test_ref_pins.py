@@ -161,3 +161,20 @@ def test_adaptive_3d_grf(oracle_mod):
     w.params.adaptive_dt = 1
     w.params.dt, w.params.dt_min, w.params.dt_max = 5.0, 0.5, 120.0
     run_both(oracle_mod, w)
+
+
+def test_b3_kirkland_first_steps(oracle_mod):
+    """benchmarks/b3-kirkland (two-class 3D map from the layer files, partial recharge, adaptive
+    dt, CG + SOR): the first 300 steps"""
+    from tests.golden_util import b3_case, b3_setup
+    _, inp = b3_case()
+    o = oracle_mod.OracleRe(inp["nx"], inp["ny"], inp["nz"], inp["params"])
+    r = ref.RefRe(inp["nx"], inp["ny"], inp["nz"], inp["params"])
+    for s in (o, r):
+        b3_setup(s, inp)
+    for step in range(300):
+        o.advance_step()
+        r.advance_step()
+        assert o.dt_used() == r.dt_used() and o.last_ksp_its() == r.last_ksp_its(), step
+    for f in FIELDS:
+        assert np.array_equal(o.field(f), r.field(f)), f
