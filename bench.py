@@ -268,12 +268,14 @@ def network_roofline(net, w, stream):
             "peak_source": kind, "ms_per_application": ms, "flop_per_application": flops}
 
 
+def ncu_table():
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    return json.load(open(p)) if os.path.exists(p) else {}
+
+
 def ncu_traffic(kernel):
     """(DRAM bytes per cell, limiter) of `kernel` from the committed ncu summary (profiles/)"""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if not os.path.exists(p):
-        return None, None
-    v = json.load(open(p)).get(kernel)
+    v = ncu_table().get(kernel)
     if isinstance(v, dict):
         return v.get("dram_bytes_per_cell"), v.get("limiter")
     return v, None
@@ -574,7 +576,12 @@ def run_gpu(args):
                                  "share": round(st["total_ms"] / tot, 4),
                                  "GBps": round(st["bytes_per_launch"] * st["launches"] /
                                                (st["total_ms"] / 1000.0) / 1e9, 1)
-                                 if st["total_ms"] > 0 else 0.0}
+                                 if st["total_ms"] > 0 else 0.0,
+                                 # ncu's FP64-pipe active fraction (profiles/), the bound of the
+                                 # kernels whose HBM fraction is low
+                                 "fp64_pipe_frac_ncu": (ncu_table().get(st["name"]) or {}).get(
+                                     "fp64_pipe_pct", None) if isinstance(
+                                     ncu_table().get(st["name"]), dict) else None}
                     for st in stats},
     }
 
