@@ -263,7 +263,8 @@ def network_roofline(net, w, stream):
     tf = flops / (ms / 1000.0) / 1e12
     del r, lnk, cap, y
     torch.cuda.empty_cache()
-    return {"bound": "tensor", "kernel": "U-Net forward (k_conv3, mma.sync BF16)",
+    return {"bound": "tensor", "kernel": "U-Net forward (k_conv3_tcz / k_conv3_tc: tcgen05.mma "
+                                          "BF16, FP32 accumulators in TMEM)",
             "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
             "peak_source": kind, "ms_per_application": ms, "flop_per_application": flops}
 
@@ -579,7 +580,7 @@ def run_gpu(args):
                                  if st["total_ms"] > 0 else 0.0,
                                  # ncu's FP64-pipe active fraction (profiles/), the bound of the
                                  # kernels whose HBM fraction is low
-                                 "fp64_pipe_frac_ncu": (ncu_table().get(st["name"]) or {}).get(
+                                 "fp64_pipe_pct_ncu": (ncu_table().get(st["name"]) or {}).get(
                                      "fp64_pipe_pct", None) if isinstance(
                                      ncu_table().get(st["name"]), dict) else None}
                     for st in stats},

@@ -24,6 +24,8 @@
 
 #include <cuda_bf16.h>
 
+#include "unet_tc.cuh"
+
 #include <cmath>
 #include <algorithm>
 #include <cstring>
@@ -435,10 +437,63 @@ static int blocks_for(size_t n) {
   return (int)(b < 1 ? 1 : b);
 }
 
+// the error word of the tensor-core convolutions (a bounded wait ran out), one per process
+int* tc_error_word() {
+  static int* w = nullptr;
+  if (!w && cudaMalloc(&w, sizeof(int)) == cudaSuccess) cudaMemset(w, 0, sizeof(int));
+  return w;
+}
+
+// The convolutions of the network (forward and data gradient) run on the tcgen05 kernel.
+// resident blocks per SM of a kernel with `smem` dynamic bytes and `tmem_cols` tensor-memory
+// columns: shared memory (1 KB reserved per block), 16 blocks of 128 threads, and the SM's 512
+// tensor-memory columns shared by its blocks
+static int tc_blocks_per_sm(int smem, int tmem_cols) {
+  int dev = 0, smem_sm = 228 * 1024;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  return std::max(1, std::min({smem_sm / (smem + 128 + 1024), 16, 512 / tmem_cols}));
+}
+
 template <int CIN, int COUT>
 static void conv(const bf16* in, int in_stride, int in_off, const bf16* W, const float* bias,
                  bf16* out, int out_stride, int out_off, int nx, int ny, int nz, bool relu,
                  cudaStream_t st) {
+  if constexpr (TcZShape<CIN, COUT>::FITS) {
+    // weights resident, z columns pipelined
+    using Z = TcZShape<CIN, COUT>;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+      cudaFuncSetAttribute(k_conv3_tcz<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           Z::SMEM);
+      per_sm = tc_blocks_per_sm(Z::SMEM, Z::TMEM_COLS);
+    }
+    const long items = (long)((nx + kTcM - 1) / kTcM) * ny * ((nz + kTcZC - 1) / kTcZC);
+    const int grid = (int)std::min<long>(items, (long)kNumSMs * per_sm);
+    k_conv3_tcz<CIN, COUT><<<grid, 128, Z::SMEM, st>>>(in, in_stride, in_off, W, bias, out,
+                                                       out_stride, out_off, nx, ny, nz,
+                                                       relu ? 1 : 0, tc_error_word());
+    return;
+  }
+  using S = TcShape<CIN, COUT>;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    cudaFuncSetAttribute(k_conv3_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         S::SMEM);
+    per_sm = tc_blocks_per_sm(S::SMEM, S::TMEM_COLS);
+  }
+  const long tiles = (long)((nx + kTcM - 1) / kTcM) * ny * nz;
+  const int grid = (int)std::min<long>(tiles, (long)kNumSMs * per_sm);
+  k_conv3_tc<CIN, COUT><<<grid, 128, S::SMEM, st>>>(in, in_stride, in_off, W, bias, out,
+                                                    out_stride, out_off, nx, ny, nz,
+                                                    relu ? 1 : 0, tc_error_word());
+}
+
+// the same convolution on the mma.sync kernel (the self-check's comparison)
+template <int CIN, int COUT>
+static void conv_sync(const bf16* in, int in_stride, int in_off, const bf16* W,
+                      const float* bias, bf16* out, int out_stride, int out_off, int nx, int ny,
+                      int nz, bool relu, cudaStream_t st) {
   dim3 grid((nx + 15) / 16, (ny + 3) / 4, nz);
   k_conv3<CIN, COUT><<<grid, 128, 0, st>>>(in, in_stride, in_off, W, bias, out, out_stride,
                                            out_off, nx, ny, nz, relu ? 1 : 0);
@@ -697,6 +752,78 @@ int unet_apply(frehg_unet* net, int nx, int ny, int nz, const float* r, const fl
 }
 }  // namespace fg
 
+// tensor-core convolution against the mma.sync one on seeded random inputs (a self-check)
+template <int CIN, int COUT>
+static int conv_check_shape(int in_stride, int in_off, int out_stride, int out_off, int nx,
+                            int ny, int nz, int relu, uint64_t seed, double* max_diff,
+                            double* max_ref) {
+  const size_t n = (size_t)nx * ny * nz;
+  const size_t nin = n * in_stride, nout = n * out_stride, nw = (size_t)27 * CIN * COUT;
+  std::vector<bf16> hin(nin), hw(nw);
+  std::vector<float> hb(COUT);
+  uint64_t s = seed * 0x9E3779B97F4A7C15ull + 7u;
+  for (auto& v : hin) v = __float2bfloat16((float)gauss(s));
+  for (auto& v : hw) v = __float2bfloat16((float)(0.1 * gauss(s)));
+  for (auto& v : hb) v = (float)(0.1 * gauss(s));
+  bf16 *din = nullptr, *dw = nullptr, *o1 = nullptr, *o2 = nullptr;
+  float* db = nullptr;
+  int rc = FREHG_OK;
+  if (cudaMalloc(&din, nin * 2) || cudaMalloc(&dw, nw * 2) || cudaMalloc(&o1, nout * 2) ||
+      cudaMalloc(&o2, nout * 2) || cudaMalloc(&db, COUT * 4)) {
+    set_error("conv check: device allocation");
+    rc = FREHG_ERR_CUDA;
+  }
+  if (rc == FREHG_OK) {
+    cudaMemcpy(din, hin.data(), nin * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(dw, hw.data(), nw * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(db, hb.data(), COUT * 4, cudaMemcpyHostToDevice);
+    cudaMemset(o1, 0, nout * 2);
+    cudaMemset(o2, 0, nout * 2);
+    conv<CIN, COUT>(din, in_stride, in_off, dw, db, o1, out_stride, out_off, nx, ny, nz,
+                    relu != 0, 0);
+    conv_sync<CIN, COUT>(din, in_stride, in_off, dw, db, o2, out_stride, out_off, nx, ny, nz,
+                         relu != 0, 0);
+    const cudaError_t e = cudaDeviceSynchronize();
+    int tc_err = 0;
+    cudaMemcpy(&tc_err, tc_error_word(), sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess || tc_err) {
+      set_error("conv check: %s (tensor-core error word %d)", cudaGetErrorString(e), tc_err);
+      rc = FREHG_ERR_CUDA;
+    }
+  }
+  if (rc == FREHG_OK) {
+    std::vector<bf16> a(nout), b(nout);
+    cudaMemcpy(a.data(), o1, nout * 2, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b.data(), o2, nout * 2, cudaMemcpyDeviceToHost);
+    double md = 0.0, mr = 0.0;
+    for (size_t q = 0; q < nout; ++q) {
+      const double x = __bfloat162float(a[q]), y = __bfloat162float(b[q]);
+      md = std::max(md, std::fabs(x - y));
+      mr = std::max(mr, std::fabs(y));
+    }
+    *max_diff = md;
+    *max_ref = mr;
+  }
+  cudaFree(din);
+  cudaFree(dw);
+  cudaFree(o1);
+  cudaFree(o2);
+  cudaFree(db);
+  return rc;
+}
+
+// the tensor-core convolutions' error word (a bounded wait ran out); checked where the host
+// synchronises anyway
+static int check_tc_error() {
+  int e = 0;
+  FG_CUDA(cudaMemcpy(&e, tc_error_word(), sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    set_error("tensor-core convolution: a bounded wait ran out (%d)", e);
+    return FREHG_ERR_CUDA;
+  }
+  return FREHG_OK;
+}
+
 extern "C" {
 
 int frehg_unet_create(uint64_t seed, frehg_unet** out) {
@@ -802,6 +929,34 @@ int frehg_unet_set_input_scaling(frehg_unet* net, float lnk_mean, float lnk_scal
   return FREHG_OK;
 }
 
+int frehg_unet_conv_check(int cin, int cout, int in_stride, int in_off, int out_stride,
+                          int out_off, int nx, int ny, int nz, int relu, uint64_t seed,
+                          double* max_diff, double* max_ref) {
+  clear_error();
+  FG_ARG(max_diff && max_ref, "null argument");
+  FG_ARG(nx > 0 && ny > 0 && nz > 0 && in_off + cin <= in_stride && out_off + cout <= out_stride &&
+             in_stride % 8 == 0 && in_off % 8 == 0 && out_stride % 8 == 0 && out_off % 8 == 0,
+         "conv check: bad sizes or channel slices");
+#define FG_CONV_CASE(CI, CO)                                                                  \
+  if (cin == CI && cout == CO)                                                                \
+    return conv_check_shape<CI, CO>(in_stride, in_off, out_stride, out_off, nx, ny, nz, relu, \
+                                    seed, max_diff, max_ref);
+  FG_CONV_CASE(16, 16)
+  FG_CONV_CASE(16, 32)
+  FG_CONV_CASE(32, 32)
+  FG_CONV_CASE(32, 64)
+  FG_CONV_CASE(64, 64)
+  FG_CONV_CASE(96, 32)
+  FG_CONV_CASE(48, 16)
+  FG_CONV_CASE(16, 48)
+  FG_CONV_CASE(32, 96)
+  FG_CONV_CASE(64, 32)
+  FG_CONV_CASE(32, 16)
+#undef FG_CONV_CASE
+  set_error("conv check: no convolution of the network has %d -> %d channels", cin, cout);
+  return FREHG_ERR_UNSUPPORTED;
+}
+
 int frehg_unet_forward(frehg_unet* net, int nx, int ny, int nz, const float* r, const float* lnk,
                        const float* cap, float* y, void* stream) {
   clear_error();
@@ -810,7 +965,7 @@ int frehg_unet_forward(frehg_unet* net, int nx, int ny, int nz, const float* r, 
   FG_TRY(ensure_acts(net, nx, ny, nz));
   FG_TRY(forward(net, r, lnk, cap, y, true, st));
   FG_CUDA(cudaStreamSynchronize(st));
-  return FREHG_OK;
+  return check_tc_error();
 }
 
 int frehg_unet_loss_grad(frehg_unet* net, int nx, int ny, int nz, const float* r,
@@ -826,7 +981,7 @@ int frehg_unet_loss_grad(frehg_unet* net, int nx, int ny, int nz, const float* r
   if (grad_host)
     FG_CUDA(cudaMemcpyAsync(grad_host, net->grad, net->nparam * 4, cudaMemcpyDeviceToHost, st));
   FG_CUDA(cudaStreamSynchronize(st));
-  return FREHG_OK;
+  return check_tc_error();
 }
 
 int frehg_unet_set_loss_weight(frehg_unet* net, float weight) {

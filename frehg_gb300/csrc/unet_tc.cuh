@@ -1,0 +1,458 @@
+// The U-Net's 3x3x3 convolutions on the fifth-generation tensor cores (tcgen05, accumulators in
+// tensor memory).  Not in reference.
+//
+// Implicit GEMM per tile of 128 consecutive x pixels of one (y, z) row: D[128 x COUT] (FP32, in
+// TMEM) = sum over the 27 taps and the input channels of A[128 x 16] . B[16 x COUT], one
+// tcgen05.mma.cta_group::1.kind::f16 (BF16 operands, FP32 accumulation, M = 128, N = COUT,
+// K = 16) per tap and 16-channel slice.  Operands sit in shared memory in the no-swizzle
+// K-major core-matrix layout, which the channels-last activations reach by splitting the
+// channels into 8-channel chunks:
+//   input rows  [dy][chunk][pixel][8]  (pixels x0-1 .. x0+128, zero outside the grid):
+//               a tap (dx, dy) is the 128-row view starting at pixel dx of row dy, K-adjacent
+//               core matrices one chunk plane (130 x 16 bytes) apart, M-adjacent ones 128 bytes;
+//   weights     [tap][chunk][o][8]:  N-adjacent core matrices 128 bytes apart, K-adjacent ones
+//               COUT x 16 bytes.
+// A block (one warpgroup) walks its tiles; per tile it loads one z plane of input rows and the
+// nine taps' weights of that plane with 16-byte cp.async copies (zero fill outside the grid),
+// one thread issues the plane's MMAs and commits them to an mbarrier, and the block waits for
+// them before the next plane's copies reuse the buffers.  The four warps then read the
+// accumulator lanes (tcgen05.ld 32x32b: warp w owns lanes 32w .. 32w+31 = pixels), add the bias,
+// apply the ReLU and store BF16.  Several blocks per SM (shared memory, tensor-memory columns
+// permitting) overlap one block's copies with another's MMAs.
+//
+// Every wait is bounded: a wait that runs out records an error word and the block stops
+// issuing work, waits (bounded) for its MMAs in flight, frees its tensor memory and returns.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+namespace fg {
+namespace unet {
+
+constexpr int kTcM = 128;       // pixels per tile
+constexpr int kTcP = kTcM + 2;  // with the x halo
+constexpr long kTcSpin = 1L << 24;
+
+template <int CIN, int COUT>
+struct TcShape {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 128, "channel counts");
+  static constexpr int CH = CIN / 8;
+  static constexpr int PLANE = kTcP * 16;              // one chunk plane of a row
+  static constexpr int ROWS = 3 * CH * PLANE;          // dy = -1, 0, 1
+  static constexpr int WTS = 9 * CH * COUT * 16;       // the nine taps of one z plane
+  static constexpr int SMEM = ROWS + WTS + 128;        // + alignment slack
+  static constexpr int TMEM_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
+};
+
+__device__ __forceinline__ uint32_t tc_smem(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: start, leading (K) and stride (M / N) byte offsets, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of the fifth-generation tensor cores
+  return d;                // base offset 0, absolute leading offset, layout: no swizzle
+}
+
+// instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t tc_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_cp16(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc_smem(dst)), "l"(src),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
+  for (long q = 0; q < kTcSpin; ++q) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(tc_smem(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restrict__ in,
+                                                  int in_stride, int in_off,
+                                                  const __nv_bfloat16* __restrict__ W,
+                                                  const float* __restrict__ bias,
+                                                  __nv_bfloat16* __restrict__ out, int out_stride,
+                                                  int out_off, int nx, int ny, int nz, int relu,
+                                                  int* err) {
+  using S = TcShape<CIN, COUT>;
+  extern __shared__ __align__(128) unsigned char tc_dyn[];
+  unsigned char* rows = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(tc_dyn) + 127) & ~static_cast<uintptr_t>(127));
+  unsigned char* wts = rows + S::ROWS;
+  __shared__ __align__(8) uint64_t mma_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_word;
+  volatile int& abort_flag = abort_word;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc_smem(&tmem_slot)),
+                 "r"(S::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mma_bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_word = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t rows_s = tc_smem(rows), wts_s = tc_smem(wts);
+  constexpr uint32_t idesc = tc_idesc(COUT);
+  uint32_t phase = 0;
+  int pending = 0;  // MMAs committed and not yet waited for
+
+  const int xt = (nx + kTcM - 1) / kTcM;
+  const long tiles = (long)xt * ny * nz;
+  for (long tile = blockIdx.x; tile < tiles && !abort_flag; tile += gridDim.x) {
+    const int x0 = (int)(tile % xt) * kTcM;
+    const long yz = tile / xt;
+    const int y = (int)(yz % ny), z = (int)(yz / ny);
+    bool first = true;
+    for (int dz = -1; dz <= 1 && !abort_flag; ++dz) {
+      const int zz = z + dz;
+      if (zz < 0 || zz >= nz) continue;  // zero padding: the plane adds nothing
+      // the plane's three input rows, [dy][chunk][pixel][8]
+      for (int q = tid; q < 3 * S::CH * kTcP; q += 128) {
+        const int p = q % kTcP, c = (q / kTcP) % S::CH, dy = q / (kTcP * S::CH);
+        const int yy = y + dy - 1, xx = x0 + p - 1;
+        const bool ok = yy >= 0 && yy < ny && xx >= 0 && xx < nx;
+        const __nv_bfloat16* src =
+            ok ? in + ((size_t)xx + (size_t)nx * ((size_t)yy + (size_t)ny * zz)) * in_stride +
+                     in_off + 8 * c
+               : in;
+        tc_cp16(rows + ((dy * S::CH + c) * kTcP + p) * 16, src, ok ? 16 : 0);
+      }
+      // the plane's nine taps of W[tap][o][i], [tap][chunk][o][8]
+      for (int q = tid; q < 9 * S::CH * COUT; q += 128) {
+        const int o = q % COUT, c = (q / COUT) % S::CH, t9 = q / (COUT * S::CH);
+        const int tap = (dz + 1) * 9 + t9;
+        tc_cp16(wts + ((t9 * S::CH + c) * COUT + o) * 16, W + ((size_t)tap * COUT + o) * CIN + 8 * c,
+                16);
+      }
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      // the copies are generic-proxy writes the tensor cores read through the async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+#pragma unroll 1
+        for (int t9 = 0; t9 < 9; ++t9) {
+          const int dy = t9 / 3, dx = t9 % 3;
+#pragma unroll
+          for (int kc = 0; kc < CIN / 16; ++kc) {
+            const uint64_t a = tc_desc(rows_s + ((dy * S::CH + 2 * kc) * kTcP + dx) * 16,
+                                       S::PLANE, 128);
+            const uint64_t b = tc_desc(wts_s + (t9 * S::CH + 2 * kc) * COUT * 16, COUT * 16, 128);
+            const uint32_t acc = first ? 0u : 1u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                : "memory");
+            first = false;
+          }
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                tc_smem(&mma_bar))
+            : "memory");
+      }
+      first = false;
+      pending = 1;
+      // the plane's MMAs read the buffers the next plane's copies overwrite (the outcome of the
+      // wait is made block-uniform, so every thread takes the same path)
+      const bool late = __syncthreads_or(!tc_wait(&mma_bar, phase));
+      if (late) {
+        if (tid == 0) atomicExch(err, 1);
+        abort_flag = 1;
+        break;
+      }
+      pending = 0;
+      phase ^= 1u;
+    }
+    if (abort_flag) break;
+    // epilogue: warp w reads TMEM lanes 32w .. 32w+31 (its 32 pixels), 16 columns at a time
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int px = x0 + warp * 32 + lane;
+    __nv_bfloat16* dst =
+        out + ((size_t)px + (size_t)nx * ((size_t)y + (size_t)ny * z)) * out_stride + out_off;
+#pragma unroll
+    for (int cb = 0; cb < COUT; cb += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+          "%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      uint32_t packed[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float v0 = __uint_as_float(r[2 * q]) + (bias ? bias[cb + 2 * q] : 0.f);
+        float v1 = __uint_as_float(r[2 * q + 1]) + (bias ? bias[cb + 2 * q + 1] : 0.f);
+        if (relu) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+        packed[q] = *reinterpret_cast<uint32_t*>(&h);
+      }
+      if (px < nx) {
+        uint4* d4 = reinterpret_cast<uint4*>(dst + cb);
+        d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+      }
+    }
+  }
+  // MMAs still in flight (a wait that ran out) finish before the tensor memory is freed
+  if (pending) (void)tc_wait(&mma_bar, phase);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(S::TMEM_COLS)
+                 : "memory");
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Pipelined form for the layers whose 27 taps of weights stay resident in shared memory
+// (27 x CIN x COUT x 2 bytes <= 64 KB: all level-1 layers and the narrower level-2 ones).
+// A block walks columns of ZC tiles along z at one (x tile, y): a ring of four slots holds
+// input planes (three rows each, [slot][dy][chunk][pixel][8]); each tile needs one new plane,
+// loaded one tile ahead with cp.async while the previous tile's MMAs run, and two tensor-memory
+// accumulators let the epilogue of tile z-1 overlap the MMAs of tile z:
+//   wait for plane z+1, barrier; issue MMA(z) -> acc[z&1], commit;
+//   wait MMA(z-1); epilogue(z-1) from acc[(z-1)&1];
+//   load plane z+2 into the slot of plane z-2 (free: MMA(z-1) was its last reader).
+constexpr int kTcZC = 16;  // tiles of one z column
+
+template <int CIN, int COUT>
+struct TcZShape {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
+  static constexpr int CH = CIN / 8;
+  static constexpr int PLANE = kTcP * 16;
+  static constexpr int SLOT = 3 * CH * PLANE;          // one input plane: rows dy = -1, 0, 1
+  static constexpr int WTS = 27 * CH * COUT * 16;      // all taps, [tap][chunk][o][8]
+  static constexpr int SMEM = WTS + 4 * SLOT + 128;
+  static constexpr int ACC_COLS = COUT <= 16 ? 16 : (COUT <= 32 ? 32 : 64);
+  static constexpr int TMEM_COLS = 2 * ACC_COLS < 32 ? 32 : 2 * ACC_COLS;
+  static constexpr bool FITS = WTS <= 64 * 1024 && COUT <= 64;
+};
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restrict__ in,
+                                                   int in_stride, int in_off,
+                                                   const __nv_bfloat16* __restrict__ W,
+                                                   const float* __restrict__ bias,
+                                                   __nv_bfloat16* __restrict__ out,
+                                                   int out_stride, int out_off, int nx, int ny,
+                                                   int nz, int relu, int* err) {
+  using S = TcZShape<CIN, COUT>;
+  extern __shared__ __align__(128) unsigned char tcz_dyn[];
+  unsigned char* wts = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(tcz_dyn) + 127) & ~static_cast<uintptr_t>(127));
+  unsigned char* ring = wts + S::WTS;
+  __shared__ __align__(8) uint64_t mma_bar[2];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc_smem(&tmem_slot)),
+                 "r"(S::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mma_bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mma_bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // all 27 taps of the weights, once per block
+  for (int q = tid; q < 27 * S::CH * COUT; q += 128) {
+    const int o = q % COUT, c = (q / COUT) % S::CH, tap = q / (COUT * S::CH);
+    tc_cp16(wts + ((tap * S::CH + c) * COUT + o) * 16, W + ((size_t)tap * COUT + o) * CIN + 8 * c,
+            16);
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t wts_s = tc_smem(wts), ring_s = tc_smem(ring);
+  constexpr uint32_t idesc = tc_idesc(COUT);
+  uint32_t phase[2] = {0u, 0u};
+  int outstanding[2] = {0, 0};  // MMAs committed to mma_bar[b] and not yet waited for
+  bool failed = false;
+
+  // copies of input plane zz (three rows) into ring slot zz & 3, zero outside the grid
+  auto load_plane = [&](int x0, int y, int zz) {
+    unsigned char* slot = ring + (zz & 3) * S::SLOT;
+    const bool zok = zz >= 0 && zz < nz;
+    for (int q = tid; q < 3 * S::CH * kTcP; q += 128) {
+      const int p = q % kTcP, c = (q / kTcP) % S::CH, dy = q / (kTcP * S::CH);
+      const int yy = y + dy - 1, xx = x0 + p - 1;
+      const bool ok = zok && yy >= 0 && yy < ny && xx >= 0 && xx < nx;
+      const __nv_bfloat16* src =
+          ok ? in + ((size_t)xx + (size_t)nx * ((size_t)yy + (size_t)ny * zz)) * in_stride +
+                   in_off + 8 * c
+             : in;
+      tc_cp16(slot + ((dy * S::CH + c) * kTcP + p) * 16, src, ok ? 16 : 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  // bias + ReLU + BF16 store of tile (x0, y, z) from accumulator b
+  auto epilogue = [&](int x0, int y, int z, int b) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int px = x0 + warp * 32 + lane;
+    __nv_bfloat16* dst =
+        out + ((size_t)px + (size_t)nx * ((size_t)y + (size_t)ny * z)) * out_stride + out_off;
+#pragma unroll
+    for (int cb = 0; cb < COUT; cb += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+          "%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * S::ACC_COLS + cb)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      uint32_t packed[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float v0 = __uint_as_float(r[2 * q]) + (bias ? bias[cb + 2 * q] : 0.f);
+        float v1 = __uint_as_float(r[2 * q + 1]) + (bias ? bias[cb + 2 * q + 1] : 0.f);
+        if (relu) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+        packed[q] = *reinterpret_cast<uint32_t*>(&h);
+      }
+      if (px < nx) {
+        uint4* d4 = reinterpret_cast<uint4*>(dst + cb);
+        d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  };
+  // block-uniform bounded wait for the MMAs committed to mma_bar[b]
+  auto wait_mma = [&](int b) -> bool {
+    const bool late = __syncthreads_or(!tc_wait(&mma_bar[b], phase[b]));
+    if (late) {
+      if (tid == 0) atomicExch(err, 2);
+      return false;
+    }
+    phase[b] ^= 1u;
+    outstanding[b] = 0;
+    return true;
+  };
+
+  const int xt = (nx + kTcM - 1) / kTcM;
+  const int zcols = (nz + kTcZC - 1) / kTcZC;
+  const long items = (long)xt * ny * zcols;
+  for (long item = blockIdx.x; item < items && !failed; item += gridDim.x) {
+    const int x0 = (int)(item % xt) * kTcM;
+    const long rest = item / xt;
+    const int y = (int)(rest % ny);
+    const int zb = (int)(rest / ny) * kTcZC, ze = min(nz, zb + kTcZC);
+    load_plane(x0, y, zb - 1);
+    load_plane(x0, y, zb);
+    load_plane(x0, y, zb + 1);
+    for (int z = zb; z < ze; ++z) {
+      const int b = z & 1;
+      // planes z-1, z, z+1 (and, the first time, the weights) have landed
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+        bool first = true;
+#pragma unroll 1
+        for (int t = 0; t < 27; ++t) {
+          const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
+          const int zz = z + dz - 1;
+          if (zz < 0 || zz >= nz) continue;  // zero padding
+          const uint32_t slot_s = ring_s + (uint32_t)((zz & 3) * S::SLOT);
+#pragma unroll
+          for (int kc = 0; kc < CIN / 16; ++kc) {
+            const uint64_t a = tc_desc(slot_s + ((dy * S::CH + 2 * kc) * kTcP + dx) * 16,
+                                       S::PLANE, 128);
+            const uint64_t bd = tc_desc(wts_s + (t * S::CH + 2 * kc) * COUT * 16, COUT * 16, 128);
+            const uint32_t acc = first ? 0u : 1u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                    tmem + (uint32_t)(b * S::ACC_COLS)),
+                "l"(a), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+            first = false;
+          }
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                tc_smem(&mma_bar[b]))
+            : "memory");
+      }
+      outstanding[b] = 1;
+      if (z > zb) {  // the previous tile: its MMAs were the last readers of plane z-2's slot
+        if (!wait_mma(b ^ 1)) {
+          failed = true;
+          break;
+        }
+        epilogue(x0, y, z - 1, b ^ 1);
+      }
+      if (z + 1 < ze) load_plane(x0, y, z + 2);
+    }
+    if (failed) break;
+    if (!wait_mma((ze - 1) & 1)) {
+      failed = true;
+      break;
+    }
+    epilogue(x0, y, ze - 1, (ze - 1) & 1);
+    __syncthreads();  // the next column's first copies reuse slots the last epilogue's MMAs read
+  }
+  // MMAs still in flight after a wait that ran out finish before the tensor memory is freed
+  for (int b = 0; b < 2; ++b)
+    if (outstanding[b]) (void)tc_wait(&mma_bar[b], phase[b]);
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(S::TMEM_COLS)
+                 : "memory");
+}
+
+}  // namespace unet
+}  // namespace fg

@@ -402,6 +402,16 @@ int frehg_fastmath_eval(int fn, const double* x, double* y, int64_t n);
 int frehg_constit_eval(const frehg_soil_params* soil, int arith, int continuous_theta,
                        const double* h, int64_t n, double* kr, double* wc, double* cap);
 
+/* Self-check of the network's tensor-core convolutions (not in reference): one 3x3x3
+ * convolution of cin -> cout channels (a shape the network uses) on seeded random BF16 inputs,
+ * by the tcgen05 kernel the network runs and by a warp-level mma.sync kernel; stores the largest
+ * absolute difference of the two BF16 outputs and the largest output magnitude.  in_stride /
+ * out_stride and in_off / out_off select channel slices of wider pixel records, as the
+ * network's concatenations do. */
+int frehg_unet_conv_check(int cin, int cout, int in_stride, int in_off, int out_stride,
+                          int out_off, int nx, int ny, int nz, int relu, uint64_t seed,
+                          double* max_diff, double* max_ref);
+
 /* Self-check of the TMA-staged Picard assembly (not in reference): on the handle's current
  * state (a Picard handle in mixed precision, soil with a per-cell Ks field, even nx -- the case
  * the step stages through the Tensor Memory Accelerator), assembles the system once with the

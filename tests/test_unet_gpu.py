@@ -65,6 +65,31 @@ def test_forward_and_gradients_match_reference(gpu_lib, shape):
     gpu_lib.frehg_unet_destroy(h)
 
 
+# (cin, cout, in_stride, in_off, out_stride, out_off): every convolution shape of the network,
+# forward and data gradient, with the channel slices of its concatenations
+CONV_SHAPES = [(16, 16, 16, 0, 16, 0), (16, 16, 48, 32, 48, 32), (16, 32, 16, 0, 32, 0),
+               (32, 32, 96, 64, 96, 64), (32, 64, 32, 0, 64, 0), (64, 64, 64, 0, 64, 0),
+               (96, 32, 96, 0, 32, 0), (48, 16, 48, 0, 16, 0), (16, 48, 16, 0, 48, 0),
+               (32, 96, 32, 0, 96, 0), (64, 32, 64, 0, 32, 0), (32, 16, 32, 0, 16, 0)]
+
+
+@pytest.mark.parametrize("grid", [(136, 3, 2), (20, 5, 4), (256, 2, 1), (40, 3, 37)])
+@pytest.mark.parametrize("shape", CONV_SHAPES)
+def test_tensor_core_conv_matches_mma_sync(gpu_lib, shape, grid):
+    """The tcgen05 convolution (TMEM accumulators, shared-memory operand descriptors) against
+    the warp-level mma.sync one on the same BF16 inputs: the FP32 sums differ only in order, so
+    the BF16 outputs agree to a rounding step (2^-8 relative) of the output scale.  Grids with a
+    partial 128-pixel tile, rows shorter than a tile and single planes."""
+    cin, cout, ins, ino, outs, outo = shape
+    nx, ny, nz = grid
+    diff, ref = C.c_double(), C.c_double()
+    rc = gpu_lib.frehg_unet_conv_check(cin, cout, ins, ino, outs, outo, nx, ny, nz, 1, 17,
+                                       C.byref(diff), C.byref(ref))
+    assert rc == 0, gpu_lib.frehg_last_error()
+    assert ref.value > 0.0
+    assert diff.value <= 2.0 ** -7 * ref.value, (diff.value, ref.value)
+
+
 def test_adam_lowers_the_loss(gpu_lib):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(2)
