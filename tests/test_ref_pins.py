@@ -5,7 +5,7 @@ GwFields.hpp), src/linear/DomainDecomposition.cpp, src/core/{Grid,MpiComm}.cpp a
 src/soil/SoilMap.cpp from the reference tree, against single-rank Kokkos/MPI shims; PETSc's
 KSPSolve is the one part stood in for (by the oracle's restatement of it, pinned by
 test_oracle_pins.py's manufactured-solution tests).  Every comparison here is bit for bit: all
-fifteen halo fields the step writes, the dt sequence and the Krylov iteration counts.
+nineteen halo fields the step writes, the dt sequence and the Krylov iteration counts.
 
 These tests need the reference tree (present in the development container, absent on the GPU
 machine); tests/golden/ carries the reference's outputs to the GPU tests.
