@@ -101,6 +101,56 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   return fast_two_sum(c.h, __fadd_rn(c.l, __fmaf_rn(a.l, b.h, t)));
 }
 
+// ---- lean forms: no renormalisation -------------------------------------------------------
+// For chains of sums and products whose end result is renormalised once.  Their results keep
+// |lo| within a few ulp of hi when their inputs do, which the error bounds of the next lean
+// operation allow for (a few 2^-48 relative, as the renormalised forms); a value that leaves
+// float-float (ff_to_double, a comparison) passes through a renormalising operation first.
+
+// a b: TwoProd of the leading words plus the two cross terms (a.l b.l, below 2^-46 of the
+// product, is dropped)
+__device__ __forceinline__ ff ff_mul_lean(ff a, ff b) {
+  const ff c = two_prod(a.h, b.h);
+  return ff_make(c.h, __fadd_rn(c.l, __fmaf_rn(a.l, b.h, __fmul_rn(a.h, b.l))));
+}
+
+// a - b: TwoSum of the leading words, the low words' difference added to its error term;
+// antisymmetric, ff_dif_lean(a, b) = -ff_dif_lean(b, a) exactly (TwoSum's error is exact and
+// rounding to nearest is symmetric)
+__device__ __forceinline__ ff ff_dif_lean(ff a, ff b) {
+  const ff s = two_sum(a.h, -b.h);
+  return ff_make(s.h, __fadd_rn(s.l, __fsub_rn(a.l, b.l)));
+}
+
+// a + b
+__device__ __forceinline__ ff ff_add_lean(ff a, ff b) {
+  const ff s = two_sum(a.h, b.h);
+  return ff_make(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+
+// A running sum of float-float terms: the leading words are summed with TwoSum and every error
+// term and low word is collected in one float, so the absolute error is a few 2^-48 of the
+// largest term (as a chain of SloppyDWPlusDW, at 8 instead of 11 instructions a term).
+struct FfSum {
+  float s, e;
+};
+
+__device__ __forceinline__ FfSum ff_sum_of(ff x) {
+  FfSum q;
+  q.s = x.h;
+  q.e = x.l;
+  return q;
+}
+
+__device__ __forceinline__ void ff_sum_add(FfSum& q, ff x) {
+  const ff t = two_sum(q.s, x.h);
+  q.s = t.h;
+  q.e = __fadd_rn(q.e, __fadd_rn(t.l, x.l));
+}
+
+// the sum, renormalised (TwoSum of the two words)
+__device__ __forceinline__ ff ff_sum_value(const FfSum& q) { return two_sum(q.s, q.e); }
+
 __device__ __forceinline__ ff ff_sqr(ff a) {
   const ff c = two_prod(a.h, a.h);
   return fast_two_sum(c.h, __fmaf_rn(__fmul_rn(2.0f, a.h), a.l, c.l));
@@ -130,11 +180,14 @@ static __device__ __noinline__ double ff_to_double_rare(ff a) { return (double)a
 // significand (truncated), lo = the next 29 bits (rounded to 24 by the int->float conversion),
 // renormalised.  Values below 2^-100 or above 2^127 in magnitude (and 0, inf, NaN) take the
 // conversion instructions instead.
-__device__ __forceinline__ ff ff_from_double(double x) {
+// The split without the final renormalisation: hi the truncated leading 24 bits, 0 <= |lo| <
+// ulp(hi), lo of the sign of hi (a lean operand).
+__device__ __forceinline__ ff ff_from_double_lean(double x) {
   const int hx = __double2hiint(x);
   const int lx = __double2loint(x);
   const int E = (hx >> 20) & 0x7ff;
-  if (E < 1023 - 100 || E > 1023 + 127) return ff_from_double_rare(x);
+  // one unsigned compare for 1023 - 100 <= E <= 1023 + 127
+  if ((unsigned)(E - (1023 - 100)) > 227u) return ff_from_double_rare(x);
   const int sign = hx & (int)0x80000000;
   const float h = __int_as_float(sign | ((E - 1023 + 127) << 23) | ((hx & 0x000fffff) << 3) |
                                  (int)((unsigned)lx >> 29));
@@ -142,7 +195,12 @@ __device__ __forceinline__ ff ff_from_double(double x) {
   const float p2 = __int_as_float((E - 1023 + 127) << 23);
   float l = __fmul_rn(__fmul_rn(__uint2float_rn((unsigned)lx & 0x1fffffffu), 0x1p-52f), p2);
   l = __int_as_float(__float_as_int(l) | sign);
-  return fast_two_sum(h, l);
+  return ff_make(h, l);
+}
+
+__device__ __forceinline__ ff ff_from_double(double x) {
+  const ff r = ff_from_double_lean(x);
+  return fast_two_sum(r.h, r.l);
 }
 
 // x rounded to a float (to nearest, ties away from zero) without a double->float conversion:

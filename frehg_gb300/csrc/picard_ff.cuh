@@ -1,19 +1,22 @@
 // Float-float forms of the Picard assembly and of the conservative final update (not in
 // reference): the same faces, boundary closures, residual and update as k_pic_assemble /
 // k_pic_final (picard.cuh), with every FP64 operation replaced by float-float arithmetic on
-// the FP32 pipe (ff32.cuh; about 48 significant bits), in one tiled kernel with two modes.  GB300 runs FP64 at 1/73 of the FP32
-// rate, and the FP64 forms of these kernels are bound by that pipe, not by memory.
+// the FP32 pipe (ff32.cuh; about 48 significant bits), in one tiled kernel with two modes.
+// GB300 runs FP64 at 1/73 of the FP32 rate, and the FP64 forms of these kernels are bound by
+// that pipe, not by memory.
 //
 // Doubles are read and split into float-float with integer operations; results are written
 // back as doubles.  The Picard residual's storage difference (theta(h^m) - theta^n of the two
-// stored doubles) and its final combination stay in FP64.  The matrix (diagonal and couplings) is formed from the leading floats of
-// the float-float transmissibilities: it shapes each Picard update, not the fixed point the
-// iteration converges to, and the mixed-precision solve rounds it to FP32 anyway.  Sums use
-// the double-word addition whose error is a few 2^-48 of the operands (not of the result): the
-// residual, which fixes the iteration's fixed point, needs absolute accuracy relative to its
-// largest terms.  The face fluxes of two neighbouring cells are exact negatives of each other
-// (the face mean takes its arguments in index order, the head difference changes sign
-// exactly), so the water budget of the final update closes to rounding as in FP64.
+// stored doubles) and its final combination stay in FP64.  The matrix (diagonal and
+// couplings) is formed from the leading floats of the float-float transmissibilities: it
+// shapes each Picard update, not the fixed point the iteration converges to, and the
+// mixed-precision solve rounds it to FP32 anyway.  The face fluxes are chains of the lean
+// operations (no renormalisation between steps) summed in an FfSum, whose error is a few
+// 2^-48 of the largest term (not of the result): the residual, which fixes the iteration's
+// fixed point, needs absolute accuracy relative to its largest terms.  The face fluxes of two
+// neighbouring cells are exact negatives of each other (the face mean takes its arguments in
+// index order, the head difference changes sign exactly), so the water budget of the final
+// update closes to rounding as in FP64.
 #pragma once
 
 #include "picard.cuh"
@@ -41,40 +44,60 @@ __device__ __forceinline__ ff ff_ks(const ReArgs& a, const SoilClass& k, size_t 
   return ff_make(k.ff_ks[d][0], k.ff_ks[d][1]);
 }
 
+// a cell's conductivity Ks kr (lean: the face sums take it)
+__device__ __forceinline__ ff ff_cond(ff ks, ff kr) { return ff_mul_lean(ks, kr); }
+
 // ISO: one conductivity serves all three axes (a per-cell Ks field, or isotropic classes
 // only); the cell then carries kx alone
+// Head, kr and Ks enter as lean splits (ff_from_double_lean): only the face sums read them.
 template <bool ISO = false>
 __device__ __forceinline__ FfCell ff_cell(const ReArgs& a, size_t c, size_t col) {
-  const ff kr = ff_from_double(a.kr[c]);
+  const ff kr = ff_from_double_lean(a.kr[c]);
   FfCell r;
-  r.h = ff_from_double(a.h_new[c]);
+  r.h = ff_from_double_lean(a.h_new[c]);
   if (ISO) {
     if (a.soil.Ks) {
-      r.kx = ff_mul(ff_from_double(a.soil.Ks[c]), kr);
+      r.kx = ff_cond(ff_from_double_lean(a.soil.Ks[c]), kr);
     } else {
       const SoilClass& k = class_of(a, c, col);
-      r.kx = ff_mul(ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
+      r.kx = ff_cond(ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
     }
     return r;
   }
   const SoilClass& k = class_of(a, c, col);
   if (a.soil.Ks || k.ks_iso) {
-    r.kx = ff_mul(ff_ks(a, k, c, 0), kr);
+    r.kx = ff_cond(a.soil.Ks ? ff_from_double_lean(a.soil.Ks[c])
+                             : ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
     r.ky = r.kx;
     r.kz = r.kx;
   } else {
-    r.kx = ff_mul(ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
-    r.ky = ff_mul(ff_make(k.ff_ks[1][0], k.ff_ks[1][1]), kr);
-    r.kz = ff_mul(ff_make(k.ff_ks[2][0], k.ff_ks[2][1]), kr);
+    r.kx = ff_cond(ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
+    r.ky = ff_cond(ff_make(k.ff_ks[1][0], k.ff_ks[1][1]), kr);
+    r.kz = ff_cond(ff_make(k.ff_ks[2][0], k.ff_ks[2][1]), kr);
   }
   return r;
 }
 
-// pic_mean of two non-negative conductivities (lower index first)
+// pic_mean of two non-negative conductivities (lower index first); lean
 __device__ __forceinline__ ff ff_face_mean(int harmonic, ff lo, ff hi) {
-  const ff s = ff_add_fast(lo, hi);
+  const ff s = ff_add_lean(lo, hi);
   if (!harmonic) return ff_scale(s, 0.5f);
   return s.h > 0.0f ? ff_scale(ff_div(ff_mul(lo, hi), s), 2.0f) : ff_make(0.0f);
+}
+
+// The flux into a cell of head h from its neighbour of head hn through a face of conductance kf
+// and geometric factor g (area / distance), kf g (hn - h), lean; *t = the face's
+// transmissibility kf g (leading float: the matrix entry's factor).  Antisymmetric in (hn, h).
+__device__ __forceinline__ ff ff_face_flux(ff kf, ff g, ff hn, ff h, float* t) {
+  const ff tt = ff_mul_lean(kf, g);
+  *t = tt.h;
+  return ff_mul_lean(tt, ff_dif_lean(hn, h));
+}
+
+// The flux into the upper cell (head hu) from the lower one (head hd) through their common z
+// face, gravity included: kf cz (hd - hu) - Az kf.  The lower cell adds its exact negative.
+__device__ __forceinline__ ff ff_zface_flux(ff kf, ff cz, ff Az, ff hd, ff hu, float* t) {
+  return ff_dif_lean(ff_face_flux(kf, cz, hd, hu, t), ff_mul_lean(Az, kf));
 }
 
 __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
@@ -150,6 +173,15 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
   }
 }
 
+// The Picard residual's float-float part V Ss (wcn/ths) (h - h_old) - dt q, renormalised (the
+// storage difference and the final combination are FP64)
+__device__ __forceinline__ ff ff_residual_rest(ff V, ff dt, ff st, ff h, double h_old, ff q) {
+  const ff dh = ff_dif_lean(h, ff_from_double_lean(h_old));
+  FfSum r = ff_sum_of(ff_mul_lean(V, ff_mul_lean(st, dh)));
+  ff_sum_add(r, ff_neg(ff_mul_lean(dt, q)));
+  return ff_sum_value(r);
+}
+
 // One level of a (32 x 8)-column tile plus the rows above and below it: the head and the
 // axis-1 conductivity of each cell, float-float (the y faces read their neighbours here).
 struct FfYPlane {
@@ -213,12 +245,10 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
     float tzm = 0.0f;  // and that face's transmissibility (leading float)
     if (act && kb < ke) {
       cur = ff_cell<ISO>(a, col + a.ncol * kb, col);
-      if (kb > 0) {
+      if (kb > 0) {  // the face above the slab, as the slab above forms it (negated)
         const FfCell up = ff_cell<ISO>(a, col + a.ncol * (kb - 1), col);
         const ff kf = ff_face_mean(hm, cell_kz<ISO>(up), cell_kz<ISO>(cur));
-        const ff t = ff_mul(kf, K.cz);
-        tzm = t.h;
-        fzm = ff_add_fast(ff_mul(t, ff_dif(up.h, cur.h)), ff_mul(K.Az, kf));
+        fzm = ff_neg(ff_zface_flux(kf, K.cz, K.Az, cur.h, up.h, &tzm));
       }
     }
     for (int k = kb; k < ke; ++k) {
@@ -280,9 +310,7 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
           Kxn = ff_make(P.xkh[row][1], P.xkl[row][1]);
           hxn = ff_make(P.xhh[row][1], P.xhl[row][1]);
         }
-        const ff t = ff_mul(ff_face_mean(hm, cur.kx, Kxn), K.cx);
-        tx = t.h;
-        fxp = ff_mul(t, ff_dif(hxn, cur.h));
+        fxp = ff_face_flux(ff_face_mean(hm, cur.kx, Kxn), K.cx, hxn, cur.h, &tx);
       }
       // -x face: the previous lane's +x face (lane 0 evaluates its own)
       float txm = __shfl_up_sync(full, tx, 1);
@@ -295,38 +323,37 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
         } else if (lane == 0) {
           const ff kxm = ff_make(P.xkh[row][0], P.xkl[row][0]);
           const ff hxm = ff_make(P.xhh[row][0], P.xhl[row][0]);
-          const ff t = ff_mul(ff_face_mean(hm, kxm, cur.kx), K.cx);
-          txm = t.h;
-          fxm = ff_mul(t, ff_dif(hxm, cur.h));
+          fxm = ff_face_flux(ff_face_mean(hm, kxm, cur.kx), K.cx, hxm, cur.h, &txm);
         }
-        ff q = ff_add_fast(fxm, fxp);
+        FfSum q = ff_sum_of(fxm);
+        ff_sum_add(q, fxp);
         float tsum = txm + tx;
         // y faces from the staged neighbours
         float ty = 0.0f;
         if (j > 0) {
           const ff hn = ff_make(P.hh[row][lane], P.hl[row][lane]);
           const ff kn = ff_make(P.kh[row][lane], P.kl[row][lane]);
-          const ff t = ff_mul(ff_face_mean(hm, kn, cell_ky<ISO>(cur)), K.cy);
-          q = ff_add_fast(q, ff_mul(t, ff_dif(hn, cur.h)));
-          tsum += t.h;
+          float t;
+          const ff kf = ff_face_mean(hm, kn, cell_ky<ISO>(cur));
+          ff_sum_add(q, ff_face_flux(kf, K.cy, hn, cur.h, &t));
+          tsum += t;
         }
         if (j + 1 < a.ny) {
           const ff hn = ff_make(P.hh[row + 2][lane], P.hl[row + 2][lane]);
           const ff kn = ff_make(P.kh[row + 2][lane], P.kl[row + 2][lane]);
-          const ff t = ff_mul(ff_face_mean(hm, cell_ky<ISO>(cur), kn), K.cy);
-          ty = t.h;
-          q = ff_add_fast(q, ff_mul(t, ff_dif(hn, cur.h)));
+          const ff kf = ff_face_mean(hm, cell_ky<ISO>(cur), kn);
+          ff_sum_add(q, ff_face_flux(kf, K.cy, hn, cur.h, &ty));
           tsum += ty;
         }
         const SoilClass& kc = class_of(a, c, col);
         // face above: carried, or the top boundary
         if (k > 0) {
-          q = ff_add_fast(q, fzm);
+          ff_sum_add(q, fzm);
           tsum += tzm;
         } else {
           ff f, t;
           ff_top_face(a, K, cur, kc, c, col, &f, &t);
-          q = ff_add_fast(q, f);
+          ff_sum_add(q, f);
           tsum += t.h;
           if (FINAL) vol[0] += ff_to_double(ff_mul(f, K.dt));
         }
@@ -334,40 +361,39 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
         float tz = 0.0f;
         if (has_below) {
           const SoilClass& kb = a.soil.cls[rb_id];
-          const ff kr = ff_from_double(rb_kr);
-          below.h = ff_from_double(rb_h);
+          const ff kr = ff_from_double_lean(rb_kr);
+          below.h = ff_from_double_lean(rb_h);
           if (ISO || a.soil.Ks || kb.ks_iso) {
-            below.kx = ff_mul(a.soil.Ks ? ff_from_double(rb_ks)
-                                        : ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
+            below.kx = ff_cond(a.soil.Ks ? ff_from_double_lean(rb_ks)
+                                         : ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
             if (!ISO) {
               below.ky = below.kx;
               below.kz = below.kx;
             }
           } else {
-            below.kx = ff_mul(ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
-            below.ky = ff_mul(ff_make(kb.ff_ks[1][0], kb.ff_ks[1][1]), kr);
-            below.kz = ff_mul(ff_make(kb.ff_ks[2][0], kb.ff_ks[2][1]), kr);
+            below.kx = ff_cond(ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
+            below.ky = ff_cond(ff_make(kb.ff_ks[1][0], kb.ff_ks[1][1]), kr);
+            below.kz = ff_cond(ff_make(kb.ff_ks[2][0], kb.ff_ks[2][1]), kr);
           }
           const ff kf = ff_face_mean(hm, cell_kz<ISO>(cur), cell_kz<ISO>(below));
-          const ff t = ff_mul(kf, K.cz);
-          tz = t.h;
-          const ff fz = ff_dif(ff_mul(t, ff_dif(below.h, cur.h)), ff_mul(K.Az, kf));
-          q = ff_add_fast(q, fz);
+          const ff fz = ff_zface_flux(kf, K.cz, K.Az, below.h, cur.h, &tz);
+          ff_sum_add(q, fz);
           tsum += tz;
           tzm = tz;
           fzm = ff_neg(fz);
         } else {
           ff f, t;
           ff_bottom_face<ISO>(a, K, cur, c, col, &f, &t);
-          q = ff_add_fast(q, f);
+          ff_sum_add(q, f);
           tsum += t.h;
           if (FINAL && k + 1 == a.nz) vol[1] += ff_to_double(ff_mul(f, K.dt));
         }
+        const ff qv = ff_sum_value(q);
         const ff wcn = ff_from_double(r_wo);
         const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
         if (FINAL) {
           const ff el = ff_mul(ff_mul(K.V, st), ff_dif(cur.h, ff_from_double(r_ho)));
-          a.w_new[c] = ff_to_double(ff_add_fast(wcn, ff_mul(ff_dif(ff_mul(K.dt, q), el), inv_V)));
+          a.w_new[c] = ff_to_double(ff_add_fast(wcn, ff_mul(ff_dif(ff_mul(K.dt, qv), el), inv_V)));
           vol[2] += ff_to_double(el);
           cur = below;
           continue;
@@ -383,9 +409,8 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
         // combination in FP64 (the difference is exact where the values are close, Sterbenz);
         // the elastic term and the face-flux sum in float-float
         const double dth = r_wch - r_wo;
-        const ff dh = ff_dif(cur.h, ff_from_double(r_ho));
-        const ff rest = ff_dif(ff_mul(K.V, ff_mul(st, dh)), ff_mul(K.dt, q));
-        bvec[c] = -fma(a.vol_cell, dth, ff_to_double(rest));
+        bvec[c] = -fma(a.vol_cell, dth, ff_to_double(ff_residual_rest(K.V, K.dt, st, cur.h,
+                                                                      r_ho, qv)));
       }
       cur = below;
     }

@@ -118,8 +118,8 @@ __device__ __forceinline__ PtStage pt_stage(const unsigned char* base, int slot)
 __device__ __forceinline__ FfCell pt_cell(const PtStage& s, int r, int x) {
   const int q = r * kPtWideX + x;
   FfCell c;
-  c.h = ff_from_double(s.h[q]);
-  c.kx = ff_mul(ff_from_double(s.ks[q]), ff_from_double(s.kr[q]));
+  c.h = ff_from_double_lean(s.h[q]);
+  c.kx = ff_cond(ff_from_double_lean(s.ks[q]), ff_from_double_lean(s.kr[q]));
   return c;
 }
 
@@ -259,9 +259,7 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
       if (kb > 0 && live && ready(seq0)) {  // the face above the slab, level kb - 1
         const FfCell up = pt_cell(pt_stage(pt_smem, seq0 % kPtStages), br, bx);
         const ff kf = ff_face_mean(hm, up.kx, cur.kx);
-        const ff t = ff_mul(kf, K.cz);
-        tzm = t.h;
-        fzm = ff_add_fast(ff_mul(t, ff_dif(up.h, cur.h)), ff_mul(K.Az, kf));
+        fzm = ff_neg(ff_zface_flux(kf, K.cz, K.Az, cur.h, up.h, &tzm));
       }
       if (kb > 0) release(seq0);
       live = __all_sync(full, live && !abort_flag);
@@ -303,9 +301,7 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
           Kxn = xn.kx;
           hxn = xn.h;
         }
-        const ff t = ff_mul(ff_face_mean(hm, cur.kx, Kxn), K.cx);
-        tx = t.h;
-        fxp = ff_mul(t, ff_dif(hxn, cur.h));
+        fxp = ff_face_flux(ff_face_mean(hm, cur.kx, Kxn), K.cx, hxn, cur.h, &tx);
       }
       float txm = __shfl_up_sync(full, tx, 1);
       ff fxm = ff_neg(ff_make(__shfl_up_sync(full, fxp.h, 1), __shfl_up_sync(full, fxp.l, 1)));
@@ -316,53 +312,49 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
           fxm = zero;
         } else if (lane == 0) {
           const FfCell xm = get(b, br, 0);
-          const ff t = ff_mul(ff_face_mean(hm, xm.kx, cur.kx), K.cx);
-          txm = t.h;
-          fxm = ff_mul(t, ff_dif(xm.h, cur.h));
+          fxm = ff_face_flux(ff_face_mean(hm, xm.kx, cur.kx), K.cx, xm.h, cur.h, &txm);
         }
-        ff q = ff_add_fast(fxm, fxp);
+        FfSum q = ff_sum_of(fxm);
+        ff_sum_add(q, fxp);
         float tsum = txm + tx;
         float ty = 0.0f;
         if (j > 0) {
           const FfCell yn = get(b, br - 1, lane + 1);
-          const ff t = ff_mul(ff_face_mean(hm, yn.kx, cur.kx), K.cy);
-          q = ff_add_fast(q, ff_mul(t, ff_dif(yn.h, cur.h)));
-          tsum += t.h;
+          float t;
+          ff_sum_add(q, ff_face_flux(ff_face_mean(hm, yn.kx, cur.kx), K.cy, yn.h, cur.h, &t));
+          tsum += t;
         }
         if (j + 1 < a.ny) {
           const FfCell yn = get(b, br + 1, lane + 1);
-          const ff t = ff_mul(ff_face_mean(hm, cur.kx, yn.kx), K.cy);
-          ty = t.h;
-          q = ff_add_fast(q, ff_mul(t, ff_dif(yn.h, cur.h)));
+          ff_sum_add(q, ff_face_flux(ff_face_mean(hm, cur.kx, yn.kx), K.cy, yn.h, cur.h, &ty));
           tsum += ty;
         }
         const SoilClass& kc = a.soil.cls[cid];
         if (k > 0) {
-          q = ff_add_fast(q, fzm);
+          ff_sum_add(q, fzm);
           tsum += tzm;
         } else {
           ff f, t;
           ff_top_face(a, K, cur, kc, c, col, &f, &t);
-          q = ff_add_fast(q, f);
+          ff_sum_add(q, f);
           tsum += t.h;
         }
         float tz = 0.0f;
         if (has_below) {
           below = pt_cell(pt_stage(pt_smem, (sk + 1) % kPtStages), br, bx);
           const ff kf = ff_face_mean(hm, cur.kx, below.kx);
-          const ff t = ff_mul(kf, K.cz);
-          tz = t.h;
-          const ff fz = ff_dif(ff_mul(t, ff_dif(below.h, cur.h)), ff_mul(K.Az, kf));
-          q = ff_add_fast(q, fz);
+          const ff fz = ff_zface_flux(kf, K.cz, K.Az, below.h, cur.h, &tz);
+          ff_sum_add(q, fz);
           tsum += tz;
           tzm = tz;
           fzm = ff_neg(fz);
         } else {
           ff f, t;
           ff_bottom_face<true>(a, K, cur, c, col, &f, &t);
-          q = ff_add_fast(q, f);
+          ff_sum_add(q, f);
           tsum += t.h;
         }
+        const ff qv = ff_sum_value(q);
         const int nq = row * 32 + lane;  // this cell in the narrow boxes
         const double r_wo = S.wo[nq], r_ho = S.ho[nq];
         const ff wcn = ff_from_double(r_wo);
@@ -373,9 +365,8 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
         a1[c] = -dtf * ty;
         a2[c] = -dtf * tz;
         const double dth = S.wch[nq] - r_wo;
-        const ff dh = ff_dif(cur.h, ff_from_double(r_ho));
-        const ff rest = ff_dif(ff_mul(K.V, ff_mul(st, dh)), ff_mul(K.dt, q));
-        bvec[c] = -fma(a.vol_cell, dth, ff_to_double(rest));
+        bvec[c] = -fma(a.vol_cell, dth, ff_to_double(ff_residual_rest(K.V, K.dt, st, cur.h,
+                                                                      r_ho, qv)));
       } else if (has_below) {
         below = pt_cell(pt_stage(pt_smem, (sk + 1) % kPtStages), br, bx);
       }

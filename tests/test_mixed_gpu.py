@@ -1,6 +1,7 @@
 """Mixed precision: FP32 Jacobi-PCG with compensated dots under FP64 iterative refinement to
-the FP64 true residual (not in reference).  Head error against the plain FP64 GPU path on the
-same inputs is checked per step (1e-8 m) and the true residual of every solve is verified."""
+the FP64 true residual (not in reference).  Heads are checked per step (1e-8 m) against the
+FP64 oracle on the same inputs and against the plain FP64 GPU path, and the true residual of
+every solve is verified."""
 import numpy as np
 import pytest
 
@@ -17,17 +18,29 @@ def make(w):
     return g
 
 
+def oracle(oracle_mod, w):
+    """the oracle on the same inputs, FP64 Jacobi-PCG at the workload's rtol"""
+    from tests.test_bench_path_gpu import oracle_solver
+    return oracle_solver(oracle_mod, w)
+
+
 @pytest.mark.parametrize("scheme", ["pca", "picard"])
-def test_mixed_matches_fp64(gpu_lib, scheme):
+def test_mixed_matches_fp64(gpu_lib, oracle_mod, scheme):
     w64 = W.config1(scheme, nx=32, ny=24, nz=32, steps=8)
     w32 = W.config1(scheme, nx=32, ny=24, nz=32, steps=8, precision=1)
     w32.solver.ir_rtol = 1e-12
-    a, b = make(w64), make(w32)
+    a, b, o = make(w64), make(w32), oracle(oracle_mod, w32)
     for s in range(w64.steps):
         a.advance_step()
         b.advance_step()
+        o.advance_step()
+        ho = o.interior("h")
+        dh = np.abs(ho - b.interior("h")).max()
+        assert dh <= 1e-8, f"step {s}: mixed vs oracle head error {dh:.3e}"
         dh = np.abs(a.interior("h") - b.interior("h")).max()
         assert dh <= 1e-8, f"step {s}: mixed vs fp64 head error {dh:.3e}"
+        if scheme == "picard":
+            assert b.counters().last_picard_iterations == o.last_picard_its(), s
 
 
 def test_mixed_seam_true_residual(gpu_lib):
@@ -55,10 +68,10 @@ def test_mixed_seam_true_residual(gpu_lib):
 
 @pytest.mark.parametrize("shape", [(32, 24, 32), (30, 14, 27)])
 @pytest.mark.parametrize("scheme", ["pca", "picard"])
-def test_line_preconditioner(gpu_lib, scheme, shape):
-    """Vertical-line PCG inside the refinement: same heads as FP64 Jacobi-PCG (1e-8 m) with
-    fewer inner iterations.  (30, 14, 27): axis 0 not a multiple of 4 (scalar SpMV) and a
-    column length that is not a multiple of the sweep's load batch."""
+def test_line_preconditioner(gpu_lib, oracle_mod, scheme, shape):
+    """Vertical-line PCG inside the refinement: same heads as the oracle and as FP64 Jacobi-PCG
+    on the GPU (1e-8 m) with fewer inner iterations.  (30, 14, 27): axis 0 not a multiple of 4
+    (scalar SpMV) and a column length that is not a multiple of the sweep's load batch."""
     nx, ny, nz = shape
     w64 = W.config1(scheme, nx=nx, ny=ny, nz=nz, steps=6)
     wj = W.config1(scheme, nx=nx, ny=ny, nz=nz, steps=6, precision=1)
@@ -66,10 +79,14 @@ def test_line_preconditioner(gpu_lib, scheme, shape):
     for w in (wj, wl):
         w.solver.ir_rtol = 1e-12
     wl.solver.pc_type = b"line"
-    a, j, l = make(w64), make(wj), make(wl)
+    a, j, l, o = make(w64), make(wj), make(wl), oracle(oracle_mod, wl)
     for s in range(w64.steps):
-        for g in (a, j, l):
+        for g in (a, j, l, o):
             g.advance_step()
+        dh = np.abs(o.interior("h") - l.interior("h")).max()
+        assert dh <= 1e-8, f"step {s}: line-PCG vs oracle head error {dh:.3e}"
+        dh = np.abs(o.interior("h") - j.interior("h")).max()
+        assert dh <= 1e-8, f"step {s}: mixed Jacobi vs oracle head error {dh:.3e}"
         dh = np.abs(a.interior("h") - l.interior("h")).max()
         assert dh <= 1e-8, f"step {s}: line-PCG vs fp64 head error {dh:.3e}"
     its_j, its_l = j.counters().ksp_iterations, l.counters().ksp_iterations
