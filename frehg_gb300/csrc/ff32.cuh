@@ -220,12 +220,10 @@ __device__ __forceinline__ float ff_hi_of(double x) {
 
 // float-float -> double without an FP64 addition: the two significands are added as integers
 // (a.l shifted to the double's last place, truncated there), so the result is within an ulp of
-// the double nearest to a.h + a.l.  Zero, subnormal, infinite and NaN a.h take the conversion
-// instructions.
-__device__ __forceinline__ double ff_to_double(ff a) {
+// the double nearest to a.h + a.l.  Valid for a normal a.h and a normalised pair.
+__device__ __forceinline__ double ff_to_double_core(ff a) {
   const int bh = __float_as_int(a.h);
   const int eh = (bh >> 23) & 0xff;
-  if (eh == 0 || eh == 0xff) return ff_to_double_rare(a);
   // a.h = mh 2^(eh-150): the double's significand M = mh 2^29 in units of 2^(eh-179)
   unsigned long long M = (unsigned long long)((bh & 0x007fffff) | 0x00800000) << 29;
   const int bl = __float_as_int(a.l);
@@ -245,6 +243,66 @@ __device__ __forceinline__ double ff_to_double(ff a) {
   const unsigned long long bits = ((unsigned long long)((unsigned)bh & 0x80000000u) << 32) |
                                   ((unsigned long long)e << 52) | (M & ((1ull << 52) - 1));
   return __longlong_as_double((long long)bits);
+}
+
+// Zero, subnormal, infinite and NaN a.h take the conversion instructions.
+__device__ __forceinline__ double ff_to_double(ff a) {
+  const int eh = (__float_as_int(a.h) >> 23) & 0xff;
+  if (eh == 0 || eh == 0xff) return ff_to_double_rare(a);
+  return ff_to_double_core(a);
+}
+
+// ---- branch-free conversions --------------------------------------------------------------
+// For kernels whose values stay within the normal float range: no out-of-line call and no
+// branch (the special cases are selected), so that the calling kernel keeps no call site.
+// Outside that range they flush: |x| < 2^-126 (and 0) gives a signed zero, an absolute error
+// below 2^-126; |x| >= 2^128, inf and NaN give NaN.
+
+// as ff_from_double_lean
+__device__ __forceinline__ ff ff_from_double_nb(double x) {
+  const int hx = __double2hiint(x);
+  const int lx = __double2loint(x);
+  const int fe = ((hx >> 20) & 0x7ff) - (1023 - 127);  // the float's biased exponent
+  const int sign = hx & (int)0x80000000;
+  float h = __int_as_float(sign | (fe << 23) | ((hx & 0x000fffff) << 3) |
+                           (int)((unsigned)lx >> 29));
+  const float p2 = __int_as_float((fe & 0xff) << 23);
+  float l = __fmul_rn(__fmul_rn(__uint2float_rn((unsigned)lx & 0x1fffffffu), 0x1p-52f), p2);
+  l = __int_as_float(__float_as_int(l) | sign);
+  if (fe < 1) {
+    h = __int_as_float(sign);
+    l = h;
+  }
+  if (fe > 254) {
+    h = __int_as_float(0x7fc00000);
+    l = 0.0f;
+  }
+  return ff_make(h, l);
+}
+
+// as ff_hi_of (|x| >= 2^127 gives NaN)
+__device__ __forceinline__ float ff_hi_of_nb(double x) {
+  const int hx = __double2hiint(x);
+  const int fe = ((hx >> 20) & 0x7ff) - (1023 - 127);
+  const unsigned lx = (unsigned)__double2loint(x);
+  float r = __int_as_float(((hx & (int)0x80000000) | (fe << 23) | ((hx & 0x000fffff) << 3) |
+                            (int)(lx >> 29)) +
+                           (int)((lx >> 28) & 1u));
+  if (fe < 1) r = __int_as_float(hx & (int)0x80000000);
+  if (fe > 253) r = __int_as_float(0x7fc00000);
+  return r;
+}
+
+// as ff_to_double for a normalised pair; a.h zero or subnormal gives a signed zero, infinite
+// or NaN a.h gives NaN
+__device__ __forceinline__ double ff_to_double_nb(ff a) {
+  const int bh = __float_as_int(a.h);
+  const int eh = (bh >> 23) & 0xff;
+  double r = ff_to_double_core(a);
+  const unsigned long long zero = (unsigned long long)((unsigned)bh & 0x80000000u) << 32;
+  if (eh == 0) r = __longlong_as_double((long long)zero);
+  if (eh == 0xff) r = __longlong_as_double(0x7ff8000000000000ll);
+  return r;
 }
 
 static __device__ __noinline__ double f2d_scaled_rare(float f, int k) {

@@ -34,12 +34,16 @@ __device__ __forceinline__ ff cell_ky(const FfCell& c) { return ISO ? c.kx : c.k
 template <bool ISO>
 __device__ __forceinline__ ff cell_kz(const FfCell& c) { return ISO ? c.kx : c.kz; }
 
-__device__ __forceinline__ const SoilClass& class_of(const ReArgs& a, size_t c, size_t col) {
+// Cell indices are 32-bit: a handle holds fewer than 2^31 cells (frehg_re_create refuses more;
+// their device state alone would exceed the GPU's memory).
+using cidx = unsigned;
+
+__device__ __forceinline__ const SoilClass& class_of(const ReArgs& a, cidx c, cidx col) {
   return a.soil.cls[a.soil.cid ? (int)a.soil.cid[a.soil.cid3d ? c : col] : 0];
 }
 
 // Ks of one cell along axis d (0 x, 1 y, 2 z)
-__device__ __forceinline__ ff ff_ks(const ReArgs& a, const SoilClass& k, size_t c, int d) {
+__device__ __forceinline__ ff ff_ks(const ReArgs& a, const SoilClass& k, cidx c, int d) {
   if (a.soil.Ks) return ff_from_double(a.soil.Ks[c]);
   return ff_make(k.ff_ks[d][0], k.ff_ks[d][1]);
 }
@@ -51,13 +55,13 @@ __device__ __forceinline__ ff ff_cond(ff ks, ff kr) { return ff_mul_lean(ks, kr)
 // only); the cell then carries kx alone
 // Head, kr and Ks enter as lean splits (ff_from_double_lean): only the face sums read them.
 template <bool ISO = false>
-__device__ __forceinline__ FfCell ff_cell(const ReArgs& a, size_t c, size_t col) {
-  const ff kr = ff_from_double_lean(a.kr[c]);
+__device__ __forceinline__ FfCell ff_cell(const ReArgs& a, cidx c, cidx col) {
+  const ff kr = ff_from_double_nb(a.kr[c]);
   FfCell r;
-  r.h = ff_from_double_lean(a.h_new[c]);
+  r.h = ff_from_double_nb(a.h_new[c]);
   if (ISO) {
     if (a.soil.Ks) {
-      r.kx = ff_cond(ff_from_double_lean(a.soil.Ks[c]), kr);
+      r.kx = ff_cond(ff_from_double_nb(a.soil.Ks[c]), kr);
     } else {
       const SoilClass& k = class_of(a, c, col);
       r.kx = ff_cond(ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
@@ -66,7 +70,7 @@ __device__ __forceinline__ FfCell ff_cell(const ReArgs& a, size_t c, size_t col)
   }
   const SoilClass& k = class_of(a, c, col);
   if (a.soil.Ks || k.ks_iso) {
-    r.kx = ff_cond(a.soil.Ks ? ff_from_double_lean(a.soil.Ks[c])
+    r.kx = ff_cond(a.soil.Ks ? ff_from_double_nb(a.soil.Ks[c])
                              : ff_make(k.ff_ks[0][0], k.ff_ks[0][1]), kr);
     r.ky = r.kx;
     r.kz = r.kx;
@@ -129,7 +133,7 @@ __device__ __forceinline__ FfConst ff_consts(const ReArgs& a, double dt) {
 // the top-face closure of one cell: flux into the cell and the transmissibility it adds to the
 // diagonal (pic_row's k = 0 branch)
 __device__ __forceinline__ void ff_top_face(const ReArgs& a, const FfConst& K, const FfCell& cell,
-                                            const SoilClass& kc, size_t c, size_t col, ff* flux,
+                                            const SoilClass& kc, cidx c, cidx col, ff* flux,
                                             ff* trans) {
   *flux = ff_make(0.0f);
   *trans = ff_make(0.0f);
@@ -155,7 +159,7 @@ __device__ __forceinline__ void ff_top_face(const ReArgs& a, const FfConst& K, c
 // the bottom-face closure (pic_row's k = nz-1 branch)
 template <bool ISO = false>
 __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K,
-                                               const FfCell& cell, size_t c, size_t col, ff* flux,
+                                               const FfCell& cell, cidx c, cidx col, ff* flux,
                                                ff* trans) {
   *flux = ff_make(0.0f);
   *trans = ff_make(0.0f);
@@ -176,7 +180,7 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
 // The Picard residual's float-float part V Ss (wcn/ths) (h - h_old) - dt q, renormalised (the
 // storage difference and the final combination are FP64)
 __device__ __forceinline__ ff ff_residual_rest(ff V, ff dt, ff st, ff h, double h_old, ff q) {
-  const ff dh = ff_dif_lean(h, ff_from_double_lean(h_old));
+  const ff dh = ff_dif_lean(h, ff_from_double_nb(h_old));
   FfSum r = ff_sum_of(ff_mul_lean(V, ff_mul_lean(st, dh)));
   ff_sum_add(r, ff_neg(ff_mul_lean(dt, q)));
   return ff_sum_value(r);
@@ -233,27 +237,28 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
     const int i = (tile % t0) * 32 + lane;
     const int j0 = (tile / t0) * 8, j = j0 + row;
     const bool act = i < a.nx && j < a.ny;
-    const size_t col = act ? (size_t)i + (size_t)a.nx * j : 0;
+    const cidx ncol = (cidx)a.ncol;
+    const cidx col = act ? (cidx)i + (cidx)a.nx * j : 0u;
     // halo rows of the tile: threads 0-31 stage row j0 - 1, threads 32-63 row j0 + 8
     const int jh = tid < 32 ? j0 - 1 : j0 + 8;
     const bool act_h = tid < 64 && i < a.nx && jh >= 0 && jh < a.ny;
-    const size_t colh = act_h ? (size_t)i + (size_t)a.nx * jh : 0;
+    const cidx colh = act_h ? (cidx)i + (cidx)a.nx * jh : 0u;
     const int hrow = tid < 32 ? 0 : 9;
     const int kb = blockIdx.y * planes, ke = min(a.nz, kb + planes);
     FfCell cur = {zero, zero, zero, zero};
     ff fzm = zero;     // flux into the current cell through its top face
     float tzm = 0.0f;  // and that face's transmissibility (leading float)
     if (act && kb < ke) {
-      cur = ff_cell<ISO>(a, col + a.ncol * kb, col);
+      cur = ff_cell<ISO>(a, col + ncol * kb, col);
       if (kb > 0) {  // the face above the slab, as the slab above forms it (negated)
-        const FfCell up = ff_cell<ISO>(a, col + a.ncol * (kb - 1), col);
+        const FfCell up = ff_cell<ISO>(a, col + ncol * (kb - 1), col);
         const ff kf = ff_face_mean(hm, cell_kz<ISO>(up), cell_kz<ISO>(cur));
         fzm = ff_neg(ff_zface_flux(kf, K.cz, K.Az, cur.h, up.h, &tzm));
       }
     }
     for (int k = kb; k < ke; ++k) {
       FfYPlane& P = ys[k & 1];
-      const size_t c = col + a.ncol * k;
+      const cidx c = col + ncol * k;
       // stage this level: the own cell and the halo rows
       P.hh[row + 1][lane] = cur.h.h;
       P.hl[row + 1][lane] = cur.h.l;
@@ -261,7 +266,7 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
       P.kl[row + 1][lane] = cell_ky<ISO>(cur).l;
       if (tid < 64) {
         FfCell hc = {zero, zero, zero, zero};
-        if (act_h) hc = ff_cell<ISO>(a, colh + a.ncol * k, colh);
+        if (act_h) hc = ff_cell<ISO>(a, colh + ncol * k, colh);
         P.hh[hrow][lane] = hc.h.h;
         P.hl[hrow][lane] = hc.h.l;
         P.kh[hrow][lane] = cell_ky<ISO>(hc).h;
@@ -271,33 +276,58 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
         const int ix = (tile % t0) * 32 + (side ? 32 : -1), jx = j0 + xr;
         FfCell xc = {zero, zero, zero, zero};
         if (ix >= 0 && ix < a.nx && jx < a.ny) {
-          const size_t colx = (size_t)ix + (size_t)a.nx * jx;
-          xc = ff_cell<ISO>(a, colx + a.ncol * k, colx);
+          const cidx colx = (cidx)ix + (cidx)a.nx * jx;
+          xc = ff_cell<ISO>(a, colx + ncol * k, colx);
         }
         P.xhh[xr][side] = xc.h.h;
         P.xhl[xr][side] = xc.h.l;
         P.xkh[xr][side] = xc.kx.h;
         P.xkl[xr][side] = xc.kx.l;
       }
-      // raw loads for the cell below (z face, carried to the next level) and for this cell's
-      // residual, issued before the barrier and converted after it, so that their latency
-      // overlaps the barrier and the x and y faces
+      // This cell's residual values are read after the faces, from L1: their lines are
+      // prefetched one level earlier (below), which keeps no registers of loads in flight during
+      // the face sums.  The cell below (z face, carried to the next level) is loaded before the
+      // barrier and converted after it.
       const bool has_below = act && k + 1 < a.nz;
-      const size_t cb = has_below ? c + a.ncol : c;
+      if (act) {
+        if (has_below) {
+          const cidx cn = c + ncol;
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(a.w_old + cn));
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(a.h_old + cn));
+          if (!FINAL) {
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a.wch + cn));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a.cap + cn));
+          }
+        }
+      }
+      // the halo cells of the next level (their rows are not the tile's own)
+      if (k + 1 < ke) {
+        if (tid < 64) {
+          if (act_h) {
+            const cidx ch = colh + ncol * (k + 1);
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a.h_new + ch));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a.kr + ch));
+            if (a.soil.Ks) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.soil.Ks + ch));
+          }
+        } else if (tid < 80) {
+          const int xr = (tid - 64) >> 1, side = (tid - 64) & 1;
+          const int ix = (tile % t0) * 32 + (side ? 32 : -1), jx = j0 + xr;
+          if (ix >= 0 && ix < a.nx && jx < a.ny) {
+            const cidx cx = (cidx)ix + (cidx)a.nx * jx + ncol * (k + 1);
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a.h_new + cx));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a.kr + cx));
+            if (a.soil.Ks) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.soil.Ks + cx));
+          }
+        }
+      }
+      const cidx cb = has_below ? c + ncol : c;
       double rb_h = 0.0, rb_kr = 0.0, rb_ks = 0.0;
       int rb_id = 0;
-      double r_wo = 0.0, r_wch = 0.0, r_ho = 0.0, r_cap = 0.0;
       if (act) {
         rb_h = a.h_new[cb];
         rb_kr = a.kr[cb];
         if (a.soil.Ks) rb_ks = a.soil.Ks[cb];
         if (a.soil.cid) rb_id = a.soil.cid[a.soil.cid3d ? cb : col];
-        r_wo = a.w_old[c];
-        r_ho = a.h_old[c];
-        if (!FINAL) {
-          r_wch = a.wch[c];
-          r_cap = a.cap[c];
-        }
       }
       __syncthreads();
       // +x face from the next lane's cell (lane 31 loads its neighbour)
@@ -361,10 +391,10 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
         float tz = 0.0f;
         if (has_below) {
           const SoilClass& kb = a.soil.cls[rb_id];
-          const ff kr = ff_from_double_lean(rb_kr);
-          below.h = ff_from_double_lean(rb_h);
+          const ff kr = ff_from_double_nb(rb_kr);
+          below.h = ff_from_double_nb(rb_h);
           if (ISO || a.soil.Ks || kb.ks_iso) {
-            below.kx = ff_cond(a.soil.Ks ? ff_from_double_lean(rb_ks)
+            below.kx = ff_cond(a.soil.Ks ? ff_from_double_nb(rb_ks)
                                          : ff_make(kb.ff_ks[0][0], kb.ff_ks[0][1]), kr);
             if (!ISO) {
               below.ky = below.kx;
@@ -389,19 +419,22 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
           if (FINAL && k + 1 == a.nz) vol[1] += ff_to_double(ff_mul(f, K.dt));
         }
         const ff qv = ff_sum_value(q);
-        const ff wcn = ff_from_double(r_wo);
+        const double r_wo = a.w_old[c], r_ho = a.h_old[c];
+        const double r_wch = FINAL ? 0.0 : a.wch[c], r_cap = FINAL ? 0.0 : a.cap[c];
+        const ff wcn = ff_from_double_nb(r_wo);
         const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
         if (FINAL) {
-          const ff el = ff_mul(ff_mul(K.V, st), ff_dif(cur.h, ff_from_double(r_ho)));
-          a.w_new[c] = ff_to_double(ff_add_fast(wcn, ff_mul(ff_dif(ff_mul(K.dt, qv), el), inv_V)));
-          vol[2] += ff_to_double(el);
+          const ff el = ff_mul(ff_mul(K.V, st), ff_dif(cur.h, ff_from_double_nb(r_ho)));
+          const ff dw = ff_mul(ff_dif(ff_mul(K.dt, qv), el), inv_V);
+          a.w_new[c] = ff_to_double_nb(ff_add_fast(wcn, dw));
+          vol[2] += ff_to_double_nb(el);
           cur = below;
           continue;
         }
         // diagonal V (C + Ss wcn/ths) + dt sum T and couplings -dt T (FP32), rhs -Rdt with
         // Rdt = V (wch - wcn) + V Ss (wcn/ths) (h - h_old) - dt q (float-float)
         const float dtf = K.dt.h;
-        dg[c] = (T)fmaf(dtf, tsum, K.V.h * (ff_hi_of(r_cap) + st.h));
+        dg[c] = (T)fmaf(dtf, tsum, K.V.h * (ff_hi_of_nb(r_cap) + st.h));
         a0[c] = (T)(-dtf * tx);
         a1[c] = (T)(-dtf * ty);
         a2[c] = (T)(-dtf * tz);
@@ -409,8 +442,8 @@ __global__ void __launch_bounds__(256, 4) k_pic_assemble_ff(ReArgs a, T* __restr
         // combination in FP64 (the difference is exact where the values are close, Sterbenz);
         // the elastic term and the face-flux sum in float-float
         const double dth = r_wch - r_wo;
-        bvec[c] = -fma(a.vol_cell, dth, ff_to_double(ff_residual_rest(K.V, K.dt, st, cur.h,
-                                                                      r_ho, qv)));
+        bvec[c] = -fma(a.vol_cell, dth, ff_to_double_nb(ff_residual_rest(K.V, K.dt, st, cur.h,
+                                                                         r_ho, qv)));
       }
       cur = below;
     }

@@ -118,8 +118,8 @@ __device__ __forceinline__ PtStage pt_stage(const unsigned char* base, int slot)
 __device__ __forceinline__ FfCell pt_cell(const PtStage& s, int r, int x) {
   const int q = r * kPtWideX + x;
   FfCell c;
-  c.h = ff_from_double_lean(s.h[q]);
-  c.kx = ff_cond(ff_from_double_lean(s.ks[q]), ff_from_double_lean(s.kr[q]));
+  c.h = ff_from_double_nb(s.h[q]);
+  c.kx = ff_cond(ff_from_double_nb(s.ks[q]), ff_from_double_nb(s.kr[q]));
   return c;
 }
 
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
     const int i = (tile % t0) * 32 + lane;
     const int j0 = (tile / t0) * 8, j = j0 + row;
     const bool act = i < a.nx && j < a.ny;
-    const size_t col = act ? (size_t)i + (size_t)a.nx * j : 0;
+    const cidx col = act ? (cidx)i + (cidx)a.nx * j : 0u;
     const uint32_t seq0 = seq;  // sequence number of level lo
     seq += (uint32_t)(hi - lo + 1);
     const int bx = lane + 2, br = row + 1;  // this cell's position in the wide boxes
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
     }
     for (int k = kb; k < ke; ++k) {
       const uint32_t sk = seq0 + (uint32_t)(k - lo);
-      const size_t c = col + a.ncol * k;
+      const cidx c = col + (cidx)a.ncol * k;
       const bool has_below = k + 1 < a.nz;
       const int b = k & 1;
       // the class id for the residual's Ss / theta_s (direct load, issued before the waits)
@@ -357,16 +357,16 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
         const ff qv = ff_sum_value(q);
         const int nq = row * 32 + lane;  // this cell in the narrow boxes
         const double r_wo = S.wo[nq], r_ho = S.ho[nq];
-        const ff wcn = ff_from_double(r_wo);
+        const ff wcn = ff_from_double_nb(r_wo);
         const ff st = ff_mul(ff_make(kc.ff_ss_ths[0], kc.ff_ss_ths[1]), wcn);  // Ss wcn / ths
         const float dtf = K.dt.h;
-        dg[c] = fmaf(dtf, tsum, K.V.h * (ff_hi_of(S.cap[nq]) + st.h));
+        dg[c] = fmaf(dtf, tsum, K.V.h * (ff_hi_of_nb(S.cap[nq]) + st.h));
         a0[c] = -dtf * tx;
         a1[c] = -dtf * ty;
         a2[c] = -dtf * tz;
         const double dth = S.wch[nq] - r_wo;
-        bvec[c] = -fma(a.vol_cell, dth, ff_to_double(ff_residual_rest(K.V, K.dt, st, cur.h,
-                                                                      r_ho, qv)));
+        bvec[c] = -fma(a.vol_cell, dth, ff_to_double_nb(ff_residual_rest(K.V, K.dt, st, cur.h,
+                                                                         r_ho, qv)));
       } else if (has_below) {
         below = pt_cell(pt_stage(pt_smem, (sk + 1) % kPtStages), br, bx);
       }

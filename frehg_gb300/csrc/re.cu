@@ -873,6 +873,8 @@ int frehg_re_create(int nx, int ny, int nz, const frehg_re_params* p, frehg_re**
   clear_error();
   FG_ARG(out != nullptr && p != nullptr, "null argument");
   FG_ARG(nx > 0 && ny > 0 && nz > 0, "grid sizes must be positive");
+  // the kernels index cells with 32-bit integers; 2^31 cells would need over 280 GB of state
+  FG_ARG((size_t)nx * ny * nz < ((size_t)1 << 31), "more than 2^31 - 1 cells");
   FG_TRY(validate_params(p));
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {

@@ -131,7 +131,8 @@ void frehg_solver_config_default(frehg_solver_config* c);
 typedef struct frehg_re frehg_re;
 
 /* ReSolver(const Grid&, const MpiComm*) + setParams (ReSolver.hpp:50,53).  Allocates the device
- * state for an nx*ny*nz grid on the current CUDA device. */
+ * state for an nx*ny*nz grid on the current CUDA device; at most 2^31 - 1 cells
+ * (FREHG_ERR_ARG beyond). */
 int frehg_re_create(int nx, int ny, int nz, const frehg_re_params* p, frehg_re** out);
 int frehg_re_destroy(frehg_re* re);
 /* ReSolver::setParams (ReSolver.hpp:53).  Grid sizes stay fixed. */
