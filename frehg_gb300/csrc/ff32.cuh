@@ -178,16 +178,10 @@ static __device__ __noinline__ double ff_to_double_rare(ff a) { return (double)a
 
 // double -> float-float without a double->float conversion: hi = the top 24 bits of the
 // significand (truncated), lo = the next 29 bits (rounded to 24 by the int->float conversion),
-// renormalised.  Values below 2^-100 or above 2^127 in magnitude (and 0, inf, NaN) take the
-// conversion instructions instead.
-// The split without the final renormalisation: hi the truncated leading 24 bits, 0 <= |lo| <
-// ulp(hi), lo of the sign of hi (a lean operand).
-__device__ __forceinline__ ff ff_from_double_lean(double x) {
-  const int hx = __double2hiint(x);
-  const int lx = __double2loint(x);
-  const int E = (hx >> 20) & 0x7ff;
-  // one unsigned compare for 1023 - 100 <= E <= 1023 + 127
-  if ((unsigned)(E - (1023 - 100)) > 227u) return ff_from_double_rare(x);
+// 0 <= |lo| < ulp(hi), lo of the sign of hi.  ff_from_double renormalises the pair;
+// ff_from_double_lean leaves it as a lean operand.  Values below 2^-100 or above 2^127 in
+// magnitude (and 0, inf, NaN) take the conversion instructions instead.
+__device__ __forceinline__ ff ff_split_bits(int hx, int lx, int E) {
   const int sign = hx & (int)0x80000000;
   const float h = __int_as_float(sign | ((E - 1023 + 127) << 23) | ((hx & 0x000fffff) << 3) |
                                  (int)((unsigned)lx >> 29));
@@ -198,8 +192,19 @@ __device__ __forceinline__ ff ff_from_double_lean(double x) {
   return ff_make(h, l);
 }
 
+__device__ __forceinline__ ff ff_from_double_lean(double x) {
+  const int hx = __double2hiint(x);
+  const int E = (hx >> 20) & 0x7ff;
+  // one unsigned compare for 1023 - 100 <= E <= 1023 + 127
+  if ((unsigned)(E - (1023 - 100)) > 227u) return ff_from_double_rare(x);
+  return ff_split_bits(hx, __double2loint(x), E);
+}
+
 __device__ __forceinline__ ff ff_from_double(double x) {
-  const ff r = ff_from_double_lean(x);
+  const int hx = __double2hiint(x);
+  const int E = (hx >> 20) & 0x7ff;
+  if ((unsigned)(E - (1023 - 100)) > 227u) return ff_from_double_rare(x);
+  const ff r = ff_split_bits(hx, __double2loint(x), E);
   return fast_two_sum(r.h, r.l);
 }
 

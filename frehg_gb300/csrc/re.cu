@@ -703,6 +703,9 @@ static int picard_step(frehg_re* re) {
     iso = true;
     for (const SoilClass& k : re->cls_host) iso = iso && k.ks_iso;
   }
+  // every class van Genuchten (not MVG): the float-float constitutive kernel without FP64 forms
+  bool all_ff = true;
+  for (const SoilClass& k : re->cls_host) all_ff = all_ff && k.use_vg && !k.use_mvg;
   // a float-float assembly solved in mixed precision writes its matrix entries as floats
   const bool f32 = !re->p.picard_fp64 && mixed_solve(re);
   if (f32) FG_TRY(re->ksp.ensure32(re->n));
@@ -719,10 +722,14 @@ static int picard_step(frehg_re* re) {
         FG_LAUNCH(prof, st, "k_kr", (32.0 + sb) * n,
                   (k_constit<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch,
                                                              re->cap)));
+      else if (all_ff)
+        FG_LAUNCH(prof, st, "k_kr_ff", (32.0 + sb) * n,
+                  (k_constit_ff<true, true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr,
+                                                                      re->wch, re->cap)));
       else
         FG_LAUNCH(prof, st, "k_kr_ff", (32.0 + sb) * n,
-                  (k_constit_ff<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch,
-                                                                re->cap)));
+                  (k_constit_ff<true, true, false><<<nb, 256, 0, st>>>(a, a.h_new, re->kr,
+                                                                       re->wch, re->cap)));
       re->A.scaled = false;
       re->A.s_in_r = false;
       re->A.f32_entries = f32;

@@ -168,8 +168,9 @@ __global__ void k_constit(ReArgs a, const double* __restrict__ h, double* __rest
 }
 
 // k_constit with the van Genuchten classes evaluated in float-float arithmetic on the FP32 pipe
-// (vg_constit_ff); MVG and exponential classes take the FP64 forms
-template <bool THETA, bool CAP>
+// (vg_constit_ff); MVG and exponential classes take the FP64 forms.  ALL_FF: every class is
+// van Genuchten (not MVG), and the FP64 forms are not compiled in.
+template <bool THETA, bool CAP, bool ALL_FF>
 __global__ void __launch_bounds__(256, 4) k_constit_ff(ReArgs a, const double* __restrict__ h,
                                                        double* __restrict__ kr,
                                                        double* __restrict__ th,
@@ -185,8 +186,8 @@ __global__ void __launch_bounds__(256, 4) k_constit_ff(ReArgs a, const double* _
     const SoilClass& k = a.soil.cls[id];
     const double hc = h[c];
     Constit r;
-    if (k.use_vg && !k.use_mvg) {
-      const ff alpha = a.soil.alpha ? ff_from_double(a.soil.alpha[c])
+    if (ALL_FF || (k.use_vg && !k.use_mvg)) {
+      const ff alpha = a.soil.alpha ? ff_from_double_nb(a.soil.alpha[c])
                                     : ff_make(k.ff_alpha[0], k.ff_alpha[1]);
       r = vg_constit_ff<THETA, CAP>(k, alpha, a.soil.continuous_theta ? 0.0 : k.aev, hc);
     } else {

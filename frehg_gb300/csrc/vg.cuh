@@ -279,7 +279,7 @@ __device__ __forceinline__ Constit vg_constit_ff(const SoilClass& k, ff alpha, d
   r.kr = 1.0;
   r.theta = k.ths;
   r.cap = 0.0;
-  const ff ah = ff_mul(alpha, ff_from_double(-h));  // |alpha h| for h < 0
+  const ff ah = ff_mul(alpha, ff_from_double_nb(-h));  // |alpha h| for h < 0
   if (!(ah.h > 0.0f)) return r;
   const ff n = ff_make(k.ff_n[0], k.ff_n[1]);
   const ff m = ff_make(k.ff_m[0], k.ff_m[1]);
@@ -302,13 +302,13 @@ __device__ __forceinline__ Constit vg_constit_ff(const SoilClass& k, ff alpha, d
   const ff one_minus = ff_neg(ff_expm1(y));
   const ff se_half = ff_exp(ff_scale(mu, -0.5f));
   const ff kr = ff_mul(se_half, ff_sqr(one_minus));
-  r.kr = ff_ge1(kr) ? 1.0 : ff_to_double(kr);
+  r.kr = ff_ge1(kr) ? 1.0 : ff_to_double_nb(kr);
   const ff se = ff_sqr(se_half);
   if (WANT_THETA && !(h > aev)) {
     // theta_r + (theta_s - theta_r) se with se in [0, 1]: theta_s where se rounds to >= 1
     const ff wc = ff_add_fast(ff_make(k.ff_thr[0], k.ff_thr[1]),
                               ff_mul(ff_make(k.ff_dth[0], k.ff_dth[1]), se));
-    r.theta = ff_ge1(se) ? k.ths : ff_to_double(wc);
+    r.theta = ff_ge1(se) ? k.ths : ff_to_double_nb(wc);
   }
   if (WANT_CAP) {
     // alpha n m (ths - thr) t se / (|alpha h| (1 + t)) from the leading floats: C enters only
