@@ -85,6 +85,42 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+// Copies of the three input rows y-1, y, y+1 of plane zz (pixels x0-1 .. x0+128) into dst,
+// [dy][chunk][pixel][8], with zero fill outside the grid: thread t copies pixel t (threads 0 and
+// 1 also pixels 128 and 129), every row and chunk, so the index arithmetic is per pixel and
+// row, not per copy.
+template <int CH>
+__device__ __forceinline__ void tc_load_rows(unsigned char* dst, const __nv_bfloat16* in,
+                                             int in_stride, int in_off, int x0, int y, int zz,
+                                             int nx, int ny, int nz, int tid) {
+  const bool zok = zz >= 0 && zz < nz;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const int p = half ? kTcM + tid : tid;
+    if (half && p >= kTcP) break;
+    const int xx = x0 + p - 1;
+    const bool xok = zok && xx >= 0 && xx < nx;
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+      const int yy = y + dy - 1;
+      const bool ok = xok && yy >= 0 && yy < ny;
+      const __nv_bfloat16* src =
+          ok ? in + ((size_t)xx + (size_t)nx * ((size_t)yy + (size_t)ny * zz)) * in_stride + in_off
+             : in;
+      unsigned char* d = dst + (dy * CH * kTcP + p) * 16;
+#pragma unroll
+      for (int c = 0; c < CH; ++c) tc_cp16(d + c * kTcP * 16, ok ? src + 8 * c : in, ok ? 16 : 0);
+    }
+  }
+}
+
+// A descriptor advanced by a byte offset (a multiple of 16): the start address is the low
+// 14-bit field in 16-byte units, and shared-memory addresses stay below 2^18 bytes, so the sum
+// does not carry out of the field.
+__device__ __forceinline__ uint64_t tc_desc_at(uint64_t d, uint32_t bytes) {
+  return d + (uint64_t)(bytes >> 4);
+}
+
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restrict__ in,
                                                   int in_stride, int in_off,
@@ -136,22 +172,13 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
       const int zz = z + dz;
       if (zz < 0 || zz >= nz) continue;  // zero padding: the plane adds nothing
       // the plane's three input rows, [dy][chunk][pixel][8]
-      for (int q = tid; q < 3 * S::CH * kTcP; q += 128) {
-        const int p = q % kTcP, c = (q / kTcP) % S::CH, dy = q / (kTcP * S::CH);
-        const int yy = y + dy - 1, xx = x0 + p - 1;
-        const bool ok = yy >= 0 && yy < ny && xx >= 0 && xx < nx;
-        const __nv_bfloat16* src =
-            ok ? in + ((size_t)xx + (size_t)nx * ((size_t)yy + (size_t)ny * zz)) * in_stride +
-                     in_off + 8 * c
-               : in;
-        tc_cp16(rows + ((dy * S::CH + c) * kTcP + p) * 16, src, ok ? 16 : 0);
-      }
+      tc_load_rows<S::CH>(rows, in, in_stride, in_off, x0, y, zz, nx, ny, nz, tid);
       // the plane's nine taps of W[tap][o][i], [tap][chunk][o][8]
       for (int q = tid; q < 9 * S::CH * COUT; q += 128) {
         const int o = q % COUT, c = (q / COUT) % S::CH, t9 = q / (COUT * S::CH);
         const int tap = (dz + 1) * 9 + t9;
-        tc_cp16(wts + ((t9 * S::CH + c) * COUT + o) * 16, W + ((size_t)tap * COUT + o) * CIN + 8 * c,
-                16);
+        tc_cp16(wts + ((t9 * S::CH + c) * COUT + o) * 16,
+                W + ((size_t)tap * COUT + o) * CIN + 8 * c, 16);
       }
       asm volatile("cp.async.wait_all;" ::: "memory");
       // the copies are generic-proxy writes the tensor cores read through the async proxy
@@ -160,14 +187,15 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (tid == 0) {
-#pragma unroll 1
+        const uint64_t a0 = tc_desc(rows_s, S::PLANE, 128);
+        const uint64_t b0 = tc_desc(wts_s, COUT * 16, 128);
+#pragma unroll
         for (int t9 = 0; t9 < 9; ++t9) {
           const int dy = t9 / 3, dx = t9 % 3;
 #pragma unroll
           for (int kc = 0; kc < CIN / 16; ++kc) {
-            const uint64_t a = tc_desc(rows_s + ((dy * S::CH + 2 * kc) * kTcP + dx) * 16,
-                                       S::PLANE, 128);
-            const uint64_t b = tc_desc(wts_s + (t9 * S::CH + 2 * kc) * COUT * 16, COUT * 16, 128);
+            const uint64_t a = tc_desc_at(a0, ((dy * S::CH + 2 * kc) * kTcP + dx) * 16);
+            const uint64_t b = tc_desc_at(b0, (t9 * S::CH + 2 * kc) * COUT * 16);
             const uint32_t acc = first ? 0u : 1u;
             asm volatile(
                 "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -250,8 +278,10 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
 // loaded one tile ahead with cp.async while the previous tile's MMAs run, and two tensor-memory
 // accumulators let the epilogue of tile z-1 overlap the MMAs of tile z:
 //   wait for plane z+1, barrier; issue MMA(z) -> acc[z&1], commit;
-//   wait MMA(z-1); epilogue(z-1) from acc[(z-1)&1];
-//   load plane z+2 into the slot of plane z-2 (free: MMA(z-1) was its last reader).
+//   wait MMA(z-1); load plane z+2 into the slot of plane z-2 (free: MMA(z-1) was its last
+//   reader); epilogue(z-1) from acc[(z-1)&1] while those copies land.
+// The MMA issue is unrolled over the taps and channel slices with the descriptors advanced by
+// constant offsets.
 constexpr int kTcZC = 16;  // tiles of one z column
 
 template <int CIN, int COUT>
@@ -315,18 +345,8 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
 
   // copies of input plane zz (three rows) into ring slot zz & 3, zero outside the grid
   auto load_plane = [&](int x0, int y, int zz) {
-    unsigned char* slot = ring + (zz & 3) * S::SLOT;
-    const bool zok = zz >= 0 && zz < nz;
-    for (int q = tid; q < 3 * S::CH * kTcP; q += 128) {
-      const int p = q % kTcP, c = (q / kTcP) % S::CH, dy = q / (kTcP * S::CH);
-      const int yy = y + dy - 1, xx = x0 + p - 1;
-      const bool ok = zok && yy >= 0 && yy < ny && xx >= 0 && xx < nx;
-      const __nv_bfloat16* src =
-          ok ? in + ((size_t)xx + (size_t)nx * ((size_t)yy + (size_t)ny * zz)) * in_stride +
-                   in_off + 8 * c
-             : in;
-      tc_cp16(slot + ((dy * S::CH + c) * kTcP + p) * 16, src, ok ? 16 : 0);
-    }
+    tc_load_rows<S::CH>(ring + (zz & 3) * S::SLOT, in, in_stride, in_off, x0, y, zz, nx, ny, nz,
+                        tid);
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
   // bias + ReLU + BF16 store of tile (x0, y, z) from accumulator b
@@ -398,25 +418,28 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (tid == 0) {
         bool first = true;
-#pragma unroll 1
-        for (int t = 0; t < 27; ++t) {
-          const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
+        const uint64_t b0 = tc_desc(wts_s, COUT * 16, 128);
+        const uint32_t d_tmem = tmem + (uint32_t)(b * S::ACC_COLS);
+#pragma unroll
+        for (int dz = 0; dz < 3; ++dz) {
           const int zz = z + dz - 1;
           if (zz < 0 || zz >= nz) continue;  // zero padding
-          const uint32_t slot_s = ring_s + (uint32_t)((zz & 3) * S::SLOT);
+          const uint64_t a0 = tc_desc(ring_s + (uint32_t)((zz & 3) * S::SLOT), S::PLANE, 128);
 #pragma unroll
-          for (int kc = 0; kc < CIN / 16; ++kc) {
-            const uint64_t a = tc_desc(slot_s + ((dy * S::CH + 2 * kc) * kTcP + dx) * 16,
-                                       S::PLANE, 128);
-            const uint64_t bd = tc_desc(wts_s + (t * S::CH + 2 * kc) * COUT * 16, COUT * 16, 128);
-            const uint32_t acc = first ? 0u : 1u;
-            asm volatile(
-                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
-                    tmem + (uint32_t)(b * S::ACC_COLS)),
-                "l"(a), "l"(bd), "r"(idesc), "r"(acc)
-                : "memory");
-            first = false;
+          for (int t9 = 0; t9 < 9; ++t9) {
+            const int dy = t9 / 3, dx = t9 % 3, t = dz * 9 + t9;
+#pragma unroll
+            for (int kc = 0; kc < CIN / 16; ++kc) {
+              const uint64_t a = tc_desc_at(a0, ((dy * S::CH + 2 * kc) * kTcP + dx) * 16);
+              const uint64_t bd = tc_desc_at(b0, (t * S::CH + 2 * kc) * COUT * 16);
+              const uint32_t acc = first ? 0u : 1u;
+              asm volatile(
+                  "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                  " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+                  "l"(a), "l"(bd), "r"(idesc), "r"(acc)
+                  : "memory");
+              first = false;
+            }
           }
         }
         asm volatile(
@@ -430,9 +453,12 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
           failed = true;
           break;
         }
+        // the next plane's copies first, so that they run during the epilogue
+        if (z + 1 < ze) load_plane(x0, y, z + 2);
         epilogue(x0, y, z - 1, b ^ 1);
+      } else if (z + 1 < ze) {
+        load_plane(x0, y, z + 2);
       }
-      if (z + 1 < ze) load_plane(x0, y, z + 2);
     }
     if (failed) break;
     if (!wait_mma((ze - 1) & 1)) {
