@@ -195,6 +195,40 @@ DEFAULT_WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__fil
                                              "unet_line_c3.npz")
 
 
+def time_application(nx, ny, nz, repeat=3, warmup=2, weights=DEFAULT_WEIGHTS, seed=0):
+    """Time one forward application of the network on seeded inputs of nx x ny x nz cells
+    (residual and ln K standard normal, C uniform in [0, 1)) with CUDA events on the stream of
+    the launches; returns (ms per application, TFLOP/s)."""
+    import os
+    import torch
+    lib = load_library()
+    net = UNet(0)
+    if weights and os.path.exists(weights):
+        net.load(weights)
+    n = nx * ny * nz
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    r = torch.randn(n, device="cuda", generator=g)
+    lnk = torch.randn(n, device="cuda", generator=g)
+    cap = torch.rand(n, device="cuda", generator=g)
+    y = torch.empty(n, device="cuda")
+    st = torch.cuda.Stream()
+
+    def app():
+        check(lib.frehg_unet_forward(net.handle, nx, ny, nz, r.data_ptr(), lnk.data_ptr(),
+                                     cap.data_ptr(), y.data_ptr(), st.cuda_stream), "forward")
+
+    for _ in range(warmup):
+        app()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(repeat):
+        app()
+    e1.record(st)
+    st.synchronize()
+    ms = e0.elapsed_time(e1) / repeat
+    return ms, UNet.flops(nx, ny, nz) / (ms * 1e-3) / 1e12
+
+
 def main(argv=None):
     """Train the preconditioner network with the layered-soil recipe and save it:
     pairs from plain solves of `--seeds` three-layer soils (seeds 100, 101, ...) at the given
@@ -211,9 +245,17 @@ def main(argv=None):
     ap.add_argument("--shape", type=int, nargs=3, default=(128, 128, 64))
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--apply", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="instead of training: time the saved network's forward application")
+    ap.add_argument("--repeat", type=int, default=3)
     a = ap.parse_args(argv)
     from .build import build
     build()
+    if a.apply:
+        ms, tf = time_application(*a.apply, repeat=a.repeat, weights=a.out)
+        print(json.dumps({"cells": list(a.apply), "ms_per_application": round(ms, 3),
+                          "tflops": round(tf, 1)}))
+        return 0
     t0 = time.time()
     data = generate_pairs(list(range(100, 100 + a.seeds)), *a.shape, pc=a.pc)
     held = generate_pairs([99], *a.shape, snapshots=(3,), pc=a.pc)
