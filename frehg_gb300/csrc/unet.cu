@@ -468,7 +468,7 @@ static void conv(const bf16* in, int in_stride, int in_off, const bf16* W, const
                            Z::SMEM);
       per_sm = tc_blocks_per_sm(Z::SMEM, Z::TMEM_COLS);
     }
-    const long items = (long)((nx + kTcM - 1) / kTcM) * ny * ((nz + kTcZC - 1) / kTcZC);
+    const long items = (long)tc_tiles_x(nx) * tc_tiles_y(ny) * ((nz + kTcZC - 1) / kTcZC);
     const int grid = (int)std::min<long>(items, (long)kNumSMs * per_sm);
     k_conv3_tcz<CIN, COUT><<<grid, 128, Z::SMEM, st>>>(in, in_stride, in_off, W, bias, out,
                                                        out_stride, out_off, nx, ny, nz,
@@ -482,7 +482,7 @@ static void conv(const bf16* in, int in_stride, int in_off, const bf16* W, const
                          S::SMEM);
     per_sm = tc_blocks_per_sm(S::SMEM, S::TMEM_COLS);
   }
-  const long tiles = (long)((nx + kTcM - 1) / kTcM) * ny * nz;
+  const long tiles = (long)tc_tiles_x(nx) * tc_tiles_y(ny) * nz;
   const int grid = (int)std::min<long>(tiles, (long)kNumSMs * per_sm);
   k_conv3_tc<CIN, COUT><<<grid, 128, S::SMEM, st>>>(in, in_stride, in_off, W, bias, out,
                                                     out_stride, out_off, nx, ny, nz,

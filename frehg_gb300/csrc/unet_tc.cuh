@@ -1,24 +1,27 @@
 // The U-Net's 3x3x3 convolutions on the fifth-generation tensor cores (tcgen05, accumulators in
 // tensor memory).  Not in reference.
 //
-// Implicit GEMM per tile of 128 consecutive x pixels of one (y, z) row: D[128 x COUT] (FP32, in
-// TMEM) = sum over the 27 taps and the input channels of A[128 x 16] . B[16 x COUT], one
-// tcgen05.mma.cta_group::1.kind::f16 (BF16 operands, FP32 accumulation, M = 128, N = COUT,
+// Implicit GEMM per tile of 8 x 16 pixels (x, y) of one z plane: D[128 x COUT] (FP32, in TMEM;
+// row r = 8 py + px) = sum over the 27 taps and the input channels of A[128 x 16] . B[16 x COUT],
+// one tcgen05.mma.cta_group::1.kind::f16 (BF16 operands, FP32 accumulation, M = 128, N = COUT,
 // K = 16) per tap and 16-channel slice.  Operands sit in shared memory in the no-swizzle
 // K-major core-matrix layout, which the channels-last activations reach by splitting the
 // channels into 8-channel chunks:
-//   input rows  [dy][chunk][pixel][8]  (pixels x0-1 .. x0+128, zero outside the grid):
-//               a tap (dx, dy) is the 128-row view starting at pixel dx of row dy, K-adjacent
-//               core matrices one chunk plane (130 x 16 bytes) apart, M-adjacent ones 128 bytes;
+//   input patch [chunk][hy][hx][8]  (the 10 x 18 pixels x0-1 .. x0+8, y0-1 .. y0+16 of a plane,
+//               zero outside the grid): a tap (dx, dy) is the view starting at pixel
+//               (dx, dy); its M-adjacent core matrices (eight pixels of one patch row) are one
+//               patch row (160 bytes) apart, its K-adjacent ones one chunk plane (2880 bytes);
 //   weights     [tap][chunk][o][8]:  N-adjacent core matrices 128 bytes apart, K-adjacent ones
 //               COUT x 16 bytes.
-// A block (one warpgroup) walks its tiles; per tile it loads one z plane of input rows and the
-// nine taps' weights of that plane with 16-byte cp.async copies (zero fill outside the grid),
-// one thread issues the plane's MMAs and commits them to an mbarrier, and the block waits for
-// them before the next plane's copies reuse the buffers.  The four warps then read the
-// accumulator lanes (tcgen05.ld 32x32b: warp w owns lanes 32w .. 32w+31 = pixels), add the bias,
-// apply the ReLU and store BF16.  Several blocks per SM (shared memory, tensor-memory columns
-// permitting) overlap one block's copies with another's MMAs.
+// Two-dimensional tiles stage 180 pixels per plane where a 128-pixel row tile needs three rows of
+// 130, which leaves shared memory for more resident blocks and deeper copy pipelines.
+// k_conv3_tc: a block (one warpgroup) walks its tiles; per z plane it loads the plane's patch and
+// the nine taps' weights of that plane with 16-byte cp.async copies, one thread issues the plane's
+// MMAs and commits them to an mbarrier, and the block waits for them before the next plane's
+// copies reuse the buffers.  The four warps then read the accumulator lanes (tcgen05.ld 32x32b:
+// warp w owns lanes 32w .. 32w+31 = rows), add the bias, apply the ReLU and store BF16.  Several
+// blocks per SM (shared memory, tensor-memory columns permitting) overlap one block's copies with
+// another's MMAs.
 //
 // Every wait is bounded: a wait that runs out records an error word and the block stops
 // issuing work, waits (bounded) for its MMAs in flight, frees its tensor memory and returns.
@@ -31,16 +34,22 @@
 namespace fg {
 namespace unet {
 
-constexpr int kTcM = 128;       // pixels per tile
-constexpr int kTcP = kTcM + 2;  // with the x halo
+constexpr int kTcM = 128;                       // pixels per tile (the MMA's M)
+constexpr int kTcTX = 8, kTcTY = 16;             // the tile: 8 x 16 pixels, row r = 8 py + px
+constexpr int kTcHX = kTcTX + 2, kTcHY = kTcTY + 2;  // with the halo
+constexpr int kTcHP = kTcHX * kTcHY;             // 180 staged pixels per plane
 constexpr long kTcSpin = 1L << 24;
+
+// tiles of an nx x ny plane
+__host__ __device__ inline int tc_tiles_x(int nx) { return (nx + kTcTX - 1) / kTcTX; }
+__host__ __device__ inline int tc_tiles_y(int ny) { return (ny + kTcTY - 1) / kTcTY; }
 
 template <int CIN, int COUT>
 struct TcShape {
   static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 128, "channel counts");
   static constexpr int CH = CIN / 8;
-  static constexpr int PLANE = kTcP * 16;              // one chunk plane of a row
-  static constexpr int ROWS = 3 * CH * PLANE;          // dy = -1, 0, 1
+  static constexpr int PLANE = kTcHP * 16;             // one chunk plane of a patch
+  static constexpr int ROWS = CH * PLANE;              // one z plane's patch
   static constexpr int WTS = 9 * CH * COUT * 16;       // the nine taps of one z plane
   static constexpr int SMEM = ROWS + WTS + 128;        // + alignment slack
   static constexpr int TMEM_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
@@ -65,8 +74,10 @@ __host__ __device__ constexpr uint32_t tc_idesc(int n) {
          ((uint32_t)(kTcM >> 4) << 24);
 }
 
+// 16-byte copy global -> shared with zero fill past `bytes`, through L1: a thread's chunks of one
+// pixel share 32-byte sectors, which L1 then serves once
 __device__ __forceinline__ void tc_cp16(void* dst, const void* src, int bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc_smem(dst)), "l"(src),
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(tc_smem(dst)), "l"(src),
                "r"(bytes)
                : "memory");
 }
@@ -85,33 +96,33 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-// Copies of the three input rows y-1, y, y+1 of plane zz (pixels x0-1 .. x0+128) into dst,
-// [dy][chunk][pixel][8], with zero fill outside the grid: thread t copies pixel t (threads 0 and
-// 1 also pixels 128 and 129), every row and chunk, so the index arithmetic is per pixel and
-// row, not per copy.
+// Copies of the patch of plane zz (pixels x0-1 .. x0+8, y0-1 .. y0+16) into dst,
+// [chunk][hy][hx][8], with zero fill outside the grid: thread t copies patch pixel t (threads
+// 0-51 also pixel 128 + t), every chunk, so the index arithmetic is per pixel, not per copy.
 template <int CH>
-__device__ __forceinline__ void tc_load_rows(unsigned char* dst, const __nv_bfloat16* in,
-                                             int in_stride, int in_off, int x0, int y, int zz,
-                                             int nx, int ny, int nz, int tid) {
+__device__ __forceinline__ void tc_load_patch(unsigned char* dst, const __nv_bfloat16* in,
+                                              int in_stride, int in_off, int x0, int y0, int zz,
+                                              int nx, int ny, int nz, int tid) {
   const bool zok = zz >= 0 && zz < nz;
 #pragma unroll
   for (int half = 0; half < 2; ++half) {
     const int p = half ? kTcM + tid : tid;
-    if (half && p >= kTcP) break;
-    const int xx = x0 + p - 1;
-    const bool xok = zok && xx >= 0 && xx < nx;
+    if (half && p >= kTcHP) break;
+    const int xx = x0 + p % kTcHX - 1, yy = y0 + p / kTcHX - 1;
+    const bool ok = zok && xx >= 0 && xx < nx && yy >= 0 && yy < ny;
+    const __nv_bfloat16* src =
+        ok ? in + ((size_t)xx + (size_t)nx * ((size_t)yy + (size_t)ny * zz)) * in_stride + in_off
+           : in;
+    unsigned char* d = dst + p * 16;
 #pragma unroll
-    for (int dy = 0; dy < 3; ++dy) {
-      const int yy = y + dy - 1;
-      const bool ok = xok && yy >= 0 && yy < ny;
-      const __nv_bfloat16* src =
-          ok ? in + ((size_t)xx + (size_t)nx * ((size_t)yy + (size_t)ny * zz)) * in_stride + in_off
-             : in;
-      unsigned char* d = dst + (dy * CH * kTcP + p) * 16;
-#pragma unroll
-      for (int c = 0; c < CH; ++c) tc_cp16(d + c * kTcP * 16, ok ? src + 8 * c : in, ok ? 16 : 0);
-    }
+    for (int c = 0; c < CH; ++c) tc_cp16(d + c * kTcHP * 16, ok ? src + 8 * c : in, ok ? 16 : 0);
   }
+}
+
+// byte offset of tap (dx, dy)'s view and of 16-channel slice kc in a patch
+template <int CH>
+__host__ __device__ constexpr uint32_t tc_tap_offset(int dx, int dy, int kc) {
+  return (uint32_t)(((2 * kc) * kTcHP + dy * kTcHX + dx) * 16);
 }
 
 // A descriptor advanced by a byte offset (a multiple of 16): the start address is the low
@@ -161,18 +172,18 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
   uint32_t phase = 0;
   int pending = 0;  // MMAs committed and not yet waited for
 
-  const int xt = (nx + kTcM - 1) / kTcM;
-  const long tiles = (long)xt * ny * nz;
+  const int xt = tc_tiles_x(nx), yt = tc_tiles_y(ny);
+  const long tiles = (long)xt * yt * nz;
   for (long tile = blockIdx.x; tile < tiles && !abort_flag; tile += gridDim.x) {
-    const int x0 = (int)(tile % xt) * kTcM;
+    const int x0 = (int)(tile % xt) * kTcTX;
     const long yz = tile / xt;
-    const int y = (int)(yz % ny), z = (int)(yz / ny);
+    const int y0 = (int)(yz % yt) * kTcTY, z = (int)(yz / yt);
     bool first = true;
     for (int dz = -1; dz <= 1 && !abort_flag; ++dz) {
       const int zz = z + dz;
       if (zz < 0 || zz >= nz) continue;  // zero padding: the plane adds nothing
-      // the plane's three input rows, [dy][chunk][pixel][8]
-      tc_load_rows<S::CH>(rows, in, in_stride, in_off, x0, y, zz, nx, ny, nz, tid);
+      // the plane's patch, [chunk][hy][hx][8]
+      tc_load_patch<S::CH>(rows, in, in_stride, in_off, x0, y0, zz, nx, ny, nz, tid);
       // the plane's nine taps of W[tap][o][i], [tap][chunk][o][8]
       for (int q = tid; q < 9 * S::CH * COUT; q += 128) {
         const int o = q % COUT, c = (q / COUT) % S::CH, t9 = q / (COUT * S::CH);
@@ -187,14 +198,14 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (tid == 0) {
-        const uint64_t a0 = tc_desc(rows_s, S::PLANE, 128);
+        const uint64_t a0 = tc_desc(rows_s, S::PLANE, kTcHX * 16);
         const uint64_t b0 = tc_desc(wts_s, COUT * 16, 128);
 #pragma unroll
         for (int t9 = 0; t9 < 9; ++t9) {
           const int dy = t9 / 3, dx = t9 % 3;
 #pragma unroll
           for (int kc = 0; kc < CIN / 16; ++kc) {
-            const uint64_t a = tc_desc_at(a0, ((dy * S::CH + 2 * kc) * kTcP + dx) * 16);
+            const uint64_t a = tc_desc_at(a0, tc_tap_offset<S::CH>(dx, dy, kc));
             const uint64_t b = tc_desc_at(b0, (t9 * S::CH + 2 * kc) * COUT * 16);
             const uint32_t acc = first ? 0u : 1u;
             asm volatile(
@@ -226,9 +237,9 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
     if (abort_flag) break;
     // epilogue: warp w reads TMEM lanes 32w .. 32w+31 (its 32 pixels), 16 columns at a time
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int px = x0 + warp * 32 + lane;
+    const int r = warp * 32 + lane, px = x0 + (r & 7), py = y0 + (r >> 3);
     __nv_bfloat16* dst =
-        out + ((size_t)px + (size_t)nx * ((size_t)y + (size_t)ny * z)) * out_stride + out_off;
+        out + ((size_t)px + (size_t)nx * ((size_t)py + (size_t)ny * z)) * out_stride + out_off;
 #pragma unroll
     for (int cb = 0; cb < COUT; cb += 16) {
       uint32_t r[16];
@@ -252,7 +263,7 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
         __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
         packed[q] = *reinterpret_cast<uint32_t*>(&h);
       }
-      if (px < nx) {
+      if (px < nx && py < ny) {
         uint4* d4 = reinterpret_cast<uint4*>(dst + cb);
         d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
         d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
@@ -273,8 +284,8 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
 // ---------------------------------------------------------------------------------------------
 // Pipelined form for the layers whose 27 taps of weights stay resident in shared memory
 // (27 x CIN x COUT x 2 bytes <= 64 KB: all level-1 layers and the narrower level-2 ones).
-// A block walks columns of ZC tiles along z at one (x tile, y): a ring of four slots holds
-// input planes (three rows each, [slot][dy][chunk][pixel][8]); each tile needs one new plane,
+// A block walks columns of ZC tiles along z at one (x, y) tile: a ring of four slots holds
+// input planes (one patch each, [slot][chunk][hy][hx][8]); each tile needs one new plane,
 // loaded one tile ahead with cp.async while the previous tile's MMAs run, and two tensor-memory
 // accumulators let the epilogue of tile z-1 overlap the MMAs of tile z:
 //   wait for plane z+1, barrier; issue MMA(z) -> acc[z&1], commit;
@@ -288,8 +299,8 @@ template <int CIN, int COUT>
 struct TcZShape {
   static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
   static constexpr int CH = CIN / 8;
-  static constexpr int PLANE = kTcP * 16;
-  static constexpr int SLOT = 3 * CH * PLANE;          // one input plane: rows dy = -1, 0, 1
+  static constexpr int PLANE = kTcHP * 16;
+  static constexpr int SLOT = CH * PLANE;              // one input plane's patch
   static constexpr int WTS = 27 * CH * COUT * 16;      // all taps, [tap][chunk][o][8]
   static constexpr int SMEM = WTS + 4 * SLOT + 128;
   static constexpr int ACC_COLS = COUT <= 16 ? 16 : (COUT <= 32 ? 32 : 64);
@@ -343,18 +354,18 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
   int outstanding[2] = {0, 0};  // MMAs committed to mma_bar[b] and not yet waited for
   bool failed = false;
 
-  // copies of input plane zz (three rows) into ring slot zz & 3, zero outside the grid
-  auto load_plane = [&](int x0, int y, int zz) {
-    tc_load_rows<S::CH>(ring + (zz & 3) * S::SLOT, in, in_stride, in_off, x0, y, zz, nx, ny, nz,
-                        tid);
+  // copies of input plane zz's patch into ring slot zz & 3, zero outside the grid
+  auto load_plane = [&](int x0, int y0, int zz) {
+    tc_load_patch<S::CH>(ring + (zz & 3) * S::SLOT, in, in_stride, in_off, x0, y0, zz, nx, ny, nz,
+                         tid);
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  // bias + ReLU + BF16 store of tile (x0, y, z) from accumulator b
-  auto epilogue = [&](int x0, int y, int z, int b) {
+  // bias + ReLU + BF16 store of tile (x0, y0, z) from accumulator b
+  auto epilogue = [&](int x0, int y0, int z, int b) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int px = x0 + warp * 32 + lane;
+    const int r = warp * 32 + lane, px = x0 + (r & 7), py = y0 + (r >> 3);
     __nv_bfloat16* dst =
-        out + ((size_t)px + (size_t)nx * ((size_t)y + (size_t)ny * z)) * out_stride + out_off;
+        out + ((size_t)px + (size_t)nx * ((size_t)py + (size_t)ny * z)) * out_stride + out_off;
 #pragma unroll
     for (int cb = 0; cb < COUT; cb += 16) {
       uint32_t r[16];
@@ -378,7 +389,7 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
         __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
         packed[q] = *reinterpret_cast<uint32_t*>(&h);
       }
-      if (px < nx) {
+      if (px < nx && py < ny) {
         uint4* d4 = reinterpret_cast<uint4*>(dst + cb);
         d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
         d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
@@ -398,17 +409,17 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
     return true;
   };
 
-  const int xt = (nx + kTcM - 1) / kTcM;
+  const int xt = tc_tiles_x(nx), yt = tc_tiles_y(ny);
   const int zcols = (nz + kTcZC - 1) / kTcZC;
-  const long items = (long)xt * ny * zcols;
+  const long items = (long)xt * yt * zcols;
   for (long item = blockIdx.x; item < items && !failed; item += gridDim.x) {
-    const int x0 = (int)(item % xt) * kTcM;
+    const int x0 = (int)(item % xt) * kTcTX;
     const long rest = item / xt;
-    const int y = (int)(rest % ny);
-    const int zb = (int)(rest / ny) * kTcZC, ze = min(nz, zb + kTcZC);
-    load_plane(x0, y, zb - 1);
-    load_plane(x0, y, zb);
-    load_plane(x0, y, zb + 1);
+    const int y0 = (int)(rest % yt) * kTcTY;
+    const int zb = (int)(rest / yt) * kTcZC, ze = min(nz, zb + kTcZC);
+    load_plane(x0, y0, zb - 1);
+    load_plane(x0, y0, zb);
+    load_plane(x0, y0, zb + 1);
     for (int z = zb; z < ze; ++z) {
       const int b = z & 1;
       // planes z-1, z, z+1 (and, the first time, the weights) have landed
@@ -424,13 +435,14 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
         for (int dz = 0; dz < 3; ++dz) {
           const int zz = z + dz - 1;
           if (zz < 0 || zz >= nz) continue;  // zero padding
-          const uint64_t a0 = tc_desc(ring_s + (uint32_t)((zz & 3) * S::SLOT), S::PLANE, 128);
+          const uint64_t a0 =
+              tc_desc(ring_s + (uint32_t)((zz & 3) * S::SLOT), S::PLANE, kTcHX * 16);
 #pragma unroll
           for (int t9 = 0; t9 < 9; ++t9) {
             const int dy = t9 / 3, dx = t9 % 3, t = dz * 9 + t9;
 #pragma unroll
             for (int kc = 0; kc < CIN / 16; ++kc) {
-              const uint64_t a = tc_desc_at(a0, ((dy * S::CH + 2 * kc) * kTcP + dx) * 16);
+              const uint64_t a = tc_desc_at(a0, tc_tap_offset<S::CH>(dx, dy, kc));
               const uint64_t bd = tc_desc_at(b0, (t * S::CH + 2 * kc) * COUT * 16);
               const uint32_t acc = first ? 0u : 1u;
               asm volatile(
@@ -454,10 +466,10 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
           break;
         }
         // the next plane's copies first, so that they run during the epilogue
-        if (z + 1 < ze) load_plane(x0, y, z + 2);
-        epilogue(x0, y, z - 1, b ^ 1);
+        if (z + 1 < ze) load_plane(x0, y0, z + 2);
+        epilogue(x0, y0, z - 1, b ^ 1);
       } else if (z + 1 < ze) {
-        load_plane(x0, y, z + 2);
+        load_plane(x0, y0, z + 2);
       }
     }
     if (failed) break;
@@ -465,7 +477,7 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
       failed = true;
       break;
     }
-    epilogue(x0, y, ze - 1, (ze - 1) & 1);
+    epilogue(x0, y0, ze - 1, (ze - 1) & 1);
     __syncthreads();  // the next column's first copies reuse slots the last epilogue's MMAs read
   }
   // MMAs still in flight after a wait that ran out finish before the tensor memory is freed
