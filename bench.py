@@ -478,6 +478,23 @@ def time_arm(args, w, net, stream, barrier, steps, warmup):
     return s, ms, d, reset
 
 
+def step_roofline(args, w, cnt, ms):
+    """The whole timed region against the copy peak, with the hot-path scope table's per-cell
+    algorithmic bytes: 16 per step (step-start copy), 72 + 32 per Picard iteration (or per PCA
+    step: assembly, update/corrector) and 80 per Krylov iteration in FP64, 40 per FP32 inner
+    iteration (half the vector and coefficient bytes)."""
+    its = cnt["picard_iterations"] if args.scheme == "picard" else args.steps
+    per_krylov = 40.0 if args.precision == "mixed" else 80.0
+    b = w.cells * (16.0 * args.steps + 104.0 * its + per_krylov * cnt["ksp_iterations"])
+    gbs = b / (ms / 1000.0) / 1e9
+    peak, kind = measured_peaks()
+    return {"bytes_per_step": b / args.steps, "achieved": gbs, "peak": peak, "unit": "GB/s",
+            "frac": gbs / peak, "peak_source": kind,
+            "formula": "cells x (16 x steps + 104 x " +
+                       ("Picard iterations" if args.scheme == "picard" else "steps") +
+                       f" + {per_krylov:.0f} x Krylov iterations)"}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -573,9 +590,14 @@ def run_gpu(args):
         "kernel_compulsory_bytes_per_cell": dom["bytes_per_launch"] / w.cells,
         "ms_per_launch": per_launch_ms,
         "share_of_step": dom["total_ms"] / tot,
-        "kernels": {st["name"]: {"launches": st["launches"], "ms": round(st["total_ms"], 4),
+        # GBps: algorithmic bytes of the launches that did work (inner Krylov iterations are
+        # launched in whole chunks; those after convergence return at once: idle_launches)
+        "kernels": {st["name"]: {"launches": st["launches"],
+                                 "idle_launches": st.get("idle_launches", 0),
+                                 "ms": round(st["total_ms"], 4),
                                  "share": round(st["total_ms"] / tot, 4),
-                                 "GBps": round(st["bytes_per_launch"] * st["launches"] /
+                                 "GBps": round(st["bytes_per_launch"] *
+                                               (st["launches"] - st.get("idle_launches", 0)) /
                                                (st["total_ms"] / 1000.0) / 1e9, 1)
                                  if st["total_ms"] > 0 else 0.0,
                                  # ncu's FP64-pipe active fraction (profiles/), the bound of the
@@ -658,7 +680,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(q_host.numel() * 8),
                 "d2h_bytes_per_step": int(h_host.numel() * 8 + wc_host.numel() * 8)},
-        "roofline": roofline,
+        "roofline": dict(roofline, step=step_roofline(args, w, cnt, ms_max)),
         "roofline_network": net_roof,
         "learned": learned_rec,
         "cpu_baseline": cpu,

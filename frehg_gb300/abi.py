@@ -183,6 +183,7 @@ class KernelStat(C.Structure):
         ("launches", C.c_int64),
         ("total_ms", C.c_double),
         ("bytes_per_launch", C.c_double),
+        ("idle_launches", C.c_int64),
     ]
 
 

@@ -53,11 +53,14 @@ class Profiler {
   void end(int slot, cudaStream_t st, const char* name, double bytes);
   // after the stream has been synchronised: fold finished event pairs into the table
   int flush();
+  // n launches of `name` (already flushed) returned without work
+  void idle(const char* name, int64_t n);
   struct Stat {
     std::string name;
     int64_t launches = 0;
     double ms = 0.0;
     double bytes = 0.0;
+    int64_t idle = 0;
   };
   std::vector<Stat> stats;
 

@@ -1114,6 +1114,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     }
     for (int q = 0; !use_net && q < cfg.max_it / chunk + 2 && hst32->status == 0; ++q) {
       const int iters = q == 0 ? chunk0 : chunk;
+      const int its_before = hst32->its;
       if (prof && prof->on) {
         for (int it = 0; it < iters; ++it) {
           if (line) {
@@ -1138,7 +1139,20 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       }
       FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
       FG_CUDA(cudaStreamSynchronize(st));
-      if (prof && prof->on) FG_TRY(prof->flush());
+      if (prof && prof->on) {
+        FG_TRY(prof->flush());
+        // the chunk's iterations after convergence returned at once
+        const int64_t idle = iters - std::min(iters, std::max(0, hst32->its - its_before));
+        if (line) {
+          prof->idle(vec4 ? "k32_spmv_v4" : "k32_spmv", idle);
+          prof->idle("k32_line_fwd", idle);
+          prof->idle("k32_line_bwd", idle);
+        } else {
+          prof->idle("k32_p", idle);
+          prof->idle(vec4 ? "k32_spmv_v4" : "k32_spmv", idle);
+          prof->idle("k32_update", idle);
+        }
+      }
     }
     inner_total += hst32->its;
     if (dbg)

@@ -51,6 +51,12 @@ void Profiler::end(int slot, cudaStream_t st, const char* name, double bytes) {
   cudaEventRecord(p.b, st);
 }
 
+void Profiler::idle(const char* name, int64_t n) {
+  if (!on || n <= 0) return;
+  for (auto& q : stats)
+    if (q.name == name) q.idle += n;
+}
+
 int Profiler::flush() {
   for (auto& p : pending_) {
     float ms = 0.0f;

@@ -1662,6 +1662,7 @@ int frehg_re_kernel_stats(frehg_re* re, frehg_kernel_stat* out, int max, int* co
     out[q].launches = s.launches;
     out[q].total_ms = s.ms;
     out[q].bytes_per_launch = s.bytes;
+    out[q].idle_launches = s.idle;
   }
   return FREHG_OK;
 }

@@ -272,7 +272,8 @@ class ReSolver:
         arr = (KernelStat * max(n.value, 1))()
         check(self._lib.frehg_re_kernel_stats(self._h, arr, n.value, C.byref(n)), "kernelStats")
         return [dict(name=a.name.decode(), launches=a.launches, total_ms=a.total_ms,
-                     bytes_per_launch=a.bytes_per_launch) for a in arr[:n.value]]
+                     bytes_per_launch=a.bytes_per_launch, idle_launches=a.idle_launches)
+                for a in arr[:n.value]]
 
     def set_stream(self, cuda_stream: int | None):
         check(self._lib.frehg_re_set_stream(self._h, C.c_void_p(cuda_stream or 0)), "setStream")

@@ -216,12 +216,16 @@ int frehg_re_boundary_volumes(frehg_re* re, double* top_in, double* bottom_in);
 /* Per-kernel timing (not in reference; benchmarking aid).  While profiling is on, every kernel
  * the handle launches is bracketed by CUDA events on the handle's stream (the Krylov loop then
  * runs without its CUDA graph), and duration, launch count and the algorithmic bytes of one
- * launch are accumulated per kernel name.  Turning profiling on clears the table. */
+ * launch are accumulated per kernel name.  idle_launches counts the launches of the inner
+ * Krylov iterations that found their solve already converged and returned at once (the inner
+ * loop launches whole chunks of iterations); their bytes are not moved.  Turning profiling on
+ * clears the table. */
 typedef struct frehg_kernel_stat {
   char name[32];
   int64_t launches;
   double total_ms;
   double bytes_per_launch;
+  int64_t idle_launches;
 } frehg_kernel_stat;
 int frehg_re_set_profiling(frehg_re* re, int on);
 int frehg_re_kernel_stats(frehg_re* re, frehg_kernel_stat* out, int max, int* count);
