@@ -95,7 +95,8 @@ __device__ __forceinline__ ff ff_face_mean(int harmonic, ff lo, ff hi) {
 __device__ __forceinline__ ff ff_face_flux(ff kf, ff g, ff hn, ff h, float* t) {
   const ff tt = ff_mul_lean(kf, g);
   *t = tt.h;
-  return ff_mul_lean(tt, ff_dif_lean(hn, h));
+  // the head difference renormalised (SloppyDWPlusDW): the product keeps it to 2^-48 of itself
+  return ff_mul_lean(tt, ff_add_fast(hn, ff_neg(h)));
 }
 
 // The flux into the upper cell (head hu) from the lower one (head hd) through their common z
@@ -180,7 +181,7 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
 // The Picard residual's float-float part V Ss (wcn/ths) (h - h_old) - dt q, renormalised (the
 // storage difference and the final combination are FP64)
 __device__ __forceinline__ ff ff_residual_rest(ff V, ff dt, ff st, ff h, double h_old, ff q) {
-  const ff dh = ff_dif_lean(h, ff_from_double_nb(h_old));
+  const ff dh = ff_add_fast(h, ff_neg(ff_from_double_nb(h_old)));  // renormalised, as in faces
   FfSum r = ff_sum_of(ff_mul_lean(V, ff_mul_lean(st, dh)));
   ff_sum_add(r, ff_neg(ff_mul_lean(dt, q)));
   return ff_sum_value(r);
