@@ -579,7 +579,8 @@ def run_gpu(args):
     del s
     tot = sum(st["total_ms"] for st in stats) or 1.0
     dom = max(stats, key=lambda st: st["total_ms"])
-    per_launch_ms = dom["total_ms"] / dom["launches"]
+    # per launch that did work (inner Krylov launches after convergence return at once)
+    per_launch_ms = dom["total_ms"] / max(1, dom["launches"] - dom.get("idle_launches", 0))
     scope_bpc = SCOPE_BYTES_PER_CELL.get(dom["name"])
     alg_bytes = scope_bpc * w.cells if scope_bpc else dom["bytes_per_launch"]
     achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
