@@ -546,7 +546,9 @@ def run_gpu(args):
     h_fast = s.interior("h").copy()
 
     # end to end through the public API: per step H2D of the top forcing (rain or qtop per
-    # column) from pinned host memory, the step, D2H of the head and water-content fields
+    # column) from pinned host memory, the step, D2H of the head and water-content fields into
+    # pinned memory (asynchronous: each step's copy overlaps the next step; the timer stops
+    # after the last copy has landed)
     reset()
     qv = w.params.rain_rate if w.params.rain_rate != 0.0 else w.params.qtop
     q_host = torch.full((w.ny * w.nx,), float(qv), dtype=torch.float64).pin_memory()
@@ -560,8 +562,9 @@ def run_gpu(args):
     for _ in range(args.steps):
         s.set_top_flux_field(qn)
         s.advance_step()
-        s.interior("h", out=hn)
-        s.interior("wc", out=wn)
+        s.interior_async("h", hn)
+        s.interior_async("wc", wn)
+    s.sync()
     e1.record(stream)
     stream.synchronize()
     barrier()

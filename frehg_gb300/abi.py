@@ -223,6 +223,7 @@ SIGNATURES = {
     "frehg_re_time": (C.c_int, [_VP, _PD]),
     "frehg_re_get_field": (C.c_int, [_VP, C.c_char_p, _PD]),
     "frehg_re_get_interior": (C.c_int, [_VP, C.c_char_p, _PD, C.c_int]),
+    "frehg_re_get_interior_async": (C.c_int, [_VP, C.c_char_p, _PD]),
     "frehg_re_get_counters": (C.c_int, [_VP, C.POINTER(ReCounters)]),
     "frehg_re_water_volume": (C.c_int, [_VP, _PD]),
     "frehg_re_boundary_volumes": (C.c_int, [_VP, _PD, _PD]),

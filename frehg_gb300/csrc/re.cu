@@ -29,6 +29,12 @@ struct frehg_re {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   int cur = 0;
+  // asynchronous result copies (frehg_re_get_interior_async): their stream, the event after the
+  // last copy out of state buffer q (H[q], W[q]) and whether it may still be in flight
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[2] = {nullptr, nullptr};
+  cudaEvent_t issue_ev = nullptr;
+  bool copy_pending[2] = {false, false};
   // state
   double* H[2] = {nullptr, nullptr};
   double* W[2] = {nullptr, nullptr};
@@ -108,7 +114,29 @@ frehg_re::~frehg_re() {
   cudaFree(lnk_f);
   cudaFree(cap_f);
   A.release();
+  if (copy_stream) {
+    cudaStreamSynchronize(copy_stream);
+    cudaStreamDestroy(copy_stream);
+  }
+  for (cudaEvent_t e : {copy_ev[0], copy_ev[1], issue_ev})
+    if (e) cudaEventDestroy(e);
   if (own_stream) cudaStreamDestroy(own_stream);
+}
+
+// Before work that writes state buffer q (-1: both): the handle's stream waits on the device for
+// the result copies still reading it; host: the host waits for them (entry points that write
+// the buffers with synchronous copies).
+static int wait_copies(frehg_re* re, int q, bool host) {
+  for (int b = 0; b < 2; ++b) {
+    if ((q >= 0 && b != q) || !re->copy_pending[b]) continue;
+    if (host) {
+      FG_CUDA(cudaEventSynchronize(re->copy_ev[b]));
+    } else {
+      FG_CUDA(cudaStreamWaitEvent(re->stream, re->copy_ev[b], 0));
+    }
+    re->copy_pending[b] = false;
+  }
+  return FREHG_OK;
 }
 
 
@@ -852,6 +880,8 @@ static int picard_step(frehg_re* re) {
 }
 
 static int advance_one(frehg_re* re) {
+  // the step writes the other state buffer: copies of the current one run on during it
+  FG_TRY(wait_copies(re, 1 - re->cur, false));
   if (!re->finalized) {
     set_error("advance_step before finalize_initial_state");
     return FREHG_ERR_STATE;
@@ -956,6 +986,7 @@ int frehg_re_destroy(frehg_re* re) {
   clear_error();
   if (re) {
     cudaStreamSynchronize(re->stream);
+    if (re->copy_stream) cudaStreamSynchronize(re->copy_stream);
     delete re;
   }
   return FREHG_OK;
@@ -1069,6 +1100,7 @@ int frehg_re_initialize_geometry(frehg_re* re) {
 int frehg_re_set_initial_head(frehg_re* re, const double* h) {
   clear_error();
   FG_ARG(re && h, "null argument");
+  FG_TRY(wait_copies(re, -1, true));
   FG_CUDA(cudaStreamSynchronize(re->stream));
   FG_CUDA(cudaMemcpy(re->H[re->cur], h, re->n * sizeof(double), cudaMemcpyHostToDevice));
   ReArgs a = make_args(re);
@@ -1082,6 +1114,7 @@ int frehg_re_set_initial_head(frehg_re* re, const double* h) {
 int frehg_re_set_initial_water_content(frehg_re* re, const double* wc) {
   clear_error();
   FG_ARG(re && wc, "null argument");
+  FG_TRY(wait_copies(re, -1, true));
   FG_CUDA(cudaStreamSynchronize(re->stream));
   FG_CUDA(cudaMemcpy(re->W[re->cur], wc, re->n * sizeof(double), cudaMemcpyHostToDevice));
   ReArgs a = make_args(re);
@@ -1095,6 +1128,7 @@ int frehg_re_set_initial_water_content(frehg_re* re, const double* wc) {
 int frehg_re_finalize_initial_state(frehg_re* re) {
   clear_error();
   FG_ARG(re, "null handle");
+  FG_TRY(wait_copies(re, -1, true));
   if (!re->have_state) {
     set_error("finalize_initial_state before an initial head or water content");
     return FREHG_ERR_STATE;
@@ -1200,6 +1234,7 @@ int frehg_re_surface_exchange(frehg_re* re, double* eta, const double* bottom, d
                               int on_device) {
   clear_error();
   FG_ARG(re && eta && bottom && q_out && total, "null argument");
+  FG_TRY(wait_copies(re, -1, true));
   FG_ARG(dt > 0.0, "dt must be positive");
   FG_ARG(re->finalized, "surface exchange before an initial state");
   cudaStream_t st = re->stream;
@@ -1268,6 +1303,7 @@ int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state) {
 int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const double* state) {
   clear_error();
   FG_ARG(re && h && wc && state, "null argument");
+  FG_TRY(wait_copies(re, -1, true));
   FG_ARG(state[1] > 0.0 && state[2] > 0.0, "checkpoint state has no positive dt");
   FG_CUDA(cudaStreamSynchronize(re->stream));
   FG_CUDA(cudaMemcpy(re->H[re->cur], h, re->n * sizeof(double), cudaMemcpyHostToDevice));
@@ -1338,6 +1374,29 @@ int frehg_re_get_interior(frehg_re* re, const char* name, double* out, int devic
                           device_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                           re->stream));
   FG_CUDA(cudaStreamSynchronize(re->stream));
+  return FREHG_OK;
+}
+
+int frehg_re_get_interior_async(frehg_re* re, const char* name, double* out) {
+  clear_error();
+  FG_ARG(re && name && out, "null argument");
+  int q = -1;
+  if (!strcmp(name, "h") || !strcmp(name, "wc")) q = re->cur;
+  else if (!strcmp(name, "hn") || !strcmp(name, "wcn")) q = 1 - re->cur;
+  FG_ARG(q >= 0, "field '%s' has no asynchronous copy (h, wc, hn, wcn)", name);
+  const double* src = name[0] == 'h' ? re->H[q] : re->W[q];
+  if (!re->copy_stream) {
+    FG_CUDA(cudaStreamCreateWithFlags(&re->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&re->copy_ev[0], &re->copy_ev[1], &re->issue_ev})
+      FG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  // after the work issued so far on the handle's stream, on the copy stream
+  FG_CUDA(cudaEventRecord(re->issue_ev, re->stream));
+  FG_CUDA(cudaStreamWaitEvent(re->copy_stream, re->issue_ev, 0));
+  FG_CUDA(cudaMemcpyAsync(out, src, re->n * sizeof(double), cudaMemcpyDeviceToHost,
+                          re->copy_stream));
+  FG_CUDA(cudaEventRecord(re->copy_ev[q], re->copy_stream));
+  re->copy_pending[q] = true;
   return FREHG_OK;
 }
 
@@ -1691,6 +1750,7 @@ int frehg_re_boundary_volumes(frehg_re* re, double* top_in, double* bottom_in) {
 int frehg_re_set_stream(frehg_re* re, void* s) {
   clear_error();
   FG_ARG(re, "null handle");
+  FG_TRY(wait_copies(re, -1, true));
   FG_CUDA(cudaStreamSynchronize(re->stream));
   re->stream = s ? (cudaStream_t)s : re->own_stream;
   return FREHG_OK;
@@ -1700,6 +1760,7 @@ int frehg_re_sync(frehg_re* re) {
   clear_error();
   FG_ARG(re, "null handle");
   FG_CUDA(cudaStreamSynchronize(re->stream));
+  FG_TRY(wait_copies(re, -1, true));
   return FREHG_OK;
 }
 

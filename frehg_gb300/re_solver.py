@@ -233,6 +233,16 @@ class ReSolver:
         check(self._lib.frehg_re_get_interior(self._h, name.encode(), dptr(out), 0), name)
         return out
 
+    def interior_async(self, name, out: np.ndarray) -> np.ndarray:
+        """Start the copy of an interior field (h, wc, hn, wcn) into `out` (C-contiguous float64,
+        page-locked for an asynchronous copy) and return at once; the values are there after
+        sync().  The copy overlaps the next step (not in reference)."""
+        g = self.grid
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != g.nx * g.ny * g.nz:
+            raise ValueError("interior_async: out must be a C-contiguous float64 array of the grid")
+        check(self._lib.frehg_re_get_interior_async(self._h, name.encode(), dptr(out)), name)
+        return out
+
     def interior_to_device(self, name, dev_ptr: int):
         check(self._lib.frehg_re_get_interior(self._h, name.encode(),
                                               C.cast(C.c_void_p(dev_ptr), C.POINTER(C.c_double)),

@@ -186,6 +186,12 @@ int frehg_re_get_field(frehg_re* re, const char* name, double* out_halo);
 /* Interior copy (nx*ny*nz, interior order) of h, wc, hn or wcn; device_out != 0 means out is a
  * device pointer (device-to-device copy). */
 int frehg_re_get_interior(frehg_re* re, const char* name, double* out, int device_out);
+/* The same copy to host memory without waiting (not in reference): it is ordered after the work
+ * issued so far and runs on a copy stream of the handle, so that the copy of a step's result
+ * overlaps the next step (which writes the other state buffer); calls that would overwrite the
+ * copied buffer wait for it.  out must stay valid and unread until frehg_re_sync; page-locked
+ * memory (cudaHostAlloc) makes the copy asynchronous.  Names: h, wc, hn, wcn. */
+int frehg_re_get_interior_async(frehg_re* re, const char* name, double* out);
 
 /* Perf counters (src/perf: cells_touched = cells*steps ReSolver.cpp:933, ksp_iterations :621). */
 typedef struct frehg_re_counters {

@@ -342,6 +342,12 @@ class ReSolver {
     check(frehg_re_get_interior(re_, name.c_str(), out.data(), 0), "interior");
     return out;
   }
+  // start the copy of an interior field into out (size nx*ny*nz, page-locked for asynchrony);
+  // complete after sync(); the copy overlaps the next step (not in the reference)
+  void interiorAsync(const std::string& name, real* out) {
+    check(frehg_re_get_interior_async(re_, name.c_str(), out), "interiorAsync");
+  }
+  void sync() { check(frehg_re_sync(re_), "sync"); }
   real waterVolume() const {
     double v = 0.0;
     check(frehg_re_water_volume(re_, &v), "waterVolume");
