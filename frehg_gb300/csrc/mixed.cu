@@ -1141,12 +1141,15 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       FG_CUDA(cudaStreamSynchronize(st));
       if (prof && prof->on) {
         FG_TRY(prof->flush());
-        // the chunk's iterations after convergence returned at once
-        const int64_t idle = iters - std::min(iters, std::max(0, hst32->its - its_before));
+        // the chunk's iterations after convergence returned at once (the line solve's backward
+        // sweep of the converging iteration too: the forward sweep's kernel ran the test)
+        const int done = std::min(iters, std::max(0, hst32->its - its_before));
+        const int64_t idle = iters - done;
         if (line) {
           prof->idle(vec4 ? "k32_spmv_v4" : "k32_spmv", idle);
           prof->idle("k32_line_fwd", idle);
-          prof->idle("k32_line_bwd", idle);
+          prof->idle("k32_line_bwd", std::min<int64_t>(iters, idle + (hst32->status != 0 &&
+                                                                       done > 0 ? 1 : 0)));
         } else {
           prof->idle("k32_p", idle);
           prof->idle(vec4 ? "k32_spmv_v4" : "k32_spmv", idle);
