@@ -170,7 +170,14 @@ static void closed_box() {
   re.setInitialWaterContent(wc);
   re.finalizeInitialState();
   const double v0 = re.waterVolume();
-  for (int s = 0; s < 40; ++s) re.advanceStep();
+  for (int s = 0; s < 39; ++s) re.advanceStep();
+  // the last step's result copied while one more step runs: the copy holds the state before it
+  std::vector<double> h_async((size_t)nx * ny * nz);
+  const std::vector<double> h_before = re.interior("h");
+  re.interiorAsync("h", h_async.data());
+  re.advanceStep();
+  re.sync();
+  EXPECT(h_async == h_before, "interiorAsync: the copy holds the result of the step it follows");
   const double v1 = re.waterVolume();
   const double rel = std::fabs(v1 - v0) / v0;
   EXPECT(rel < 1e-10, "ReSolver closed box: water volume drift %.3e relative over 40 steps", rel);

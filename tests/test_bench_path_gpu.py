@@ -10,6 +10,8 @@ stated sizes.
 * 40x40x100 loam infiltration with the Picard scheme, 120 steps (the PCA scheme at this size is
   checked against the reference's own outputs in test_golden_gpu.py).
 * 256x256x128 heterogeneous loam: 3 PCA steps and 1 Picard step against the oracle.
+* The 512x512x128 loam's and the three-layer soil's generators on windows, Picard with the
+  mixed line-PCG solve.
 
 The oracle solves with FP64 Jacobi-PCG at the same rtol (it has no mixed precision, line or
 learned preconditioner: those change how the linear systems are solved, not their solutions).
@@ -125,3 +127,30 @@ def test_config1_full_size_picard_mixed_line(gpu_lib, oracle_mod):
     worst = compare(g, o, w.steps)
     print(f"\n  256x256x128 Picard (mixed line, float-float), 1 step: max head difference "
           f"{worst:.2e} m")
+
+
+def test_config2_window_picard_mixed_line(gpu_lib, oracle_mod):
+    """512x512x128 loam's generator (its own seeds) on a 48x48x128 window, the benchmark's
+    mixed line-PCG Picard path, 8 steps"""
+    w = W.config2("picard", nx=48, ny=48, steps=8)
+    w.solver.pc_type = b"line"
+    w.solver.ir_rtol = 1e-12
+    g, o = gpu_solver(w), oracle_solver(oracle_mod, w)
+    v0 = g.water_volume()
+    worst = compare(g, o, w.steps)
+    print(f"\n  512x512x128 generator, 48x48 window, 8 Picard steps: max head difference "
+          f"{worst:.2e} m")
+    assert budget_rel(g, v0) < 1e-12
+
+
+def test_config3_window_picard_mixed_line(gpu_lib, oracle_mod):
+    """the three-layer soil (learned-preconditioner configuration's generator) on a 24x24x128
+    window, Picard with the mixed line-PCG solve, 6 steps: the first step's attempts at 60, 30,
+    15 and 7.5 s fail to converge and the step is taken at 3.75 s, on both"""
+    w = W.config3("picard", nx=24, ny=24, steps=6, precision=1, pc="line")
+    g, o = gpu_solver(w), oracle_solver(oracle_mod, w)
+    v0 = g.water_volume()
+    worst = compare(g, o, w.steps)
+    print(f"\n  three-layer soil, 24x24x128 window, 6 Picard steps: max head difference "
+          f"{worst:.2e} m")
+    assert budget_rel(g, v0) < 1e-12
