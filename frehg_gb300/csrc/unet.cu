@@ -459,7 +459,22 @@ template <int CIN, int COUT>
 static void conv(const bf16* in, int in_stride, int in_off, const bf16* W, const float* bias,
                  bf16* out, int out_stride, int out_off, int nx, int ny, int nz, bool relu,
                  cudaStream_t st) {
-  if constexpr (TcZShape<CIN, COUT>::FITS) {
+  if constexpr (CIN <= 16 && TcPShape<CIN, COUT>::FITS) {
+    // weights resident, one MMA group per output plane (16-channel inputs)
+    using Z = TcPShape<CIN, COUT>;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+      cudaFuncSetAttribute(k_conv3_tcp<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           Z::SMEM);
+      per_sm = tc_blocks_per_sm(Z::SMEM, Z::TMEM_COLS);
+    }
+    const long items = (long)tc_tiles_x(nx) * tc_tiles_y(ny) * ((nz + kTcZC - 1) / kTcZC);
+    const int grid = (int)std::min<long>(items, (long)kNumSMs * per_sm);
+    k_conv3_tcp<CIN, COUT><<<grid, 128, Z::SMEM, st>>>(in, in_stride, in_off, W, bias, out,
+                                                       out_stride, out_off, nx, ny, nz,
+                                                       relu ? 1 : 0, tc_error_word());
+    return;
+  } else if constexpr (TcZShape<CIN, COUT>::FITS) {
     // weights resident, z columns pipelined
     using Z = TcZShape<CIN, COUT>;
     static int per_sm = 0;
@@ -468,7 +483,7 @@ static void conv(const bf16* in, int in_stride, int in_off, const bf16* W, const
                            Z::SMEM);
       per_sm = tc_blocks_per_sm(Z::SMEM, Z::TMEM_COLS);
     }
-    const long items = (long)tc_tiles_x(nx) * tc_tiles_y(ny) * ((nz + kTcZC - 1) / kTcZC);
+    const long items = (long)tc_tiles_x(nx) * tc_tiles_y(ny) * ((nz + Z::ZC - 1) / Z::ZC);
     const int grid = (int)std::min<long>(items, (long)kNumSMs * per_sm);
     k_conv3_tcz<CIN, COUT><<<grid, 128, Z::SMEM, st>>>(in, in_stride, in_off, W, bias, out,
                                                        out_stride, out_off, nx, ny, nz,

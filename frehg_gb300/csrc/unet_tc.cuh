@@ -282,8 +282,11 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
 
 
 // ---------------------------------------------------------------------------------------------
-// Pipelined form for the layers whose 27 taps of weights stay resident in shared memory
-// (27 x CIN x COUT x 2 bytes <= 64 KB: all level-1 layers and the narrower level-2 ones).
+// Per-output-plane pipelined form, for the 16-channel-input layers: their patches and weights
+// are small, and small tensor-memory accumulators (COUT columns, two of them) let six blocks
+// share an SM, which beats the dz-stacked form below for them (2.0 against 2.6 ms per
+// 16-to-16-channel layer at 768 x 768 x 96).  The 27 taps of weights stay resident in shared
+// memory (27 x CIN x COUT x 2 bytes <= 64 KB).
 // A block walks columns of ZC tiles along z at one (x, y) tile: a ring of four slots holds
 // input planes (one patch each, [slot][chunk][hy][hx][8]); each tile needs one new plane,
 // loaded one tile ahead with cp.async while the previous tile's MMAs run, and two tensor-memory
@@ -293,10 +296,10 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
 //   reader); epilogue(z-1) from acc[(z-1)&1] while those copies land.
 // The MMA issue is unrolled over the taps and channel slices with the descriptors advanced by
 // constant offsets.
-constexpr int kTcZC = 16;  // tiles of one z column
+constexpr int kTcZC = 16;  // output planes of one z column
 
 template <int CIN, int COUT>
-struct TcZShape {
+struct TcPShape {
   static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
   static constexpr int CH = CIN / 8;
   static constexpr int PLANE = kTcHP * 16;
@@ -309,17 +312,17 @@ struct TcZShape {
 };
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restrict__ in,
+__global__ void __launch_bounds__(128) k_conv3_tcp(const __nv_bfloat16* __restrict__ in,
                                                    int in_stride, int in_off,
                                                    const __nv_bfloat16* __restrict__ W,
                                                    const float* __restrict__ bias,
                                                    __nv_bfloat16* __restrict__ out,
                                                    int out_stride, int out_off, int nx, int ny,
                                                    int nz, int relu, int* err) {
-  using S = TcZShape<CIN, COUT>;
-  extern __shared__ __align__(128) unsigned char tcz_dyn[];
+  using S = TcPShape<CIN, COUT>;
+  extern __shared__ __align__(128) unsigned char tcp_dyn[];
   unsigned char* wts = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(tcz_dyn) + 127) & ~static_cast<uintptr_t>(127));
+      (reinterpret_cast<uintptr_t>(tcp_dyn) + 127) & ~static_cast<uintptr_t>(127));
   unsigned char* ring = wts + S::WTS;
   __shared__ __align__(8) uint64_t mma_bar[2];
   __shared__ uint32_t tmem_slot;
@@ -479,6 +482,239 @@ __global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restri
     }
     epilogue(x0, y0, ze - 1, (ze - 1) & 1);
     __syncthreads();  // the next column's first copies reuse slots the last epilogue's MMAs read
+  }
+  // MMAs still in flight after a wait that ran out finish before the tensor memory is freed
+  for (int b = 0; b < 2; ++b)
+    if (outstanding[b]) (void)tc_wait(&mma_bar[b], phase[b]);
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(S::TMEM_COLS)
+                 : "memory");
+}
+
+// ---------------------------------------------------------------------------------------------
+// dz-stacked pipelined form, for the layers with 32 or more input channels whose 27 taps of
+// weights stay resident in shared memory (27 x CIN x COUT x 2 bytes <= 64 KB).  The three dz
+// taps are stacked along N: the weights sit as [t9][chunk][rb * COUT + o][8] with
+// row block rb = 2 - dz, so one group of MMAs per INPUT plane z' (9 taps x CIN/16 slices, N =
+// 3 COUT) adds W(dz=2) In(z') to out(z'-1), W(1) In(z') to out(z') and W(0) In(z') to out(z'+1)
+// at once: a third of the MMAs of one group per output plane over the three input planes, and
+// each input patch is read by one group only.  The accumulators of a column of ZC output planes
+// and of the planes on either side lie side by side in tensor memory (COUT columns each, zeroed
+// when the column starts); the input planes just outside the column add their one relevant
+// third (N = COUT).
+// A block walks columns of ZC output planes along z at one (x, y) tile with a ring of three
+// input patches; per input plane z' of the column (zb-1 .. ze):
+//   wait for plane z' (copied two planes ahead), barrier; issue MMAs(z'), commit;
+//   wait MMAs(z'-1), the last reader of plane z'-1's slot: copy plane z'+2 into it, then the
+//   epilogue of out(z'-2), complete with MMAs(z'-1), while MMAs(z') run.
+// The MMA issue is unrolled over the taps and channel slices with the descriptors advanced by
+// constant offsets.
+template <int CIN, int COUT>
+struct TcZShape {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
+  static constexpr int CH = CIN / 8;
+  static constexpr int N3 = 3 * COUT;                  // the stacked N
+  static constexpr int PLANE = kTcHP * 16;
+  static constexpr int SLOT = CH * PLANE;              // one input plane's patch
+  static constexpr int WTS = 9 * CH * N3 * 16;         // all taps, [t9][chunk][rb COUT + o][8]
+  static constexpr int SMEM = WTS + 3 * SLOT + 128;
+  static constexpr int TMEM_COLS = 256;
+  static constexpr int ZC = TMEM_COLS / COUT - 2;      // output planes per z column
+  static constexpr bool FITS = WTS <= 64 * 1024 && N3 <= 256;
+};
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv3_tcz(const __nv_bfloat16* __restrict__ in,
+                                                   int in_stride, int in_off,
+                                                   const __nv_bfloat16* __restrict__ W,
+                                                   const float* __restrict__ bias,
+                                                   __nv_bfloat16* __restrict__ out,
+                                                   int out_stride, int out_off, int nx, int ny,
+                                                   int nz, int relu, int* err) {
+  using S = TcZShape<CIN, COUT>;
+  extern __shared__ __align__(128) unsigned char tcz_dyn[];
+  unsigned char* wts = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(tcz_dyn) + 127) & ~static_cast<uintptr_t>(127));
+  unsigned char* ring = wts + S::WTS;
+  __shared__ __align__(8) uint64_t mma_bar[2];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc_smem(&tmem_slot)),
+                 "r"(S::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mma_bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mma_bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // all 27 taps of the weights, once per block, the dz taps stacked along N
+  for (int q = tid; q < 9 * S::CH * S::N3; q += 128) {
+    const int orow = q % S::N3, c = (q / S::N3) % S::CH, t9 = q / (S::N3 * S::CH);
+    const int rb = orow / COUT, o = orow % COUT, tap = (2 - rb) * 9 + t9;
+    tc_cp16(wts + ((t9 * S::CH + c) * S::N3 + orow) * 16,
+            W + ((size_t)tap * COUT + o) * CIN + 8 * c, 16);
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t wts_s = tc_smem(wts), ring_s = tc_smem(ring);
+  constexpr uint32_t idesc3 = tc_idesc(S::N3), idesc1 = tc_idesc(COUT);
+  uint32_t phase[2] = {0u, 0u};
+  int outstanding[2] = {0, 0};  // MMAs committed to mma_bar[b] and not yet waited for
+  bool failed = false;
+
+  // copies of input plane zz's patch into ring slot (zz + 3) % 3, zero outside the grid; a
+  // commit group every call (empty past the column), so each wait leaves exactly one pending
+  auto load_plane = [&](int x0, int y0, int zz, bool copy) {
+    if (copy)
+      tc_load_patch<S::CH>(ring + ((zz + 3) % 3) * S::SLOT, in, in_stride, in_off, x0, y0, zz,
+                           nx, ny, nz, tid);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  // bias + ReLU + BF16 store of tile (x0, y0, z) from its accumulator (column col)
+  auto epilogue = [&](int x0, int y0, int z, uint32_t col) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int r = warp * 32 + lane, px = x0 + (r & 7), py = y0 + (r >> 3);
+    __nv_bfloat16* dst =
+        out + ((size_t)px + (size_t)nx * ((size_t)py + (size_t)ny * z)) * out_stride + out_off;
+#pragma unroll
+    for (int cb = 0; cb < COUT; cb += 16) {
+      uint32_t v[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+          "%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(lane_base + col + (uint32_t)cb));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      uint32_t packed[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float v0 = __uint_as_float(v[2 * q]) + (bias ? bias[cb + 2 * q] : 0.f);
+        float v1 = __uint_as_float(v[2 * q + 1]) + (bias ? bias[cb + 2 * q + 1] : 0.f);
+        if (relu) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+        packed[q] = *reinterpret_cast<uint32_t*>(&h);
+      }
+      if (px < nx && py < ny) {
+        uint4* d4 = reinterpret_cast<uint4*>(dst + cb);
+        d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  };
+  // block-uniform bounded wait for the MMAs committed to mma_bar[b]
+  auto wait_mma = [&](int b) -> bool {
+    const bool late = __syncthreads_or(!tc_wait(&mma_bar[b], phase[b]));
+    if (late) {
+      if (tid == 0) atomicExch(err, 2);
+      return false;
+    }
+    phase[b] ^= 1u;
+    outstanding[b] = 0;
+    return true;
+  };
+
+  const int xt = tc_tiles_x(nx), yt = tc_tiles_y(ny);
+  const int zcols = (nz + S::ZC - 1) / S::ZC;
+  const long items = (long)xt * yt * zcols;
+  for (long item = blockIdx.x; item < items && !failed; item += gridDim.x) {
+    const int x0 = (int)(item % xt) * kTcTX;
+    const long rest = item / xt;
+    const int y0 = (int)(rest % yt) * kTcTY;
+    const int zb = (int)(rest / yt) * S::ZC, ze = min(nz, zb + S::ZC);
+    // accumulator of output plane z (zb-1 .. ze) at column (z - zb + 1) COUT
+    auto col = [&](int z) { return (uint32_t)((z - zb + 1) * COUT); };
+    // zero the column's accumulators (the previous column's epilogues have read theirs)
+    {
+      const uint32_t zero[16] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+      for (int c0 = 0; c0 < (ze - zb + 2) * COUT; c0 += 16)
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+            "%13,%14,%15,%16};" ::"r"(lane_base + (uint32_t)c0),
+            "r"(zero[0]), "r"(zero[1]), "r"(zero[2]), "r"(zero[3]), "r"(zero[4]), "r"(zero[5]),
+            "r"(zero[6]), "r"(zero[7]), "r"(zero[8]), "r"(zero[9]), "r"(zero[10]),
+            "r"(zero[11]), "r"(zero[12]), "r"(zero[13]), "r"(zero[14]), "r"(zero[15])
+            : "memory");
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    load_plane(x0, y0, zb - 1, true);
+    load_plane(x0, y0, zb, true);
+    for (int zp = zb - 1; zp <= ze; ++zp) {
+      const int b = (zp + 1) & 1;
+      // plane zp (and, the first time, the weights) has landed; plane zp+1 may be in flight
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+        if (zp >= 0 && zp < nz) {  // zero padding outside the grid adds nothing
+          // the stacked row blocks this plane adds: rb = 2 - dz adds to out(zp - 1 + rb)
+          const int rb0 = zp < zb ? 2 : 0, rbn = (zp < zb || zp >= ze) ? 1 : 3;
+          const uint64_t a0 =
+              tc_desc(ring_s + (uint32_t)(((zp + 3) % 3) * S::SLOT), S::PLANE, kTcHX * 16);
+          const uint64_t b0 = tc_desc(wts_s + (uint32_t)(rb0 * COUT * 16), S::N3 * 16, 128);
+          const uint32_t d_tmem = tmem + col(zp - 1 + rb0);
+          const uint32_t idesc = rbn == 3 ? idesc3 : idesc1;
+#pragma unroll
+          for (int t9 = 0; t9 < 9; ++t9) {
+            const int dy = t9 / 3, dx = t9 % 3;
+#pragma unroll
+            for (int kc = 0; kc < CIN / 16; ++kc) {
+              const uint64_t a = tc_desc_at(a0, tc_tap_offset<S::CH>(dx, dy, kc));
+              const uint64_t bd = tc_desc_at(b0, (t9 * S::CH + 2 * kc) * S::N3 * 16);
+              asm volatile(
+                  "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                  " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+                  "l"(a), "l"(bd), "r"(idesc), "r"(1u)
+                  : "memory");
+            }
+          }
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                tc_smem(&mma_bar[b]))
+            : "memory");
+      }
+      outstanding[b] = 1;
+      if (zp > zb - 1) {  // MMAs(zp-1) were the last readers of plane zp-1's slot
+        if (!wait_mma(b ^ 1)) {
+          failed = true;
+          break;
+        }
+        load_plane(x0, y0, zp + 2, zp + 2 <= ze);
+        if (zp - 2 >= zb) epilogue(x0, y0, zp - 2, col(zp - 2));
+      } else {
+        load_plane(x0, y0, zp + 2, zp + 2 <= ze);
+      }
+    }
+    if (failed) break;
+    if (!wait_mma((ze + 1) & 1)) {  // MMAs(ze)
+      failed = true;
+      break;
+    }
+    epilogue(x0, y0, ze - 1, col(ze - 1));
+    // the next column zeroes accumulators and overwrites slots this column's last reads used
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
   }
   // MMAs still in flight after a wait that ran out finish before the tensor memory is freed
   for (int b = 0; b < 2; ++b)
