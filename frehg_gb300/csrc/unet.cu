@@ -205,22 +205,37 @@ __global__ void k_relu_bwd(bf16* __restrict__ g, int g_stride, int g_off,
 }
 
 // 2x2x2 average pooling: out (coarse, stride C) from a channel slice of in (fine)
+// 2x2x2 mean pooling of a channel slice: one thread per coarse cell and group of 8 channels
+// (16-byte loads of the eight children, one 16-byte store); c, in_stride and in_off are
+// multiples of 8, and the network's cell counts stay below 2^32
 __global__ void k_pool(const bf16* __restrict__ in, int in_stride, int in_off, bf16* __restrict__ out,
                        int c, int nx, int ny, int nz) {
-  const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
-  const size_t nc = (size_t)cx * cy * cz;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nc * c;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const size_t q = e / c;
-    const int ch = (int)(e % c);
-    const int x = (int)(q % cx), y = (int)((q / cx) % cy), z = (int)(q / ((size_t)cx * cy));
-    float s = 0.f;
+  const uint32_t cx = nx / 2, cy = ny / 2, cz = nz / 2;
+  const uint32_t g = (uint32_t)c / 8;
+  const uint64_t tot = (uint64_t)cx * cy * cz * g;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < tot;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = (uint32_t)(e / g), cg = (uint32_t)(e - (uint64_t)q * g);
+    const uint32_t x = q % cx, yz = q / cx, y = yz % cy, z = yz / cy;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
     for (int k = 0; k < 8; ++k) {
-      const size_t p = (size_t)(2 * x + (k & 1)) + (size_t)nx * ((size_t)(2 * y + ((k >> 1) & 1)) +
-                                                                   (size_t)ny * (2 * z + (k >> 2)));
-      s += __bfloat162float(in[p * in_stride + in_off + ch]);
+      const uint32_t p = (2 * x + (k & 1)) + (uint32_t)nx * ((2 * y + ((k >> 1) & 1)) +
+                                                             (uint32_t)ny * (2 * z + (k >> 2)));
+      const uint4 v = *reinterpret_cast<const uint4*>(in + (size_t)p * in_stride + in_off + 8 * cg);
+      const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float2 f = __bfloat1622float2(h[u]);
+        s[2 * u] += f.x;
+        s[2 * u + 1] += f.y;
+      }
     }
-    out[q * c + ch] = __float2bfloat16(0.125f * s);
+    uint4 o;
+    uint32_t* ow = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ow[u] = pack2(0.125f * s[2 * u], 0.125f * s[2 * u + 1]);
+    *reinterpret_cast<uint4*>(out + (size_t)q * c + 8 * cg) = o;
   }
 }
 
@@ -287,10 +302,10 @@ __global__ void k_pack_input(const float* __restrict__ r, const float* __restric
   const float rs = *rscale;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n;
        p += (size_t)gridDim.x * blockDim.x) {
-    uint32_t* o = reinterpret_cast<uint32_t*>(x + p * 16);
-    o[0] = pack2(r[p] * rs, (lnk[p] - kmean) * kscale);
-    o[1] = pack2(cap[p] * cscale, 0.f);
-    o[2] = o[3] = o[4] = o[5] = o[6] = o[7] = 0u;
+    uint4* o = reinterpret_cast<uint4*>(x + p * 16);  // two 16-byte stores per cell
+    o[0] = make_uint4(pack2(r[p] * rs, (lnk[p] - kmean) * kscale), pack2(cap[p] * cscale, 0.f),
+                      0u, 0u);
+    o[1] = make_uint4(0u, 0u, 0u, 0u);
   }
 }
 
@@ -337,8 +352,18 @@ __global__ void k_out(const bf16* __restrict__ d1, const float* __restrict__ wo,
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n;
        p += (size_t)gridDim.x * blockDim.x) {
     float v = wo[16];
+    const uint4* dv = reinterpret_cast<const uint4*>(d1 + p * 16);  // two 16-byte loads
 #pragma unroll
-    for (int c = 0; c < 16; ++c) v = fmaf(wo[c], __bfloat162float(d1[p * 16 + c]), v);
+    for (int half = 0; half < 2; ++half) {
+      const uint4 w = dv[half];
+      const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&w);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float2 f = __bfloat1622float2(h[u]);
+        v = fmaf(wo[8 * half + 2 * u], f.x, v);
+        v = fmaf(wo[8 * half + 2 * u + 1], f.y, v);
+      }
+    }
     y[p] = v * s;
   }
 }
@@ -665,10 +690,10 @@ int forward(frehg_unet* net, const float* r, const float* lnk, const float* cap,
                                                net->cscale, net->x0, n1);
   conv<16, 16>(net->x0, 16, 0, W + net->wboff[0], M + net->boff[0], net->a1, 16, 0, nx, ny, nz, true, st);
   conv<16, 16>(net->a1, 16, 0, W + net->wboff[1], M + net->boff[1], net->cat1, 48, 32, nx, ny, nz, true, st);
-  k_pool<<<blocks_for(n2 * 16), 256, 0, st>>>(net->cat1, 48, 32, net->p1, 16, nx, ny, nz);
+  k_pool<<<blocks_for(n2 * 2), 256, 0, st>>>(net->cat1, 48, 32, net->p1, 16, nx, ny, nz);
   conv<16, 32>(net->p1, 16, 0, W + net->wboff[2], M + net->boff[2], net->a2, 32, 0, x2, y2, z2, true, st);
   conv<32, 32>(net->a2, 32, 0, W + net->wboff[3], M + net->boff[3], net->cat2, 96, 64, x2, y2, z2, true, st);
-  k_pool<<<blocks_for(n3 * 32), 256, 0, st>>>(net->cat2, 96, 64, net->p2, 32, x2, y2, z2);
+  k_pool<<<blocks_for(n3 * 4), 256, 0, st>>>(net->cat2, 96, 64, net->p2, 32, x2, y2, z2);
   conv<32, 64>(net->p2, 32, 0, W + net->wboff[4], M + net->boff[4], net->a3, 64, 0, x3, y3, z3, true, st);
   conv<64, 64>(net->a3, 64, 0, W + net->wboff[5], M + net->boff[5], net->e3, 64, 0, x3, y3, z3, true, st);
   k_up<<<blocks_for(n2 * 64), 256, 0, st>>>(net->e3, net->cat2, 96, 0, 64, x2, y2, z2);
