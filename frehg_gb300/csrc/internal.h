@@ -266,4 +266,11 @@ StencilLaunch stencil_launch(int n0, int n1, int n2);
 
 int reduction_blocks(size_t n, int threads, int per_thread);
 
+// Small device-to-host read-backs (the solvers' control state, a few hundred bytes) ordered on
+// st: a one-warp kernel writes them into mapped page-locked host memory (host_mapped, from
+// alloc_mapped), so that they do not queue on the copy engines behind a bulk result copy in
+// flight.  The caller synchronises st before reading.  bytes: a multiple of 4.
+int fetch_small(void* host_mapped, const void* dev, size_t bytes, cudaStream_t st);
+int alloc_mapped(void** host, size_t bytes);
+
 }  // namespace fg

@@ -62,6 +62,27 @@ StencilLaunch stencil_launch(int n0, int n1, int n2) {
   return L;
 }
 
+namespace {
+__global__ void k_fetch_words(const unsigned* __restrict__ src, unsigned* __restrict__ dst,
+                              int words) {
+  for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+}
+}  // namespace
+
+int alloc_mapped(void** host, size_t bytes) {
+  FG_CUDA(cudaHostAlloc(host, bytes, cudaHostAllocMapped));
+  return FREHG_OK;
+}
+
+int fetch_small(void* host_mapped, const void* dev, size_t bytes, cudaStream_t st) {
+  void* d = nullptr;
+  FG_CUDA(cudaHostGetDevicePointer(&d, host_mapped, 0));
+  k_fetch_words<<<1, 32, 0, st>>>(static_cast<const unsigned*>(dev), static_cast<unsigned*>(d),
+                                  (int)(bytes / 4));
+  FG_CUDA(cudaGetLastError());
+  return FREHG_OK;
+}
+
 int reduction_blocks(size_t n, int threads, int per_thread) {
   size_t b = (n + (size_t)threads * per_thread - 1) / ((size_t)threads * per_thread);
   if (b < 1) b = 1;
@@ -397,7 +418,7 @@ int KrylovSolver::ensure(size_t n) {
   if (!dst) {
     FG_CUDA(cudaMalloc(&dst, sizeof(CgDevState)));
     FG_CUDA(cudaMemset(dst, 0, sizeof(CgDevState)));
-    FG_CUDA(cudaMallocHost(&hst, sizeof(CgDevState)));
+    FG_TRY(alloc_mapped(reinterpret_cast<void**>(&hst), sizeof(CgDevState)));
   }
   cap = n;
   return FREHG_OK;
@@ -432,7 +453,7 @@ int KrylovSolver::run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int
   for (int q = 0; q < max_launch; ++q) {
     FG_CUDA(cudaGraphLaunch(g, st));
     if (prof) prof->launches += 3 * chunk;
-    FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+    FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (hst->status != 0) return FREHG_OK;
   }
@@ -493,7 +514,7 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
   if (prof && prof->on) {
     // profiled path: the same kernels launched one by one between CUDA events
-    FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+    FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
     FG_CUDA(cudaStreamSynchronize(st));
     for (int q = 0; q < cfg.max_it / chunk + 2 && hst->status == 0; ++q) {
       for (int it = 0; it < chunk; ++it) {
@@ -505,7 +526,7 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
                   k_cg_update<<<nb, 256, 0, st>>>(x, r, p, w, A.s, n, dst, partials));
       }
       FG_CUDA(cudaGetLastError());
-      FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+      FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
       FG_CUDA(cudaStreamSynchronize(st));
       FG_TRY(prof->flush());
     }
@@ -544,7 +565,7 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
     g_n = n;
   }
   // iteration 0 may already have converged
-  FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+  FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
   FG_CUDA(cudaStreamSynchronize(st));
   if (hst->status == 0) FG_TRY(run_chunks(g64, st, cfg.max_it, chunk));
   return finish64(A, x_out, st, res, nb);

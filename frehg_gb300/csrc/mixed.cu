@@ -597,7 +597,7 @@ int KrylovSolver::ensure32(size_t n) {
   if (!dst32) {
     FG_CUDA(cudaMalloc(&dst32, sizeof(CgDevState)));
     FG_CUDA(cudaMemset(dst32, 0, sizeof(CgDevState)));
-    FG_CUDA(cudaMallocHost(&hst32, sizeof(CgDevState)));
+    FG_TRY(alloc_mapped(reinterpret_cast<void**>(&hst32), sizeof(CgDevState)));
   }
   cap32 = n;
   return FREHG_OK;
@@ -1037,7 +1037,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
                 k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
                                                cfg.inner_rtol));
     FG_CUDA(cudaGetLastError());
-    FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+    FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (prof && prof->on) FG_TRY(prof->flush());
     if (sweeps == 0 && first_done_here && hst->rhs_rescale) {
@@ -1051,7 +1051,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
                 k_ir_scale<<<nb, 256, 0, st>>>(rres, rf, n, dst, dst32, partials,
                                                cfg.inner_rtol));
       FG_CUDA(cudaGetLastError());
-      FG_CUDA(cudaMemcpyAsync(hst, dst, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+      FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
       FG_CUDA(cudaStreamSynchronize(st));
       if (prof && prof->on) FG_TRY(prof->flush());
     }
@@ -1060,7 +1060,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
     if (hst->status != 0) break;
     if (sweeps >= max_sweeps) break;
     // inner FP32 solve: flexible CG with the learned preconditioner, or Jacobi CG
-    FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+    FG_TRY(fetch_small(hst32, dst32, sizeof(CgDevState), st));
     FG_CUDA(cudaStreamSynchronize(st));
     // a sweep that starts with the network's budget (twice the reference solve's inner
     // iterations) spent runs without it, as do the later ones
@@ -1089,7 +1089,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
                   k32_update<<<nb, 256, 0, st>>>(xf, rf, pf, wf, n, dst32, partials));
         FG_CUDA(cudaGetLastError());
         if ((it + 1) % check == 0) {
-          FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+          FG_TRY(fetch_small(hst32, dst32, sizeof(CgDevState), st));
           FG_CUDA(cudaStreamSynchronize(st));
           if (prof && prof->on) FG_TRY(prof->flush());
           if (net.max_inner > 0 && inner_total + hst32->its > net.max_inner) {
@@ -1098,7 +1098,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
           }
         }
       }
-      FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+      FG_TRY(fetch_small(hst32, dst32, sizeof(CgDevState), st));
       FG_CUDA(cudaStreamSynchronize(st));
       if (prof && prof->on) FG_TRY(prof->flush());
     }
@@ -1137,7 +1137,7 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
         FG_CUDA(cudaGraphLaunch(q == 0 ? g32s : g32, st));
         if (prof) prof->launches += 3 * iters;
       }
-      FG_CUDA(cudaMemcpyAsync(hst32, dst32, sizeof(CgDevState), cudaMemcpyDeviceToHost, st));
+      FG_TRY(fetch_small(hst32, dst32, sizeof(CgDevState), st));
       FG_CUDA(cudaStreamSynchronize(st));
       if (prof && prof->on) {
         FG_TRY(prof->flush());

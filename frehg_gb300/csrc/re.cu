@@ -603,8 +603,7 @@ static int pca_step(frehg_re* re) {
     FG_CUDA(cudaGetLastError());
     ++sweeps;
     int changed = 0;
-    FG_CUDA(cudaMemcpyAsync(&re->sc_host->changed, &re->sc->changed, sizeof(int),
-                            cudaMemcpyDeviceToHost, st));
+    FG_TRY(fetch_small(&re->sc_host->changed, &re->sc->changed, sizeof(int), st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (prof->on) FG_TRY(prof->flush());
     changed = re->sc_host->changed;
@@ -707,8 +706,8 @@ static int launch_staged_assembly(frehg_re* re, const ReArgs& a, const StencilLa
 }
 
 static int read_scalars(const frehg_re* re) {
+  FG_TRY(fetch_small(re->sc_host, re->sc, sizeof(ReScalars), re->stream));
   FG_CUDA(cudaStreamSynchronize(re->stream));
-  FG_CUDA(cudaMemcpy(re->sc_host, re->sc, sizeof(ReScalars), cudaMemcpyDeviceToHost));
   return FREHG_OK;
 }
 
@@ -814,10 +813,8 @@ static int picard_step(frehg_re* re) {
                   k_pic_update<true><<<nb, 256, 0, st>>>(a, re->ksp.x,
                                                          re->ksp.scale_vector(re->A)));
       FG_CUDA(cudaGetLastError());
-      FG_CUDA(cudaMemcpyAsync(&re->sc_host->dq_max, &re->sc->dq_max, sizeof(double),
-                              cudaMemcpyDeviceToHost, st));
-      FG_CUDA(cudaMemcpyAsync(&re->sc_host->stage_err, &re->sc->stage_err, sizeof(int),
-                              cudaMemcpyDeviceToHost, st));
+      FG_TRY(fetch_small(&re->sc_host->dq_max, &re->sc->dq_max, sizeof(double), st));
+      FG_TRY(fetch_small(&re->sc_host->stage_err, &re->sc->stage_err, sizeof(int), st));
       FG_CUDA(cudaStreamSynchronize(st));
       if (re->sc_host->stage_err) {
         set_error("staged Picard assembly: a bounded wait on its copy pipeline ran out (%d)",
@@ -956,7 +953,8 @@ int frehg_re_create(int nx, int ny, int nz, const frehg_re_params* p, frehg_re**
   ALLOC(re->sc, sizeof(ReScalars));
   ALLOC(re->partials, 4 * kMaxRedBlocks * sizeof(double));
 #undef ALLOC
-  if (cudaMallocHost(&re->sc_host, sizeof(ReScalars)) != cudaSuccess) return fail(FREHG_ERR_CUDA);
+  if (alloc_mapped(reinterpret_cast<void**>(&re->sc_host), sizeof(ReScalars)) != FREHG_OK)
+    return fail(FREHG_ERR_CUDA);
   if (re->A.alloc(nx, ny, nz) != FREHG_OK) return fail(FREHG_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&re->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(FREHG_ERR_CUDA);
