@@ -18,6 +18,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "frehg_gb300.h"
@@ -86,13 +87,55 @@ struct Grid {
   }
 };
 
-// Decomp3D of one rank (src/linear/DomainDecomposition.hpp): the owned box.
+// Decomp3D of one rank (src/linear/DomainDecomposition.hpp:94-120, .cpp:109-185): the owned box
+// of the one process whose global system the library solves.  Rows are numbered with k
+// fastest, row = (j nx + i) nz + k; the STAR stencil's columns come in the reference's order
+// (centre, W, E, S, N, Up, Down); packOwned / unpackOwned move between a halo-padded field
+// ((nx+2)(ny+2)(nz+2), i fastest, Grid::getIndex) and the owned vector.
 struct Decomp3D {
   int nx = 1, ny = 1, nz = 1;
   Decomp3D() = default;
   Decomp3D(int nx_, int ny_, int nz_) : nx(nx_), ny(ny_), nz(nz_) {}
   long nOwned() const { return (long)nx * ny * nz; }
+  long globalRowCount() const { return nOwned(); }
+  std::pair<long, long> ownershipRange() const { return {0L, nOwned()}; }
   long globalRow(int i, int j, int k) const { return ((long)j * nx + i) * nz + k; }
+  // centre and in-domain W, E, S, N, Up (k-1, toward the surface), Down (k+1); up to 7
+  void stencilColumns(int i, int j, int k, long* cols, int& ncols) const {
+    ncols = 0;
+    cols[ncols++] = globalRow(i, j, k);
+    if (i - 1 >= 0) cols[ncols++] = globalRow(i - 1, j, k);
+    if (i + 1 < nx) cols[ncols++] = globalRow(i + 1, j, k);
+    if (j - 1 >= 0) cols[ncols++] = globalRow(i, j - 1, k);
+    if (j + 1 < ny) cols[ncols++] = globalRow(i, j + 1, k);
+    if (k - 1 >= 0) cols[ncols++] = globalRow(i, j, k - 1);
+    if (k + 1 < nz) cols[ncols++] = globalRow(i, j, k + 1);
+  }
+  void ownedRowStencil(long local, long& global_row, long* cols, int& ncols) const {
+    const int k = (int)(local % nz);
+    const long horiz = local / nz;
+    const int i = (int)(horiz % nx), j = (int)(horiz / nx);
+    global_row = globalRow(i, j, k);
+    stencilColumns(i, j, k, cols, ncols);
+  }
+  long localHaloFieldSize() const { return (long)(nx + 2) * (ny + 2) * (nz + 2); }
+  long haloIndex(int i, int j, int k) const {
+    return (long)(i + 1) + (long)(j + 1) * (nx + 2) + (long)(k + 1) * (nx + 2) * (ny + 2);
+  }
+  void packOwned(const std::vector<double>& field_halo, std::vector<double>& owned) const {
+    owned.resize((size_t)nOwned());
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        for (int k = 0; k < nz; ++k)
+          owned[(size_t)globalRow(i, j, k)] = field_halo[(size_t)haloIndex(i, j, k)];
+  }
+  void unpackOwned(const std::vector<double>& owned, std::vector<double>& field_halo) const {
+    field_halo.resize((size_t)localHaloFieldSize(), 0.0);
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        for (int k = 0; k < nz; ++k)
+          field_halo[(size_t)haloIndex(i, j, k)] = owned[(size_t)globalRow(i, j, k)];
+  }
 };
 
 // ---- linear-solver seam ------------------------------------------------------------------

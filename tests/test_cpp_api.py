@@ -29,3 +29,16 @@ def test_cpp_program_runs(gpu_lib):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "ALL OK" in r.stdout
+
+
+def test_decomp3d_on_the_cpu():
+    """the Decomp3D of the C++ mirror (header only): numbering, STAR stencil, pack / unpack"""
+    src = os.path.join(ROOT, "tests", "cpp", "test_decomp3d.cpp")
+    out_dir = os.path.join(ROOT, "tests", "cpp", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "test_decomp3d")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", INC, src,
+                    "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL OK" in r.stdout
