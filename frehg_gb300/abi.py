@@ -116,6 +116,7 @@ class ReParams(C.Structure):
         self.scheme, self.face_mean, self.picard_max_it, self.picard_tol = 0, 0, 50, 1.0e-6
         self.rain_rate, self.rain_until, self.picard_dt_adapt = 0.0, 0.0, 0
         self.picard_dh_max = 0.0
+        self.picard_fp64 = -1  # float-float with the mixed-precision solve, else FP64
         for k, v in kw.items():
             if k == "bc_type":
                 self.bc_type[:] = list(v)
@@ -247,6 +248,7 @@ SIGNATURES = {
     "frehg_cg_iteration_count": (C.c_int, [_VP, _PI]),
     "frehg_cg_residual_norm": (C.c_int, [_VP, _PD]),
     "frehg_cg_converged_reason": (C.c_int, [_VP, _PI]),
+    "frehg_cg_set_fused_iteration": (C.c_int, [_VP, C.c_int]),
     "frehg_cg_solve_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _VP,
                                          _VP, C.POINTER(SolverConfig), _VP, _PI, _PD]),
     "frehg_unet_create": (C.c_int, [C.c_uint64, C.POINTER(_VP)]),
@@ -264,6 +266,7 @@ SIGNATURES = {
     "frehg_re_attach_unet": (C.c_int, [_VP, _VP]),
     "frehg_re_set_learned_policy": (C.c_int, [_VP, C.c_int, C.c_double]),
     "frehg_re_set_assembly_staging": (C.c_int, [_VP, C.c_int]),
+    "frehg_re_set_fused_iteration": (C.c_int, [_VP, C.c_int]),
     "frehg_re_training_pairs": (C.c_int, [_VP, C.c_int, _PI, C.c_int, _VP, _VP, _VP, _VP]),
     "frehg_build_arch": (C.c_int, []),
     "frehg_re_checkpoint": (C.c_int, [_VP, _VP, _VP, _VP]),

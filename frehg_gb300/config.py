@@ -318,8 +318,10 @@ def re_params(cfg, scheme):
     p.picard_dt_adapt = int(bool(get(cfg, "groundwater.picard_dt_adapt", False)))
     p.picard_dh_max = float(get(cfg, "groundwater.picard_dh_max", 0.0))
     # constitutive relations, assembly and final update of the Picard scheme in native FP64
-    # (true) or in float-float arithmetic on the FP32 pipe (false, the default)
-    p.picard_fp64 = int(bool(get(cfg, "groundwater.picard_fp64", False)))
+    # (true) or in float-float arithmetic on the FP32 pipe (false); unset: float-float with
+    # the mixed-precision solve, FP64 with the FP64 solve (-1)
+    pf = get(cfg, "groundwater.picard_fp64", None)
+    p.picard_fp64 = -1 if pf is None else int(bool(pf))
     p.rain_rate = float(get(cfg, "groundwater.rain.rate", 0.0))
     p.rain_until = float(get(cfg, "groundwater.rain.until", 0.0))
     return p

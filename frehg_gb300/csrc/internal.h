@@ -85,6 +85,10 @@ class Profiler {
 
 // Upper bound of the blocks any reduction kernel launches (partials buffers are sized to it).
 constexpr int kMaxRedBlocks = 32768;
+// largest system the FP64 Jacobi-PCG runs as one launch per iteration by default: on GB300 the
+// one-launch form is 5-8 % faster up to about 32k unknowns and 4-25 % slower from 262k on
+// (its two grid barriers and half occupancy against three kernels' launch gaps)
+constexpr size_t kFusedAutoCells = 65536;
 constexpr int kNumSMs = 152;
 
 // ------------------------------------------------------------------------------------------
@@ -136,6 +140,11 @@ struct CgDevState {
   double rscale;              // the inner right-hand side is r~ / rscale (mixed precision)
   int ir_its;
   int rhs_rescale;  // k_prep_ff: its power-of-two scaled right-hand side needs k_ir_scale instead
+  // grid barrier of the one-launch CG iteration (k_cg_iter): arrival count, generation, and
+  // the flag a block sets when its bounded wait ran out
+  unsigned int bar_count, bar_gen;
+  int bar_timeout;
+  int pad_;
 };
 
 // KSPConvergedReason values
@@ -147,6 +156,8 @@ enum {
   kDivergedIndefinitePc = -8,
   kDivergedNanOrInf = -9,
   kDivergedIndefiniteMat = -10,
+  // not a PETSc reason: a grid barrier of the one-launch CG iteration did not complete in time
+  kGridBarrierTimeout = -90,
 };
 
 struct CgResult {
@@ -171,8 +182,8 @@ struct NetPrecond {
   int max_inner = 0;  // fall back to Jacobi CG beyond this many inner iterations (0 = never)
 };
 
-// Jacobi-preconditioned CG in FP64 (3 kernels per iteration, CUDA-graph chunks), with an
-// optional FP32 inner solve under FP64 iterative refinement.
+// Jacobi-preconditioned CG in FP64 (one cooperative launch or three kernels per iteration,
+// CUDA-graph chunks), with an optional FP32 inner solve under FP64 iterative refinement.
 class KrylovSolver {
  public:
   ~KrylovSolver();
@@ -205,6 +216,13 @@ class KrylovSolver {
   cudaGraphExec_t g32s = nullptr;  // first, short chunk of the inner solve
   const void* g64_key = nullptr;
   const void* g64_key2 = nullptr;
+  // the FP64 Jacobi-PCG iteration as one cooperative launch (k_cg_iter) rather than three
+  // kernels, where the device has cooperative launches: 1 always, 0 never, -1 (default) for
+  // systems of at most kFusedAutoCells unknowns (larger ones run faster as three kernels);
+  // g64_form: the form g64 holds; coop_failed: a cooperative capture failed, use three kernels
+  int fused64 = -1;
+  int g64_form = -1;
+  bool coop_failed = false;
   Profiler* prof = nullptr;  // owner's profiler (launch counts, optional event timing)
   NetPrecond net;            // learned preconditioner (FCG inner solves when set)
   // the mixed path's scaled couplings in float-float (2^-48) instead of FP64 products: for
@@ -251,7 +269,8 @@ class KrylovSolver {
   // CG + PCSOR on the unscaled operator; the solution is left in x and copied to x_out
   int solve_sor(Stencil64& A, double* x_out, const frehg_solver_config& cfg, cudaStream_t st,
                 CgResult* res);
-  int run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk);
+  int run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk,
+                 int launches_per_it = 3);
   int finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResult* res, int nb);
 };
 

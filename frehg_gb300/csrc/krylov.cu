@@ -11,17 +11,21 @@
 //    is Jacobi-PCG on A (x~ = D^1/2 x, r~ = D^-1/2 r, beta = r.z = r~.r~, p'Ap = p~'A~p~,
 //    ||B r|| = ||s r~|| with s = D^-1/2), so the diagonal is never stored or multiplied and
 //    no divisions remain in the loop.
-//  * Three kernels per iteration (p-update, stencil SpMV + p.w, update + two norms); every
-//    reduction ends in the last-arriving block, which also runs the scalar part of the
-//    algorithm (alpha, beta, stopping test) on the device.  Kernels of a converged solve
-//    return at once, so iterations are captured in a CUDA graph of `chunk` iterations and
-//    the host only reads the status between chunks.  Reductions are deterministic (fixed
-//    block partition, fixed summation tree).
+//  * One cooperative launch per iteration (k_cg_iter: p-update, stencil SpMV + p.w, update +
+//    two norms, separated by two bounded grid barriers), or, where the device has no
+//    cooperative launch, the same three phases as three kernels; the last reduction ends in
+//    the last-arriving block, which also runs the scalar part of the algorithm (beta,
+//    stopping test) on the device.  Launches of a converged solve return at once, so
+//    iterations are captured in a CUDA graph of `chunk` iterations and the host only reads
+//    the status between chunks.  Reductions are deterministic (fixed block partition, fixed
+//    summation tree).
 //  * FP64 is 1/64 of the FP32 rate on GB300, so the kernels are arranged to keep the FP64
 //    instruction count per cell low (13 FMA-class ops per iteration) as well as the bytes.
 #include "internal.h"
 #include "reduce.cuh"
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -39,28 +43,34 @@ __device__ __forceinline__ int converged_test(CgDevState* s, double rnorm) {
 // ------------------------------------------------------------------------------------------
 // geometry helpers
 
-StencilLaunch stencil_launch(int n0, int n1, int n2) {
+// target: the blocks aimed at; total_cap: the most blocks in all
+static StencilLaunch stencil_launch_for(int n0, int n1, int n2, long target, long total_cap) {
   StencilLaunch L;
   L.block = dim3(32, 8, 1);
   const int t0 = (n0 + 31) / 32, t1 = (n1 + 7) / 8;
   const long tiles = (long)t0 * t1;
-  // about two waves of 8 resident (32 x 8)-thread blocks per SM; the launch shape, and with
-  // it the summation tree of the reductions, depends on the grid sizes only
-  const long target = (long)kNumSMs * 8 * 2;
   long z = target / (tiles > 0 ? tiles : 1);
   if (z < 1) z = 1;
   if (z > n2) z = n2;
   int planes = (int)((n2 + z - 1) / z);
   z = (n2 + planes - 1) / planes;
-  // blocks stride over tiles when there are more tiles than reduction partial slots
+  // blocks stride over tiles when there are more tiles than the cap allows
   long gx = tiles;
-  const long cap = kMaxRedBlocks / z;
+  const long cap = total_cap / z;
   if (gx > cap) gx = cap;
+  if (gx < 1) gx = 1;
   L.planes = planes;
   L.tiles = (int)tiles;
   L.grid = dim3((unsigned)gx, (unsigned)z, 1);
   return L;
 }
+
+StencilLaunch stencil_launch(int n0, int n1, int n2) {
+  // about two waves of 8 resident (32 x 8)-thread blocks per SM; the launch shape, and with
+  // it the summation tree of the reductions, depends on the grid sizes only
+  return stencil_launch_for(n0, n1, n2, (long)kNumSMs * 8 * 2, kMaxRedBlocks);
+}
+
 
 namespace {
 __global__ void k_fetch_words(const unsigned* __restrict__ src, unsigned* __restrict__ dst,
@@ -251,6 +261,32 @@ __global__ void __launch_bounds__(256) k_cg_spmv(const double* __restrict__ a0,
   }
 }
 
+// The scalar end of an iteration (last block): ||B r|| = sqrt(tot[1]) and the stopping test,
+// beta = r~.r~ = tot[0] and the next direction's coefficient.
+__device__ __forceinline__ void cg_update_tail(CgDevState* st, const double (&tot)[2]) {
+  const double dp = sqrt(tot[1]);
+  st->dp = dp;
+  const int reason = converged_test(st, dp);
+  if (reason) {
+    st->status = reason;
+    return;
+  }
+  st->betaold = st->beta;
+  st->beta = tot[0];
+  st->iter += 1;
+  if (st->iter >= st->max_it) {
+    st->status = kDivergedIts;
+    return;
+  }
+  st->its = st->iter + 1;
+  if (st->beta == 0.0) {
+    st->status = kConvergedAtol;
+    return;
+  }
+  st->bcoef = st->beta / st->betaold;
+  if (st->bcoef < 0.0) st->status = kDivergedIndefinitePc;
+}
+
 // x~ += a p, r~ -= a w, then ||B r|| and beta = r~.r~; the last block runs the stopping test
 // and prepares the next iteration's beta ratio.
 __global__ void k_cg_update(double* __restrict__ x, double* __restrict__ r,
@@ -293,29 +329,134 @@ __global__ void k_cg_update(double* __restrict__ x, double* __restrict__ r,
   }
   double tot[2];
   if (!grid_sum<2>(v, partials, &st->arrive[2], tot)) return;
-  if (flat_tid() == 0) {
-    const double dp = sqrt(tot[1]);
-    st->dp = dp;
-    const int reason = converged_test(st, dp);
-    if (reason) {
-      st->status = reason;
-      return;
+  if (flat_tid() == 0) cg_update_tail(st, tot);
+}
+
+// One Jacobi-PCG iteration (KSPSolve_CG's loop body) in one cooperative launch, all blocks
+// resident: the direction p = r~ + bcoef p (p = r~ in iteration 0), a grid barrier, w = A~ p
+// with the block partials of p.w, a grid barrier after which every block sums the same
+// partials in the same order and forms alpha itself, then x~ += alpha p, r~ -= alpha w and the
+// two norms, reduced by the last block to arrive, which runs the stopping test (cg_update_tail).
+// The arithmetic per cell is that of k_cg_p, k_cg_spmv and k_cg_update.  Work units (a
+// 32 x 8-column tile over a chunk of `planes` planes) are dealt round-robin to the blocks, the
+// same units to the same block in all three phases, so the only values a block reads that
+// another block wrote in this launch are the neighbours' directions of the stencil product;
+// every direction read goes through L2 (ld.global.cg), since L1 is not coherent within a
+// launch.  The iteration's scalars are read once at the start, before the first barrier, so
+// that block 0 may update them after the second.
+__global__ void __launch_bounds__(256) k_cg_iter(const double* __restrict__ a0,
+                                                 const double* __restrict__ a1,
+                                                 const double* __restrict__ a2,
+                                                 const double* __restrict__ s,
+                                                 double* __restrict__ x, double* __restrict__ r,
+                                                 double* __restrict__ p, double* __restrict__ w,
+                                                 int n0, int n1, int n2, int planes, int tiles,
+                                                 CgDevState* st, double* partials) {
+  if (st->status) return;
+  const double bc = st->bcoef, beta = st->beta, dpi_prev = st->dpi;
+  const int iter = st->iter;
+  const int t0 = (n0 + 31) / 32;
+  const size_t s01 = (size_t)n0 * n1;
+  const int units = tiles * ((n2 + planes - 1) / planes);
+  const int nb = flat_nblocks(), bid = flat_bid();
+  // 1. direction
+  for (int u = bid; u < units; u += nb) {
+    const int tile = u % tiles, kb = (u / tiles) * planes, ke = min(n2, kb + planes);
+    const int i0 = (tile % t0) * 32 + threadIdx.x;
+    const int i1 = (tile / t0) * 8 + threadIdx.y;
+    if (i0 >= n0 || i1 >= n1) continue;
+    size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
+    for (int k = kb; k < ke; ++k, c += s01) {
+      const double rc = r[c];
+      p[c] = iter == 0 ? rc : fma(bc, __ldcg(p + c), rc);
     }
-    st->betaold = st->beta;
-    st->beta = tot[0];
-    st->iter += 1;
-    if (st->iter >= st->max_it) {
-      st->status = kDivergedIts;
-      return;
-    }
-    st->its = st->iter + 1;
-    if (st->beta == 0.0) {
-      st->status = kConvergedAtol;
-      return;
-    }
-    st->bcoef = st->beta / st->betaold;
-    if (st->bcoef < 0.0) st->status = kDivergedIndefinitePc;
   }
+  if (!grid_barrier(&st->bar_count, &st->bar_gen, &st->bar_timeout)) {
+    if (flat_tid() == 0) atomicExch(&st->status, (int)kGridBarrierTimeout);
+    return;
+  }
+  // 2. stencil product and p.w
+  double acc[1] = {0.0};
+  for (int u = bid; u < units; u += nb) {
+    const int tile = u % tiles, kb = (u / tiles) * planes, ke = min(n2, kb + planes);
+    const int i0 = (tile % t0) * 32 + threadIdx.x;
+    const int i1 = (tile / t0) * 8 + threadIdx.y;
+    if (i0 >= n0 || i1 >= n1) continue;
+    size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
+    double pm = 0.0, am = 0.0;
+    if (kb > 0) {
+      pm = __ldcg(p + c - s01);
+      am = a2[c - s01];
+    }
+    double pc = __ldcg(p + c);
+    for (int k = kb; k < ke; ++k) {
+      const double pp = (k + 1 < n2) ? __ldcg(p + c + s01) : 0.0;
+      const double ac = a2[c];
+      double v = pc;
+      if (i0 > 0) v = fma(a0[c - 1], __ldcg(p + c - 1), v);
+      if (i0 + 1 < n0) v = fma(a0[c], __ldcg(p + c + 1), v);
+      if (i1 > 0) v = fma(a1[c - n0], __ldcg(p + c - n0), v);
+      if (i1 + 1 < n1) v = fma(a1[c], __ldcg(p + c + n0), v);
+      v = fma(am, pm, v);
+      v = fma(ac, pp, v);
+      w[c] = v;
+      acc[0] = fma(pc, v, acc[0]);
+      pm = pc;
+      pc = pp;
+      am = ac;
+      c += s01;
+    }
+  }
+  __shared__ double sh[32];
+  __shared__ double dpi_sh;
+  double* pw = partials + 3 * (size_t)kMaxRedBlocks;
+  block_sum<1>(acc, sh);
+  if (flat_tid() == 0) pw[bid] = acc[0];
+  if (!grid_barrier(&st->bar_count, &st->bar_gen, &st->bar_timeout)) {
+    if (flat_tid() == 0) atomicExch(&st->status, (int)kGridBarrierTimeout);
+    return;
+  }
+  double t[1] = {0.0};
+  for (int b = flat_tid(); b < nb; b += flat_nthreads()) t[0] += __ldcg(&pw[b]);
+  block_sum<1>(t, sh);
+  if (flat_tid() == 0) dpi_sh = t[0];
+  __syncthreads();
+  const double dpi = dpi_sh;
+  const bool lead = bid == 0 && flat_tid() == 0;
+  if (dpi == 0.0 || (iter > 0 && ((dpi > 0.0) != (dpi_prev > 0.0))) || isnan(dpi)) {
+    if (lead) {
+      st->its = iter + 1;
+      st->status = isnan(dpi) ? kDivergedNanOrInf : kDivergedIndefiniteMat;
+    }
+    return;
+  }
+  const double a = beta / dpi;
+  if (lead) {
+    st->its = iter + 1;
+    st->dpiold = dpi_prev;
+    st->dpi = dpi;
+    st->a = a;
+  }
+  // 3. update and norms
+  double v[2] = {0.0, 0.0};
+  for (int u = bid; u < units; u += nb) {
+    const int tile = u % tiles, kb = (u / tiles) * planes, ke = min(n2, kb + planes);
+    const int i0 = (tile % t0) * 32 + threadIdx.x;
+    const int i1 = (tile / t0) * 8 + threadIdx.y;
+    if (i0 >= n0 || i1 >= n1) continue;
+    size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
+    for (int k = kb; k < ke; ++k, c += s01) {
+      x[c] = fma(a, __ldcg(p + c), x[c]);
+      const double rc = fma(-a, w[c], r[c]);
+      r[c] = rc;
+      v[0] = fma(rc, rc, v[0]);
+      const double z = s[c] * rc;
+      v[1] = fma(z, z, v[1]);
+    }
+  }
+  double tot[2];
+  if (!grid_sum<2>(v, partials, &st->arrive[2], tot)) return;
+  if (flat_tid() == 0) cg_update_tail(st, tot);
 }
 
 __global__ void k_unscale(const double* __restrict__ s, const double* __restrict__ xs,
@@ -448,11 +589,12 @@ int KrylovSolver::scale(Stencil64& A, cudaStream_t st) {
 }
 
 // Run a captured chunk graph until the device status leaves "running" or max_it is reached.
-int KrylovSolver::run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk) {
+int KrylovSolver::run_chunks(cudaGraphExec_t g, cudaStream_t st, int max_it, int chunk,
+                            int launches_per_it) {
   const int max_launch = max_it / chunk + 2;
   for (int q = 0; q < max_launch; ++q) {
     FG_CUDA(cudaGraphLaunch(g, st));
-    if (prof) prof->launches += 3 * chunk;
+    if (prof) prof->launches += (int64_t)launches_per_it * chunk;
     FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (hst->status != 0) return FREHG_OK;
@@ -487,6 +629,56 @@ int KrylovSolver::solve(Stencil64& A, double* x_out, const frehg_solver_config& 
   return solve64(A, x_out, cfg, st, res);
 }
 
+// Launch shape of k_cg_iter: the stencil tiles over at most the blocks the device holds at
+// once (a cooperative launch may not exceed them).  False where the device has no cooperative
+// launch or the shape does not fit.
+static bool cg_iter_launch(int n0, int n1, int n2, StencilLaunch* L) {
+  int dev = 0, coop = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_iter, 256, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (!coop || per_sm < 1 || sms < 1) return false;
+  const long resident = std::min<long>((long)per_sm * sms, kMaxRedBlocks);
+  const long t0 = (n0 + 31) / 32, t1 = (n1 + 7) / 8, tiles = t0 * t1;
+  // plane chunks short enough for about 16 work units per block (the blocks' shares then
+  // differ by at most a sixteenth), long enough to keep the stencil's march along axis 2
+  long planes = (tiles * n2 + 16 * resident - 1) / (16 * resident);
+  planes = std::max<long>(1, std::min<long>(planes, n2));
+  const long units = tiles * ((n2 + planes - 1) / planes);
+  if (units > (long)INT32_MAX - resident) return false;
+  // as few blocks as give every block the same number of units (small systems: fewer blocks
+  // to wait for at the grid barriers)
+  const long per_block = (units + resident - 1) / resident;
+  const long blocks = (units + per_block - 1) / per_block;
+  L->block = dim3(32, 8, 1);
+  L->grid = dim3((unsigned)blocks, 1, 1);
+  L->planes = (int)planes;
+  L->tiles = (int)tiles;
+  return true;
+}
+
+static cudaError_t launch_cg_iter(const StencilLaunch& L, cudaStream_t st, const Stencil64& A,
+                                  double* x, double* r, double* p, double* w, CgDevState* dst,
+                                  double* partials) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = L.grid;
+  cfg.blockDim = L.block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_cg_iter, (const double*)A.a0, (const double*)A.a1,
+                            (const double*)A.a2, (const double*)A.s, x, r, p, w, A.n0, A.n1,
+                            A.n2, L.planes, L.tiles, dst, partials);
+}
+
 static int chunk_for(size_t n) {
   if (n >= (size_t)4 << 20) return 16;
   if (n >= (size_t)1 << 18) return 32;
@@ -512,12 +704,20 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
 
   const int chunk = chunk_for(n);
   const StencilLaunch L = stencil_launch(A.n0, A.n1, A.n2);
+  StencilLaunch LF;
+  const bool want = !coop_failed && (fused64 > 0 || (fused64 < 0 && n <= kFusedAutoCells));
+  const int form = want && cg_iter_launch(A.n0, A.n1, A.n2, &LF) ? 1 : 0;
   if (prof && prof->on) {
     // profiled path: the same kernels launched one by one between CUDA events
     FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
     FG_CUDA(cudaStreamSynchronize(st));
     for (int q = 0; q < cfg.max_it / chunk + 2 && hst->status == 0; ++q) {
       for (int it = 0; it < chunk; ++it) {
+        if (form) {
+          FG_LAUNCH(prof, st, "k_cg_iter", 120.0 * dn,
+                    FG_CUDA(launch_cg_iter(LF, st, A, x, r, p, w, dst, partials)));
+          continue;
+        }
         FG_LAUNCH(prof, st, "k_cg_p", 24.0 * dn, k_cg_p<<<nb, 256, 0, st>>>(r, p, n, dst));
         FG_LAUNCH(prof, st, "k_cg_spmv", 40.0 * dn,
                   k_cg_spmv<<<L.grid, L.block, 0, st>>>(A.a0, A.a1, A.a2, p, w, A.n0, A.n1, A.n2,
@@ -533,7 +733,7 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
     return finish64(A, x_out, st, res, nb);
   }
   const bool rebuild = !g64 || g64_key != (const void*)A.a0 || g64_key2 != (const void*)A.s ||
-                       g_stream != st || g_n != n;
+                       g_stream != st || g_n != n || g64_form != form;
   if (rebuild) {
     if (g64) cudaGraphExecDestroy(g64);
     g64 = nullptr;
@@ -541,7 +741,13 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
     FG_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
     cudaGraph_t graph;
     FG_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaSuccess;
     for (int q = 0; q < chunk; ++q) {
+      if (form) {
+        const cudaError_t e1 = launch_cg_iter(LF, cap_st, A, x, r, p, w, dst, partials);
+        if (le == cudaSuccess) le = e1;
+        continue;
+      }
       k_cg_p<<<nb, 256, 0, cap_st>>>(r, p, n, dst);
       k_cg_spmv<<<L.grid, L.block, 0, cap_st>>>(A.a0, A.a1, A.a2, p, w, A.n0, A.n1, A.n2,
                                                 L.planes, L.tiles, dst, partials);
@@ -549,6 +755,13 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
     }
     cudaError_t e = cudaStreamEndCapture(cap_st, &graph);
     cudaStreamDestroy(cap_st);
+    if (le != cudaSuccess) {
+      // the cooperative launch was refused (e.g. under MPS): three kernels from now on
+      if (e == cudaSuccess) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      coop_failed = true;
+      return solve64(A, x_out, cfg, st, res);
+    }
     if (e != cudaSuccess) {
       set_error("graph capture failed: %s", cudaGetErrorString(e));
       return FREHG_ERR_CUDA;
@@ -563,11 +776,12 @@ int KrylovSolver::solve64(Stencil64& A, double* x_out, const frehg_solver_config
     g64_key2 = A.s;
     g_stream = st;
     g_n = n;
+    g64_form = form;
   }
   // iteration 0 may already have converged
   FG_TRY(fetch_small(hst, dst, sizeof(CgDevState), st));
   FG_CUDA(cudaStreamSynchronize(st));
-  if (hst->status == 0) FG_TRY(run_chunks(g64, st, cfg.max_it, chunk));
+  if (hst->status == 0) FG_TRY(run_chunks(g64, st, cfg.max_it, chunk, form ? 1 : 3));
   return finish64(A, x_out, st, res, nb);
 }
 
@@ -582,6 +796,11 @@ int KrylovSolver::finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResul
   res->rnorm = hst->dp;
   res->inner_its = hst->its;
   res->ir_its = 0;
+  if (hst->bar_timeout || hst->status == kGridBarrierTimeout) {
+    set_error("Krylov loop: a grid barrier of the one-launch CG iteration timed out after %d "
+              "iterations", hst->its);
+    return FREHG_ERR_CUDA;
+  }
   if (hst->status < 0) {
     set_error("KSP diverged (reason %d) after %d iterations, residual norm %g", hst->status,
               hst->its, hst->dp);

@@ -480,11 +480,19 @@ static bool mixed_solve(const frehg_re* re) {
   return re->cfg.precision == 1 || !strncmp(re->cfg.pc_type, "unet", 4);
 }
 
+// the Picard kernels in float-float arithmetic: picard_fp64 = 0, or -1 (the default) with the
+// mixed-precision solve.  With the FP64 solve the float-float kernels' noise floor in K
+// (about 1e-12 relative) leaves the late Picard solves right-hand sides that an FP64 CG to
+// rtol 1e-12 reduces only slowly, so the default keeps that path FP64 throughout.
+static bool picard_ff(const frehg_re* re) {
+  return re->p.picard_fp64 == 0 || (re->p.picard_fp64 < 0 && mixed_solve(re));
+}
+
 static int solve_system(frehg_re* re, double* x_out, CgResult* res) {
   cudaStream_t st = re->stream;
   frehg_solver_config cfg = re->cfg;
   // a Picard solve yields an update of the iterate: its operator may carry 48 bits
-  re->ksp.ff_operator = re->p.scheme == 1 && !re->p.picard_fp64;
+  re->ksp.ff_operator = re->p.scheme == 1 && picard_ff(re);
   const bool learned = !strncmp(cfg.pc_type, "unet", 4);
   re->ksp.net = NetPrecond();
   bool use_net = false;
@@ -734,7 +742,7 @@ static int picard_step(frehg_re* re) {
   bool all_ff = true;
   for (const SoilClass& k : re->cls_host) all_ff = all_ff && k.use_vg && !k.use_mvg;
   // a float-float assembly solved in mixed precision writes its matrix entries as floats
-  const bool f32 = !re->p.picard_fp64 && mixed_solve(re);
+  const bool f32 = picard_ff(re) && mixed_solve(re);
   if (f32) FG_TRY(re->ksp.ensure32(re->n));
   int its = 0;
   for (;;) {
@@ -745,7 +753,7 @@ static int picard_step(frehg_re* re) {
     bool converged = false;
     int fail = FREHG_OK;
     for (its = 0; its < re->p.picard_max_it; ++its) {
-      if (re->p.picard_fp64)
+      if (!picard_ff(re))
         FG_LAUNCH(prof, st, "k_kr", (32.0 + sb) * n,
                   (k_constit<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch,
                                                              re->cap)));
@@ -760,7 +768,7 @@ static int picard_step(frehg_re* re) {
       re->A.scaled = false;
       re->A.s_in_r = false;
       re->A.f32_entries = f32;
-      if (re->p.picard_fp64)
+      if (!picard_ff(re))
         FG_LAUNCH(prof, st, "k_pic_assemble", (88.0 + sb) * n,
                   k_pic_assemble<<<PL.grid, PL.block, 0, st>>>(a, re->A.s, re->A.a0, re->A.a1,
                                                                re->A.a2, re->A.b, PL.planes,
@@ -844,7 +852,7 @@ static int picard_step(frehg_re* re) {
     }
     dt = fmax(0.5 * dt, dt_floor);
   }
-  if (re->p.picard_fp64)
+  if (!picard_ff(re))
     FG_LAUNCH(prof, st, "k_pic_final", (40.0 + sb) * n,
               k_pic_final<<<PL.grid, PL.block, 0, st>>>(a, PL.planes, PL.tiles));
   else if (iso)
@@ -1485,7 +1493,7 @@ int frehg_re_check_staged_assembly(frehg_re* re, int64_t* mismatches) {
   FG_ARG(re && mismatches, "null argument");
   FG_ARG(re->finalized, "check before a finalized state");
   const ReArgs a = make_args(re);
-  if (re->p.scheme != 1 || re->p.picard_fp64 || !mixed_solve(re) || !re->fKs || (re->nx & 1)) {
+  if (re->p.scheme != 1 || !picard_ff(re) || !mixed_solve(re) || !re->fKs || (re->nx & 1)) {
     set_error("the staged assembly serves Picard handles in mixed precision with a per-cell Ks "
               "field and an even nx");
     return FREHG_ERR_UNSUPPORTED;
@@ -1595,6 +1603,14 @@ int frehg_re_set_assembly_staging(frehg_re* re, int on) {
   clear_error();
   FG_ARG(re, "null handle");
   re->staged = on != 0;
+  return FREHG_OK;
+}
+
+int frehg_re_set_fused_iteration(frehg_re* re, int on) {
+  clear_error();
+  FG_ARG(re, "null handle");
+  FG_ARG(on >= -1 && on <= 1, "on must be -1, 0 or 1");
+  re->ksp.fused64 = on;
   return FREHG_OK;
 }
 

@@ -1,5 +1,5 @@
 // Deterministic block / grid reductions shared by the kernels (last-arriving-block pattern:
-// no grid barrier, no spin-wait).
+// no grid barrier, no spin-wait), and the bounded grid barrier of cooperative launches.
 #pragma once
 
 #include "internal.h"
@@ -79,6 +79,43 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double* partials, unsi
   for (int q = 0; q < NV; ++q) tot[q] = acc[q];
   if (tid == 0) *arrive = 0u;
   return true;
+}
+
+// Grid barrier for cooperative launches (every block resident at once): an arrival counter
+// and a generation word in device memory, both 0 before the first use; the last block to
+// arrive resets the counter and advances the generation, so consecutive barriers and launches
+// reuse them.  The wait is bounded (kGridBarrierPolls polls, about two seconds); a block whose
+// wait runs out sets *timeout and gets false, and the caller stops (its launch then reports
+// the timeout instead of a result).
+constexpr long kGridBarrierPolls = 1L << 24;
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int* gen,
+                                             int* timeout) {
+  __shared__ int ok;
+  __syncthreads();
+  if (flat_tid() == 0) {
+    volatile unsigned int* vgen = gen;
+    const unsigned int g = *vgen;
+    __threadfence();
+    int good = 1;
+    if (atomicAdd(count, 1u) + 1u == (unsigned int)flat_nblocks()) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      for (long q = 0; *vgen == g; ++q) {
+        if (q >= kGridBarrierPolls) {
+          good = 0;
+          atomicExch(timeout, 1);
+          break;
+        }
+        if (q >= 256) __nanosleep(100);  // poll at once first: most waits are short
+      }
+      __threadfence();
+    }
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
 }
 
 // Grid-wide max through per-block partials (NaN-ignoring, as std::max/std::min with a NaN

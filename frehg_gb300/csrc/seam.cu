@@ -90,6 +90,7 @@ void frehg_re_params_default(frehg_re_params* p) {
   p->bc_type[5] = 1;
   p->picard_max_it = 50;
   p->picard_tol = 1.0e-6;
+  p->picard_fp64 = -1;
 }
 
 void frehg_solver_config_default(frehg_solver_config* c) {
@@ -352,6 +353,14 @@ int frehg_cg_converged_reason(const frehg_cg* cg, int* reason) {
   clear_error();
   FG_ARG(cg && reason, "null argument");
   *reason = cg->last.reason;
+  return FREHG_OK;
+}
+
+int frehg_cg_set_fused_iteration(frehg_cg* cg, int on) {
+  clear_error();
+  FG_ARG(cg, "null handle");
+  FG_ARG(on >= -1 && on <= 1, "on must be -1, 0 or 1");
+  cg->ksp.fused64 = on;
   return FREHG_OK;
 }
 

@@ -109,6 +109,12 @@ class GpuLinearSolver:
         check(self._lib.frehg_cg_converged_reason(self._h, C.byref(v)), "getConvergedReason")
         return v.value
 
+    def setFusedIteration(self, on):
+        """FP64 Jacobi-PCG: one cooperative launch per iteration (True), three kernels (False)
+        or, None (the default), one launch up to 65,536 unknowns (not in reference)."""
+        v = -1 if on is None else int(bool(on))
+        check(self._lib.frehg_cg_set_fused_iteration(self._h, v), "setFusedIteration")
+
 
 def makeLinearSolver(backend: str, cfg: SolverConfig):
     """LinearSolverFactory (src/linear/backends/LinearSolverFactory.cpp:9-16) with the gb300

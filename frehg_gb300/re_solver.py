@@ -273,6 +273,12 @@ class ReSolver:
         not in reference)."""
         check(self._lib.frehg_re_set_assembly_staging(self._h, int(bool(on))), "setAssemblyStaging")
 
+    def set_fused_iteration(self, on):
+        """FP64 Jacobi-PCG solves as one cooperative launch per iteration (True), three kernels
+        (False) or, None (the default), one launch up to 65,536 unknowns (not in reference)."""
+        v = -1 if on is None else int(bool(on))
+        check(self._lib.frehg_re_set_fused_iteration(self._h, v), "setFusedIteration")
+
     def set_profiling(self, on: bool):
         check(self._lib.frehg_re_set_profiling(self._h, int(bool(on))), "setProfiling")
 

@@ -101,9 +101,11 @@ typedef struct frehg_re_params {
                              admits (no ponding, the excess runs off); 0 disables             */
   double rain_until;      /* [s]                                                             */
   int32_t picard_dt_adapt;/* Picard-count driven dt (1) or fixed (0)                         */
-  int32_t picard_fp64;    /* Picard constitutive relations (van Genuchten classes) in native
-                             FP64 (1) or in float-float arithmetic on the FP32 pipe, ~48
-                             significant bits, several times faster on GB300 (0, default)    */
+  int32_t picard_fp64;    /* Picard constitutive relations, fluxes and final update
+                             (van Genuchten classes) in native FP64 (1) or in float-float
+                             arithmetic on the FP32 pipe, ~48 significant bits, several times
+                             faster on GB300 (0); -1 (default): float-float with the mixed-
+                             precision solve, FP64 with the FP64 solve                       */
   double picard_dh_max;   /* largest head change one Picard iteration applies per cell [m];
                              0 = unlimited (default)                                         */
 } frehg_re_params;
@@ -281,6 +283,14 @@ int frehg_cg_solve(frehg_cg* cg, frehg_system* sys, const double* b, double* x, 
 int frehg_cg_iteration_count(const frehg_cg* cg, int* its);   /* getIterationCount */
 int frehg_cg_residual_norm(const frehg_cg* cg, double* rnorm); /* getResidualNorm   */
 int frehg_cg_converged_reason(const frehg_cg* cg, int* reason); /* KSPConvergedReason */
+/* Not in reference: the FP64 Jacobi-PCG iteration (precision 0, pc_type "jacobi") as one
+ * cooperative launch (direction, stencil product with p.w and update with the norms, separated
+ * by grid barriers whose waits are bounded) or as three kernels.  on = 1: one launch wherever
+ * the device has cooperative launches; 0: three kernels; -1 (default): one launch for systems
+ * of at most 65,536 unknowns, where it is the faster form on GB300, three kernels above.  The
+ * two forms sum the dot products over different block partitions, so their last bits (and, in
+ * a borderline case, an iteration count) may differ. */
+int frehg_cg_set_fused_iteration(frehg_cg* cg, int on);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Learned preconditioner (not in reference): 3-level 3D U-Net (16/32/64 channels, 3x3x3 conv,  */
@@ -336,6 +346,8 @@ int frehg_re_set_learned_policy(frehg_re* re, int probe_every, double max_ratio)
  * the assembly is bound by float-float instruction issue, not by memory (the staged kernel moves
  * fewer DRAM bytes but runs about 5 % longer on GB300). */
 int frehg_re_set_assembly_staging(frehg_re* re, int on);
+/* Not in reference: frehg_cg_set_fused_iteration for the handle's FP64 Jacobi-PCG solves. */
+int frehg_re_set_fused_iteration(frehg_re* re, int on);
 /* Training pairs from the plain solver: assembles the next PCA step's system at the current
  * state (nothing advances), solves it with FP64 Jacobi-PCG, re-runs the iteration from zero and
  * at each iteration number iters[q] (increasing) stores the scaled residual r~ and a target
@@ -361,7 +373,8 @@ int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, int targ
  *   - all calls share the array: calls that overlap on the GPU race; serialise them;
  *   - no cudaMalloc, cudaFree or other allocating routine is called.
  * stream: cudaStream_t as void* (NULL = the legacy default stream).  Same stopping rule,
- * iteration count and residual norm as frehg_cg_solve (Jacobi-PCG, PETSc semantics). */
+ * iteration count and residual norm as frehg_cg_solve in its three-kernel form
+ * (frehg_cg_set_fused_iteration 0; Jacobi-PCG, PETSc semantics). */
 int frehg_cg_solve_noalloc(int nx, int ny, int nz, const double* diag, const double* a_k,
                            const double* a_i, const double* a_j, const double* b, double* x,
                            const frehg_solver_config* cfg, void* stream, int* its,

@@ -83,7 +83,11 @@ def input_digest(w, case) -> str:
     whose last bits may differ between machines, so the fixture stores them and the tests use
     the stored values."""
     h = hashlib.sha256()
-    h.update(bytes(w.params))
+    # picard_fp64 only chooses the GPU's Picard kernels, not the step's inputs: hashed as 0,
+    # the value the fixtures were written with
+    p = type(w.params).from_buffer_copy(bytes(w.params))
+    p.picard_fp64 = 0
+    h.update(bytes(p))
     h.update(bytes(w.solver))
     for a in (w.h0, w.wc0, w.class_index, w.top_flux):
         if a is not None:

@@ -2,7 +2,8 @@
 
 Per step: head within 1e-8 m (max norm), equal Picard iteration counts; cumulative mass
 balance closes below 1e-12 relative on the GPU.  The GPU kernels run in float-float arithmetic
-(the default, picard_fp64 = 0) unless a test selects native FP64 (picard_fp64 = 1)."""
+(picard_fp64 = 0, set here: the library's default picks it with the mixed-precision solve only)
+unless a test selects native FP64 (picard_fp64 = 1)."""
 import numpy as np
 import pytest
 
@@ -13,6 +14,8 @@ pytestmark = pytest.mark.gpu
 
 def pair(w, oracle_mod):
     from frehg_gb300.re_solver import Grid, ReSolver
+    if w.params.picard_fp64 < 0:
+        w.params.picard_fp64 = 0
     g = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
     o = oracle_mod.OracleRe(w.nx, w.ny, w.nz, w.params)
     w.apply(g)

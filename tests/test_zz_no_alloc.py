@@ -36,10 +36,12 @@ def spd_owned(nx, ny, nz, seed):
 
 
 def reference_solve(nx, ny, nz, diag, a_k, a_i, a_j, b, cfg):
-    """the allocating entry point: rows through addCOO, frehg_cg_solve"""
+    """the allocating entry point: rows through addCOO, frehg_cg_solve in the three-kernel
+    form of the iteration, which the allocation-free solve runs"""
     from frehg_gb300.linear import makeLinearSolver
     n = nx * ny * nz
     s = makeLinearSolver("gb300", cfg)
+    s.setFusedIteration(False)
     A = s.createSystem(nx, ny, nz)
     A.zeroEntries()
     r = np.arange(n)
