@@ -503,29 +503,52 @@ def step_roofline(args, w, cnt, ms):
                        f" + {per_krylov:.0f} x Krylov iterations)"}
 
 
+def rank_ops(world, local, backend="nccl"):
+    """The replicas' host-side coordination: (barrier, max_over_ranks).  One process per GPU,
+    no collective on the data path; the barrier brackets the timed region and the slowest
+    rank's time sets the job's.  backend "nccl" on GPUs (the device is synchronised as well),
+    "gloo" for the CPU tests of this logic."""
+    import torch
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            if backend == "nccl":
+                dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+            else:
+                dist.init_process_group(backend)
+        pg = dist
+    on_gpu = backend == "nccl"
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        if on_gpu:
+            torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if not pg:
+            return v
+        t = torch.tensor([float(v)], dtype=torch.float64, device="cuda" if on_gpu else "cpu")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
+def replica_rate(cells, steps, world, ms_max):
+    """whole-job cells·steps/s of `world` replicas that each ran `steps` steps of `cells`
+    cells, the slowest taking ms_max milliseconds"""
+    return cells * steps * world / (ms_max / 1000.0)
+
+
 def run_gpu(args):
     import numpy as np
     import torch
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-        pg = dist
-
-    def barrier():
-        if pg:
-            pg.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(v):
-        if not pg:
-            return v
-        t = torch.tensor([v], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = rank_ops(world, local)
 
     from frehg_gb300 import build as B
     B.build()
@@ -544,7 +567,7 @@ def run_gpu(args):
     s, ms, cnt, reset = time_arm(args, w, net, stream, barrier, args.steps, args.warmup)
     clk = clocks.stop()
     ms_max = max_over_ranks(ms)
-    value = w.cells * args.steps * world / (ms_max / 1000.0)
+    value = replica_rate(w.cells, args.steps, world, ms_max)
     h_fast = s.interior("h").copy()
 
     # end to end through the public API: per step H2D of the top forcing (rain or qtop per
@@ -581,7 +604,7 @@ def run_gpu(args):
     stream.synchronize()
     barrier()
     e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0)))
-    e2e_value = w.cells * args.steps * world / (e2e_ms / 1000.0)
+    e2e_value = replica_rate(w.cells, args.steps, world, e2e_ms)
 
     # per-kernel durations from CUDA events on the launching stream (profiling pass)
     reset()
@@ -659,7 +682,7 @@ def run_gpu(args):
         h64 = s64.interior("h")
         del s64
         dh = np.abs(h_fast - h64)
-        v64 = w.cells * args.steps * world / (ms64 / 1000.0)
+        v64 = replica_rate(w.cells, args.steps, world, ms64)
         comparison = {
             "plain_fp64": {"value": v64, "ms_per_step": ms64 / args.steps,
                            "cg_iterations": cnt64["ksp_iterations"],
