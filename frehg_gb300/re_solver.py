@@ -57,6 +57,11 @@ class SoilMap:
         self.index, self.is3d = idx, True
 
 
+# GwFields arrays in a checkpoint record (those frehg_re_get_field materialises)
+GW_RECORD_FIELDS = ("h", "hn", "wc", "wcn", "wch", "hwc", "ch", "Kx", "Ky", "Kz", "qx", "qy",
+                    "qz", "room", "bot3d", "dz3d", "actv")
+
+
 class Fields:
     """Lazy view of GwFields (src/re/GwFields.hpp:52-59): fields['h'] is the halo array as a
     (nz+2, ny+2, nx+2) numpy array copied from the device on access."""
@@ -215,6 +220,56 @@ class ReSolver:
         wc = np.ascontiguousarray(cp["wc"], dtype=np.float64)
         st = np.ascontiguousarray(cp["state"], dtype=np.float64)
         check(self._lib.frehg_re_restart(self._h, dptr(h), dptr(wc), dptr(st)), "restart")
+
+    def checkpoint_record(self) -> dict:
+        """The groundwater part of the reference's checkpoint record (Orchestrator::
+        writeCheckpointNow, src/driver/Orchestrator.cpp:1461-1502): cp.h, cp.hn, cp.wc, cp.wcn
+        and, under "gw_<name>", every GwFields array (src/re/GwFields.hpp:62-74) that
+        frehg_re_get_field materialises, each flattened in the halo layout
+        ((nx+2)(ny+2)(nz+2) doubles, Grid::getIndex order), with time, dt and the layout tag
+        "internal-with-halo".  The matrix and density arrays of namedViews (G*, r_*) are
+        rewritten by every step before they are read and are not part of it.  The names and
+        layout are the HDF5 checkpoint's (np.savez(path, **record) keeps them on disk here,
+        where no HDF5 library is present)."""
+        rec = {"time": np.float64(self.time()), "dt": np.float64(self.dt()),
+               "storage_layout": "internal-with-halo", "has_gw": True}
+        for name in GW_RECORD_FIELDS:
+            rec["gw_" + name] = self.field(name).ravel().copy()
+        for name in ("h", "hn", "wc", "wcn"):
+            rec[name] = rec["gw_" + name]
+        return rec
+
+    def restart_from_record(self, rec):
+        """Continue from a checkpoint record in the reference's layout (the groundwater part of
+        Orchestrator::loadCheckpointState, Orchestrator.cpp:688-747): the head and water content
+        from gw_h and gw_wc (the arrays the next step reads; it recomputes the rest), then
+        primeAdaptiveDt(dt) and the record's time.  A missing field or a size mismatch raises,
+        as the reference does.  The head's ghost layer tells whether a step has run (its
+        enforceHeadBc wrote it; the first step after an initial state reads zero ghosts)."""
+        g = self.grid
+        shape = (g.nz + 2, g.ny + 2, g.nx + 2)
+        arrays = {}
+        for name in ("h", "wc"):
+            key = "gw_" + name
+            if key not in rec:
+                raise RuntimeError(f"checkpoint load: missing field '{key}'")
+            a = np.asarray(rec[key], dtype=np.float64)
+            if a.size != shape[0] * shape[1] * shape[2]:
+                raise RuntimeError(f"checkpoint load: field '{key}' size mismatch (grid differs "
+                                   "from checkpoint)")
+            arrays[name] = a.reshape(shape)
+        h = arrays["h"]
+        shell = np.ones(shape, dtype=bool)
+        shell[1:-1, 1:-1, 1:-1] = False
+        ghosts = bool(np.any(h[shell] != 0.0))
+        dt = float(rec["dt"])
+        st = np.zeros(CHECKPOINT_SCALARS)
+        st[0] = float(rec.get("time", 0.0))
+        st[1:4] = dt  # dt, dtn (primeAdaptiveDt) and the last step's dt
+        st[7] = 1.0 if ghosts else 0.0
+        self.restart({"h": np.ascontiguousarray(h[1:-1, 1:-1, 1:-1]).ravel(),
+                      "wc": np.ascontiguousarray(arrays["wc"][1:-1, 1:-1, 1:-1]).ravel(),
+                      "state": st})
 
     # -- outputs ---------------------------------------------------------------------------
     def field(self, name) -> np.ndarray:

@@ -296,6 +296,17 @@ class GwFields {
   }
   std::vector<real> h() const { return get("h"); }
   std::vector<real> wc() const { return get("wc"); }
+  // Every array the GPU state materialises, paired with its GwFields name, for the reference's
+  // checkpoint writer (GwFields::namedViews, GwFields.hpp:62-74; Orchestrator::
+  // writeCheckpointNow stores each as "gw_<name>").  The matrix and density arrays (G*, r_*)
+  // are rewritten by every step before they are read and are not materialised.
+  std::vector<std::pair<std::string, std::vector<real>>> namedViews() const {
+    static const char* const names[] = {"h",  "hn", "wc", "wcn", "wch",  "hwc",  "ch",  "Kx", "Ky",
+                                        "Kz", "qx", "qy", "qz",  "room", "bot3d", "dz3d", "actv"};
+    std::vector<std::pair<std::string, std::vector<real>>> v;
+    for (const char* n : names) v.emplace_back(n, get(n));
+    return v;
+  }
 
  private:
   frehg_re* re_;
@@ -413,6 +424,44 @@ class ReSolver {
     size_check(cp.wc.size(), "restart");
     check(frehg_re_restart(re_, cp.h.data(), cp.wc.data(), cp.state), "restart");
     params_.dt = cp.state[1];
+  }
+  // Restart from the reference's checkpoint record (the groundwater part of
+  // Orchestrator::loadCheckpointState, Orchestrator.cpp:688-747): the gw_h and gw_wc arrays in
+  // the halo layout (the arrays the next step reads; it recomputes the rest), then
+  // primeAdaptiveDt(dt) and the record's time.  The head's ghost layer tells whether a step
+  // has run (its enforceHeadBc wrote it; the first step after an initial state reads zeros).
+  void restartFromFields(const std::vector<real>& h_halo, const std::vector<real>& wc_halo,
+                         real dt, real time = 0.0) {
+    if ((long)h_halo.size() != grid_.nCell() || (long)wc_halo.size() != grid_.nCell())
+      throw std::runtime_error(
+          "checkpoint load: field size mismatch (grid differs from checkpoint)");
+    Checkpoint cp;
+    const size_t n = (size_t)grid_.nx * grid_.ny * grid_.nz;
+    cp.h.resize(n);
+    cp.wc.resize(n);
+    size_t q = 0;
+    for (int k = 0; k < grid_.nz; ++k)
+      for (int j = 0; j < grid_.ny; ++j)
+        for (int i = 0; i < grid_.nx; ++i, ++q) {
+          cp.h[q] = h_halo[(size_t)grid_.getIndex(i, j, k)];
+          cp.wc[q] = wc_halo[(size_t)grid_.getIndex(i, j, k)];
+        }
+    bool ghosts = false;
+    for (int k = -1; k <= grid_.nz && !ghosts; ++k)
+      for (int j = -1; j <= grid_.ny && !ghosts; ++j)
+        for (int i = -1; i <= grid_.nx; ++i) {
+          const bool inner = i >= 0 && i < grid_.nx && j >= 0 && j < grid_.ny && k >= 0 &&
+                             k < grid_.nz;
+          if (!inner && h_halo[(size_t)grid_.getIndex(i, j, k)] != 0.0) {
+            ghosts = true;
+            break;
+          }
+        }
+    for (double& v : cp.state) v = 0.0;
+    cp.state[0] = time;
+    cp.state[1] = cp.state[2] = cp.state[3] = dt;  // dt, dtn (primeAdaptiveDt), last dt
+    cp.state[7] = ghosts ? 1.0 : 0.0;
+    restart(cp);
   }
   // groundwater side of Coupling::exchange: eta (surface level per column, i + j*nx) is updated
   // in place, q (if given) receives the limited rates [m^3/s]; returns sum q dt

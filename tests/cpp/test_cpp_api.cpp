@@ -138,7 +138,7 @@ static void errors() {
 static void closed_box() {
   const int nx = 4, ny = 4, nz = 8;
   g::Grid grid(nx, ny, nz, 2.0, 1.0, 0.05);
-  g::ReSolver re(grid);
+  g::ReSolver re(grid), re2(grid);
   g::ReParams p;
   p.dx = 2.0;
   p.dy = 1.0;
@@ -155,20 +155,23 @@ static void closed_box() {
   p.soil.theta_r = 0.05;
   p.soil.Ks_x = p.soil.Ks_y = p.soil.Ks_z = 1.0e-5;
   p.soil.Ss = 0.0;
-  re.setParams(p);
   g::SolverConfig cfg;
   cfg.rtol = 1e-13;
   auto ls = g::makeLinearSolver("gb300", cfg);
+  auto ls2 = g::makeLinearSolver("gb300", cfg);
   g::Decomp3D dd(nx, ny, nz);
-  re.attachSolver(*ls, dd);
-  re.initializeGeometry();
   std::vector<double> wc((size_t)nx * ny * nz);
   for (int k = 0; k < nz; ++k)
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i)
         wc[i + nx * (j + ny * k)] = 0.20 + 0.03 * std::sin(0.9 * i) + 0.02 * std::cos(0.7 * j);
-  re.setInitialWaterContent(wc);
-  re.finalizeInitialState();
+  for (g::ReSolver* r : {&re, &re2}) {
+    r->setParams(p);
+    r->attachSolver(r == &re ? *ls : *ls2, dd);
+    r->initializeGeometry();
+    r->setInitialWaterContent(wc);
+    r->finalizeInitialState();
+  }
   const double v0 = re.waterVolume();
   for (int s = 0; s < 39; ++s) re.advanceStep();
   // the last step's result copied while one more step runs: the copy holds the state before it
@@ -187,6 +190,28 @@ static void closed_box() {
   EXPECT(std::isfinite(h[grid.getIndex(1, 2, 3)]) && re.dtUsed() == 5.0,
          "fields() readable, dtUsed %.1f", re.dtUsed());
 
+  // the reference's checkpoint record (namedViews in the halo layout, dt) restarts a second
+  // solver, which then steps exactly like the first
+  const auto views = re.fields().namedViews();
+  EXPECT(views.size() == 17 && views[0].first == "h" && views[2].first == "wc" &&
+             (long)views[0].second.size() == grid.nCell() && views[0].second == h,
+         "fields().namedViews(): %zu named halo arrays", views.size());
+  re2.restartFromFields(views[0].second, views[2].second, re.dt());
+  for (int s = 0; s < 2; ++s) {
+    re.advanceStep();
+    re2.advanceStep();
+  }
+  EXPECT(re.interior("h") == re2.interior("h") && re.interior("wc") == re2.interior("wc"),
+         "restartFromFields: two more steps equal the continuous run's bit for bit");
+  bool threw = false;
+  try {
+    re2.restartFromFields(std::vector<double>(3), views[2].second, re.dt());
+  } catch (const std::runtime_error&) {
+    threw = true;
+  }
+  EXPECT(threw, "restartFromFields refuses a record of another grid");
+  const double v1b = re.waterVolume();
+
   // ponded water on half the columns infiltrates through the top face: the surface loses what
   // the soil gains
   std::vector<double> eta((size_t)nx * ny), bottom((size_t)nx * ny, 0.0), q;
@@ -198,7 +223,7 @@ static void closed_box() {
   const double v2 = re.waterVolume();
   EXPECT(total < 0.0 && q.size() == eta.size() && q[0] == 0.0 && q[1] < 0.0,
          "surfaceExchange: infiltration where ponded (total %.3e m^3)", total);
-  const double bal = std::fabs((surf1 - surf0) + (v2 - v1)) / std::fabs(total);
+  const double bal = std::fabs((surf1 - surf0) + (v2 - v1b)) / std::fabs(total);
   EXPECT(bal < 1e-10 && std::fabs((surf0 - surf1) + total) < 1e-15,
          "surfaceExchange conserves water: imbalance %.3e of the exchanged volume", bal);
 }

@@ -76,3 +76,57 @@ def test_checkpoint_refused_after_surface_exchange(gpu_lib):
     assert e.value.code == FREHG_ERR_STATE
     g.advance_step()
     g.checkpoint()  # between steps again
+
+
+@pytest.mark.parametrize("scheme", ["pca", "picard"])
+def test_restart_from_reference_layout_record(gpu_lib, scheme):
+    """A checkpoint record in the reference's layout (gw_<name> halo arrays, dt, time, the
+    "internal-with-halo" tag) written by one handle and read by a new one: the FP64 path's next
+    steps equal the continuous run's bit for bit."""
+    w = W.config1(scheme, nx=16, ny=12, nz=24, steps=6)
+    a = new(w)
+    for _ in range(3):
+        a.advance_step()
+    rec = a.checkpoint_record()
+    assert rec["storage_layout"] == "internal-with-halo"
+    assert rec["gw_h"].size == 18 * 14 * 26 and np.array_equal(rec["h"], rec["gw_h"])
+    b = new(w)
+    b.restart_from_record(rec)
+    for s in range(3):
+        a.advance_step()
+        b.advance_step()
+        assert np.array_equal(a.interior("h"), b.interior("h")), f"step {s}"
+        assert np.array_equal(a.interior("wc"), b.interior("wc")), f"step {s}"
+        assert a.dt() == b.dt() and a.time() == b.time()
+
+
+def test_restart_from_oracle_record(gpu_lib, oracle_mod):
+    """The oracle (the reference's step restated with the reference's halo storage) writes the
+    record after three steps; a GPU handle restarted from it follows the oracle's next steps
+    within 1e-8 m."""
+    w = W.config1("pca", nx=16, ny=12, nz=24, steps=6)
+    o = oracle_mod.OracleRe(w.nx, w.ny, w.nz, w.params)
+    w.apply(o)
+    for _ in range(3):
+        o.advance_step()
+    rec = {"gw_h": o.field("h").ravel(), "gw_wc": o.field("wc").ravel(), "dt": o.dt(),
+           "time": o.time()}
+    g = new(w)
+    g.restart_from_record(rec)
+    for s in range(3):
+        o.advance_step()
+        g.advance_step()
+        assert np.abs(g.interior("h") - o.interior("h")).max() <= 1e-8, f"step {s}"
+        assert abs(g.dt() - o.dt()) <= 1e-12 * o.dt()
+
+
+def test_record_missing_or_mismatched_fields(gpu_lib):
+    w = W.config1("pca", nx=8, ny=6, nz=10, steps=1)
+    g = new(w)
+    g.advance_step()
+    rec = g.checkpoint_record()
+    with pytest.raises(RuntimeError, match="missing field 'gw_wc'"):
+        g.restart_from_record({k: v for k, v in rec.items() if k != "gw_wc"})
+    bad = dict(rec, gw_h=rec["gw_h"][:-1])
+    with pytest.raises(RuntimeError, match="size mismatch"):
+        g.restart_from_record(bad)
