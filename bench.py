@@ -741,8 +741,10 @@ def run_gpu(args):
                                          policy="probe every 32 solves, keep if <= 1.0x plain time")
     if rank == 0:
         print(json.dumps(line))
-    if pg:
-        pg.destroy_process_group()
+    if world > 1:
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.destroy_process_group()
     return 0
 
 
