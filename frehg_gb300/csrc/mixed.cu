@@ -48,36 +48,14 @@ __device__ __forceinline__ void line_first_state(CgDevState* in, double rz) {
 // (Applying the line preconditioner to the new right-hand side in the same column march, as
 // k_prep_ff does for the first sweep, made this kernel slower by more than the separate
 // k32_line_fwd<false> takes.)
-// XE (the second sweep's residual): x~ is the first inner solution, x~ = rscale e, which this
-// kernel forms itself from e (integer operations, as k_ir_update<true> does) for the cell and
-// its neighbours, and writes for the cell; the first sweep's k_ir_update then does not run.
-// The iterate's bits are those k_ir_update<true> writes.  rscale and the inner iteration count
-// are read before this launch's reduction, after which its last block sets the next ones.
-template <bool FIRST, bool INV_S = false, bool XE = false>
+template <bool FIRST, bool INV_S = false>
 __global__ void __launch_bounds__(256) k_ir_residual(
     const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ s, const double* __restrict__ sq, const double* __restrict__ b,
     double* __restrict__ x, double* __restrict__ rres, int n0, int n1, int n2, int planes,
     int tiles, CgDevState* ir, double* partials, double ir_rtol,
-    float* __restrict__ rfo = nullptr, CgDevState* in = nullptr, double inner_rtol = 0.0,
-    const float* __restrict__ e = nullptr) {
+    float* __restrict__ rfo = nullptr, CgDevState* in = nullptr, double inner_rtol = 0.0) {
   if (ir->status) return;
-  // XE: rscale = 2^scale (k_ir_update's power-of-two path) unless no path set one; an inner
-  // solve that stopped before its first iteration contributes e = 0
-  bool e_zero = false, e_pow2 = true;
-  int e_scale = 0;
-  double e_rs = 1.0;
-  if (XE) {
-    e_zero = in->iter == 0;
-    e_rs = ir->rscale;
-    e_scale = pow2_above(e_rs) - 1;
-    e_pow2 = e_rs == pow2d(e_scale);
-  }
-  auto xv = [&](size_t q) -> double {
-    if (!XE) return x[q];
-    if (e_zero) return 0.0;
-    return e_pow2 ? f2d_scaled(e[q], e_scale) : e_rs * (double)e[q];
-  };
   const int t0 = (n0 + 31) / 32;
   const size_t s01 = (size_t)n0 * n1;
   double v[3] = {0.0, 0.0, 0.0};
@@ -113,14 +91,13 @@ __global__ void __launch_bounds__(256) k_ir_residual(
       const int kb = blockIdx.y * planes, ke = min(n2, kb + planes);
       size_t c = (size_t)i0 + (size_t)n0 * i1 + s01 * kb;
       for (int k = kb; k < ke; ++k, c += s01) {
-        double ax = xv(c);
-        if (XE) x[c] = ax;
-        if (i0 > 0) ax = fma(a0[c - 1], xv(c - 1), ax);
-        if (i0 + 1 < n0) ax = fma(a0[c], xv(c + 1), ax);
-        if (i1 > 0) ax = fma(a1[c - n0], xv(c - n0), ax);
-        if (i1 + 1 < n1) ax = fma(a1[c], xv(c + n0), ax);
-        if (k > 0) ax = fma(a2[c - s01], xv(c - s01), ax);
-        if (k + 1 < n2) ax = fma(a2[c], xv(c + s01), ax);
+        double ax = x[c];
+        if (i0 > 0) ax = fma(a0[c - 1], x[c - 1], ax);
+        if (i0 + 1 < n0) ax = fma(a0[c], x[c + 1], ax);
+        if (i1 > 0) ax = fma(a1[c - n0], x[c - n0], ax);
+        if (i1 + 1 < n1) ax = fma(a1[c], x[c + n0], ax);
+        if (k > 0) ax = fma(a2[c - s01], x[c - s01], ax);
+        if (k + 1 < n2) ax = fma(a2[c], x[c + s01], ax);
         const double r = fma(s[c], b[c], -ax);
         const float rf = ff_hi_of(r);
         // sq r~ = r~ / s (INV_S: s holds floats and sq is not stored)
@@ -1042,18 +1019,6 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
                       L.tiles, dst, partials, cfg.ir_rtol));
       else
         fwd0_done = first_line_here;
-    } else if (sweeps == 1) {
-      // the second sweep's residual also forms and writes x~ = rscale e of the first
-      if (A.s_in_r)
-        FG_LAUNCH(prof, st, "k_ir_residual", 52.0 * dn,
-                  (k_ir_residual<false, true, true><<<L.grid, L.block, 0, st>>>(
-                      A.a0, A.a1, A.a2, sv, sv, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
-                      L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol, xf)));
-      else
-        FG_LAUNCH(prof, st, "k_ir_residual", 52.0 * dn,
-                  (k_ir_residual<false, false, true><<<L.grid, L.block, 0, st>>>(
-                      A.a0, A.a1, A.a2, A.s, r, A.b, x, rres, A.n0, A.n1, A.n2, L.planes,
-                      L.tiles, dst, partials, cfg.ir_rtol, rf, dst32, cfg.inner_rtol, xf)));
     } else if (A.s_in_r) {
       FG_LAUNCH(prof, st, "k_ir_residual", 52.0 * dn,
                 (k_ir_residual<false, true><<<L.grid, L.block, 0, st>>>(
@@ -1197,8 +1162,10 @@ int KrylovSolver::solve_mixed(Stencil64& A, double* x_out, const frehg_solver_co
       fprintf(stderr, "ir sweep %d: true |r| %.3e / |b| %.3e ; inner its %d status %d |r0| %.3e -> %.3e\n",
               sweeps, hst->ir_rnorm, hst->ir_bnorm, hst32->its, hst32->status, hst32->rnorm0,
               hst32->dp);
-    // the first sweep's update x~ = rscale e is formed by the second sweep's residual kernel
-    if (sweeps > 0)
+    if (sweeps == 0)
+      FG_LAUNCH(prof, st, "k_ir_update", 12.0 * dn,
+                k_ir_update<true><<<nb, 256, 0, st>>>(x, xf, n, dst, dst32));
+    else
       FG_LAUNCH(prof, st, "k_ir_update", 20.0 * dn,
                 k_ir_update<false><<<nb, 256, 0, st>>>(x, xf, n, dst, dst32));
     FG_CUDA(cudaGetLastError());
