@@ -249,6 +249,7 @@ SIGNATURES = {
     "frehg_cg_residual_norm": (C.c_int, [_VP, _PD]),
     "frehg_cg_converged_reason": (C.c_int, [_VP, _PI]),
     "frehg_cg_set_fused_iteration": (C.c_int, [_VP, C.c_int]),
+    "frehg_check_grid_barrier": (C.c_int, [C.c_int, C.c_longlong, _PI]),
     "frehg_cg_solve_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _VP,
                                          _VP, C.POINTER(SolverConfig), _VP, _PI, _PD]),
     "frehg_unet_create": (C.c_int, [C.c_uint64, C.POINTER(_VP)]),

@@ -629,6 +629,15 @@ int KrylovSolver::solve(Stencil64& A, double* x_out, const frehg_solver_config& 
   return solve64(A, x_out, cfg, st, res);
 }
 
+// Self-check of the grid barrier: every block but skip_block waits at one barrier with a
+// bound of `polls` polls; with a block that never arrives the others' waits run out and set
+// *timeout, and the kernel returns normally.
+__global__ void k_barrier_check(unsigned int* count, unsigned int* gen, int* timeout,
+                                int skip_block, long polls) {
+  if ((int)blockIdx.x == skip_block) return;
+  grid_barrier(count, gen, timeout, polls);
+}
+
 // Launch shape of k_cg_iter: the stencil tiles over at most the blocks the device holds at
 // once (a cooperative launch may not exceed them).  False where the device has no cooperative
 // launch or the shape does not fit.
@@ -810,3 +819,38 @@ int KrylovSolver::finish64(Stencil64& A, double* x_out, cudaStream_t st, CgResul
 }
 
 }  // namespace fg
+
+extern "C" int frehg_check_grid_barrier(int skip_block, long long polls, int* timed_out) {
+  using namespace fg;
+  clear_error();
+  FG_ARG(timed_out && polls > 0 && skip_block >= -1 && skip_block < 2,
+         "timed_out required, polls > 0, skip_block in {-1, 0, 1}");
+  int dev = 0, coop = 0;
+  FG_CUDA(cudaGetDevice(&dev));
+  FG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) {
+    set_error("the device has no cooperative launch");
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  unsigned int* w = nullptr;  // count, generation, timeout flag
+  FG_CUDA(cudaMalloc(&w, 3 * sizeof(unsigned int)));
+  cudaError_t e = cudaMemset(w, 0, 3 * sizeof(unsigned int));
+  if (e == cudaSuccess) {
+    unsigned int* count = w;
+    unsigned int* gen = w + 1;
+    int* flag = reinterpret_cast<int*>(w + 2);
+    long npolls = (long)polls;
+    void* args[] = {&count, &gen, &flag, &skip_block, &npolls};
+    e = cudaLaunchCooperativeKernel((const void*)k_barrier_check, dim3(2), dim3(32), args, 0,
+                                    nullptr);
+  }
+  int host_flag = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&host_flag, w + 2, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(w);
+  if (e != cudaSuccess) {
+    set_error("grid barrier check: %s", cudaGetErrorString(e));
+    return FREHG_ERR_CUDA;
+  }
+  *timed_out = host_flag;
+  return FREHG_OK;
+}

@@ -89,7 +89,7 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double* partials, unsi
 // the timeout instead of a result).
 constexpr long kGridBarrierPolls = 1L << 24;
 __device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int* gen,
-                                             int* timeout) {
+                                             int* timeout, long max_polls = kGridBarrierPolls) {
   __shared__ int ok;
   __syncthreads();
   if (flat_tid() == 0) {
@@ -103,7 +103,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int* 
       atomicAdd(gen, 1u);
     } else {
       for (long q = 0; *vgen == g; ++q) {
-        if (q >= kGridBarrierPolls) {
+        if (q >= max_polls) {
           good = 0;
           atomicExch(timeout, 1);
           break;

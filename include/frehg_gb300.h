@@ -291,6 +291,12 @@ int frehg_cg_converged_reason(const frehg_cg* cg, int* reason); /* KSPConvergedR
  * two forms sum the dot products over different block partitions, so their last bits (and, in
  * a borderline case, an iteration count) may differ. */
 int frehg_cg_set_fused_iteration(frehg_cg* cg, int on);
+/* Self-check of the one-launch iteration's grid barrier (not in reference): two cooperative
+ * blocks meet at one barrier whose wait is bounded by `polls` polls; skip_block = 0 or 1 makes
+ * that block return without arriving, so the other's wait runs out, sets the timeout flag and
+ * the kernel ends normally (*timed_out = 1; the context stays usable); skip_block = -1: both
+ * arrive (*timed_out = 0). */
+int frehg_check_grid_barrier(int skip_block, long long polls, int* timed_out);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Learned preconditioner (not in reference): 3-level 3D U-Net (16/32/64 channels, 3x3x3 conv,  */

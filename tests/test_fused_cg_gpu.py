@@ -110,3 +110,20 @@ def test_re_step_solves_fused(gpu_lib, oracle_mod, shape):
         o.advance_step()
     assert np.abs(runs[0] - runs[1]).max() <= 1e-10
     assert np.abs(runs[0] - o.interior("h")).max() <= 1e-8
+
+
+def test_grid_barrier_wait_runs_out(gpu_lib):
+    """The barrier's bounded wait: a block that never arrives (nothing else would release the
+    other) makes the other's wait run out; the kernel ends, the flag is set and the context
+    stays usable (a solve runs after it)."""
+    import ctypes as C
+    flag = C.c_int(-1)
+    for skip in (1, 0):
+        assert gpu_lib.frehg_check_grid_barrier(skip, 1 << 12, C.byref(flag)) == 0, \
+            gpu_lib.frehg_last_error()
+        assert flag.value == 1
+    assert gpu_lib.frehg_check_grid_barrier(-1, 1 << 12, C.byref(flag)) == 0
+    assert flag.value == 0
+    rows, cols, vals, _, b = spd_coo(6, 5, 4, seed=1)
+    _, its, reason = solve(6, 5, 4, rows, cols, vals, b, True)
+    assert reason > 0 and its > 0
