@@ -277,6 +277,7 @@ SIGNATURES = {
     "frehg_fastmath_eval": (C.c_int, [C.c_int, _VP, _VP, C.c_int64]),
     "frehg_constit_eval": (C.c_int, [_VP, C.c_int, C.c_int, _VP, C.c_int64, _VP, _VP, _VP]),
     "frehg_re_check_staged_assembly": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
+    "frehg_re_check_staged_wait": (C.c_int, [_VP, _PI]),
     "frehg_unet_conv_check": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -133,7 +133,7 @@ __device__ __forceinline__ void pt_levels(int kb, int ke, int nz, int* lo, int* 
 __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
     ReArgs a, const __grid_constant__ PicTmaMaps m, float* __restrict__ dg,
     float* __restrict__ a0, float* __restrict__ a1, float* __restrict__ a2,
-    double* __restrict__ bvec, int planes, int tiles, int* err) {
+    double* __restrict__ bvec, int planes, int tiles, int* err, int stall_producer = 0) {
   extern __shared__ __align__(128) unsigned char pt_dyn[];
   // the stages start on a 128-byte boundary (the launch adds 128 bytes of slack)
   unsigned char* pt_smem = reinterpret_cast<unsigned char*>(
@@ -162,7 +162,9 @@ __global__ void __launch_bounds__(288, 3) k_pic_assemble_tma(
 
   if (producer) {
     // ---- producer warp: lane 0 issues every level's copies in the consumers' order ----------
-    if (lane == 0) {
+    // (stall_producer, the self-check of the bounded waits: nothing is issued, so the
+    // consumers' first waits run out and the block finishes without reading a stage)
+    if (lane == 0 && !stall_producer) {
       uint32_t seq = 0;
       for (int tile = blockIdx.x; tile < tiles && !abort_flag; tile += gridDim.x) {
         const int x0 = (tile % t0) * 32, y0 = (tile / t0) * 8;

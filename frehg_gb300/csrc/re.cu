@@ -690,7 +690,8 @@ bool pic_tma_maps(const ReArgs& a, const double* ks, PicTmaMaps* m) {
 // Launch the staged assembly (mixed-precision form: float matrix entries).  *launched stays
 // false when the handle's layout does not qualify; the caller then launches k_pic_assemble_ff.
 static int launch_staged_assembly(frehg_re* re, const ReArgs& a, const StencilLaunch& PL,
-                                  float* dgf, const Stencil32& o, double* b, bool* launched) {
+                                  float* dgf, const Stencil32& o, double* b, bool* launched,
+                                  int stall_producer = 0) {
   *launched = false;
   PicTmaMaps maps;
   if (!pic_tma_maps(a, re->fKs, &maps)) return FREHG_OK;
@@ -707,7 +708,8 @@ static int launch_staged_assembly(frehg_re* re, const ReArgs& a, const StencilLa
   const dim3 grid((unsigned)std::max(1L, std::min((long)PL.tiles, per_slab)), PL.grid.y, 1);
   FG_LAUNCH(&re->prof, re->stream, "k_pic_assemble_ff", (72.0 + soil_bytes(re)) * n,
             (k_pic_assemble_tma<<<grid, dim3(32, 9), kPtSmemBytes + 128, re->stream>>>(
-                a, maps, dgf, o.a0, o.a1, o.a2, b, PL.planes, PL.tiles, &re->sc->stage_err)));
+                a, maps, dgf, o.a0, o.a1, o.a2, b, PL.planes, PL.tiles, &re->sc->stage_err,
+                stall_producer)));
   FG_CUDA(cudaGetLastError());
   *launched = true;
   return FREHG_OK;
@@ -1486,6 +1488,61 @@ int frehg_re_get_field(frehg_re* re, const char* name, double* out_halo) {
       for (int i = 0; i < re->nx; ++i) out_halo[(size_t)(i + 1) + (size_t)(j + 1) * hx] = top[(size_t)i + (size_t)re->nx * j];
   }
   return FREHG_OK;
+}
+
+int frehg_re_check_staged_wait(frehg_re* re, int* err_word) {
+  clear_error();
+  FG_ARG(re && err_word, "null argument");
+  FG_ARG(re->finalized, "check before a finalized state");
+  const ReArgs a = make_args(re);
+  if (re->p.scheme != 1 || !picard_ff(re) || !mixed_solve(re) || !re->fKs || (re->nx & 1)) {
+    set_error("the staged assembly serves Picard handles in mixed precision with a per-cell Ks "
+              "field and an even nx");
+    return FREHG_ERR_UNSUPPORTED;
+  }
+  const size_t n = re->n;
+  const StencilLaunch PL = stencil_launch(re->nx, re->ny, re->nz);
+  cudaStream_t st = re->stream;
+  float* f[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* b = nullptr;
+  int rc = FREHG_OK;
+  for (int q = 0; q < 4; ++q)
+    if (cudaMalloc(&f[q], n * sizeof(float)) != cudaSuccess) rc = FREHG_ERR_CUDA;
+  if (cudaMalloc(&b, n * sizeof(double)) != cudaSuccess) rc = FREHG_ERR_CUDA;
+  if (rc != FREHG_OK) set_error("self-check allocation failed");
+  if (rc == FREHG_OK) {
+    Stencil32 o;
+    o.n = n;
+    o.a0 = f[1];
+    o.a1 = f[2];
+    o.a2 = f[3];
+    bool staged = false;
+    rc = launch_staged_assembly(re, a, PL, f[0], o, b, &staged, 1);
+    o.a0 = o.a1 = o.a2 = nullptr;  // not owned
+    if (rc == FREHG_OK && !staged) {
+      set_error("tensor maps of the staged assembly could not be encoded");
+      rc = FREHG_ERR_UNSUPPORTED;
+    }
+    ReScalars sh;
+    if (rc == FREHG_OK && (cudaStreamSynchronize(st) != cudaSuccess ||
+                           cudaMemcpy(&sh, re->sc, sizeof(sh), cudaMemcpyDeviceToHost) !=
+                               cudaSuccess)) {
+      set_error("staged-wait self-check failed: %s", cudaGetErrorString(cudaGetLastError()));
+      rc = FREHG_ERR_CUDA;
+    }
+    if (rc == FREHG_OK) {
+      *err_word = sh.stage_err;
+      const int zero = 0;
+      if (cudaMemcpy(&re->sc->stage_err, &zero, sizeof(int), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+        set_error("staged-wait self-check: resetting the error word failed");
+        rc = FREHG_ERR_CUDA;
+      }
+    }
+  }
+  for (int q = 0; q < 4; ++q) cudaFree(f[q]);
+  cudaFree(b);
+  return rc;
 }
 
 int frehg_re_check_staged_assembly(frehg_re* re, int64_t* mismatches) {

@@ -449,6 +449,12 @@ int frehg_unet_conv_check(int cin, int cout, int in_stride, int in_off, int out_
  * and right-hand-side entries whose bits differ in *mismatches (0: identical).  Returns
  * FREHG_ERR_UNSUPPORTED when the handle's case does not take the staged kernel. */
 int frehg_re_check_staged_assembly(frehg_re* re, int64_t* mismatches);
+/* Self-check of the staged assembly's bounded waits (not in reference): one launch whose
+ * producer warp issues no copies, so every consumer's first wait on a stage runs out (after
+ * about a second); the blocks finish without reading a stage, *err_word receives the kernel's
+ * error word (2: a consumer's wait ran out) and the handle's word is cleared, so the handle
+ * steps normally afterwards.  Same handles as frehg_re_check_staged_assembly. */
+int frehg_re_check_staged_wait(frehg_re* re, int* err_word);
 
 #ifdef __cplusplus
 }

@@ -58,3 +58,23 @@ def test_staged_unsupported_case_reports(gpu_lib):
     g.advance_step()  # the unstaged kernel serves it
     bad = C.c_int64(-1)
     assert g._lib.frehg_re_check_staged_assembly(g._h, C.byref(bad)) == FREHG_ERR_UNSUPPORTED
+
+
+def test_staged_wait_runs_out_and_handle_recovers(gpu_lib):
+    """The staged kernel's bounded waits: with a producer that issues nothing (nothing else
+    would fill a stage) every consumer's first wait runs out, the kernel ends and reports error
+    word 2; the handle then steps normally and the staged kernel still matches the unstaged."""
+    from frehg_gb300.abi import check
+    from frehg_gb300.re_solver import Grid, ReSolver
+    w = W.config4(nx=64, ny=16, nz=24, steps=2, precision=1, pc="line")
+    g = ReSolver(Grid(w.nx, w.ny, w.nz, w.params.dx, w.params.dy, w.params.dz), w.params)
+    g.set_assembly_staging(True)
+    w.apply(g)
+    g.advance_step()
+    err = C.c_int(-1)
+    check(g._lib.frehg_re_check_staged_wait(g._h, C.byref(err)), "check_staged_wait")
+    assert err.value == 2
+    g.advance_step()
+    bad = C.c_int64(-1)
+    check(g._lib.frehg_re_check_staged_assembly(g._h, C.byref(bad)), "check")
+    assert bad.value == 0
