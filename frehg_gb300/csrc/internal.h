@@ -86,8 +86,9 @@ class Profiler {
 // Upper bound of the blocks any reduction kernel launches (partials buffers are sized to it).
 constexpr int kMaxRedBlocks = 32768;
 // largest system the FP64 Jacobi-PCG runs as one launch per iteration by default: on GB300 the
-// one-launch form is 5-8 % faster up to about 32k unknowns and 4-25 % slower from 262k on
-// (its two grid barriers and half occupancy against three kernels' launch gaps)
+// one-launch form is up to 8 % faster up to about 32k unknowns; beyond, its two grid barriers
+// and half occupancy weigh about as much as the three kernels' launch gaps (25 % slower at
+// 262k, 5 % faster at 1M, 6 % slower at 2M and 8.4M unknowns)
 constexpr size_t kFusedAutoCells = 65536;
 constexpr int kNumSMs = 152;
 
