@@ -7,8 +7,8 @@ stated sizes.
   float-float Picard kernels; and the learned arm with the benchmark's trained network forced
   on for every solve.  Per step: head within 1e-8 m of the oracle (max norm), equal Picard
   iteration counts and time steps; on the GPU the cumulative water budget closes below 1e-12.
-* 40x40x100 loam infiltration with the Picard scheme, 120 steps (the PCA scheme at this size is
-  checked against the reference's own outputs in test_golden_gpu.py).
+* 40x40x100 loam infiltration, 120 steps, with the Picard and the PCA scheme (the PCA scheme at
+  this size is also checked against the reference's own outputs in test_golden_gpu.py).
 * 256x256x128 heterogeneous loam: 3 PCA steps and 1 Picard step against the oracle.
 * The 512x512x128 loam's and the three-layer soil's generators on windows, Picard with the
   mixed line-PCG solve.
@@ -110,6 +110,13 @@ def test_config0_picard_full_size(gpu_lib, oracle_mod):
     worst = compare(g, o, w.steps)
     print(f"\n  40x40x100 Picard, 120 steps: max head difference {worst:.2e} m")
     assert budget_rel(g, v0) < 1e-12
+
+
+def test_config0_pca_full_size(gpu_lib, oracle_mod):
+    w = W.config0("pca")  # 40x40x100, 120 steps of 30 s, the reference's scheme
+    g, o = gpu_solver(w), oracle_solver(oracle_mod, w)
+    worst = compare(g, o, w.steps, picard=False)
+    print(f"\n  40x40x100 PCA, 120 steps: max head difference {worst:.2e} m")
 
 
 def test_config1_full_size_pca(gpu_lib, oracle_mod):
