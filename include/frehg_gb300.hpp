@@ -238,6 +238,9 @@ class GpuLinearSolver : public LinearSolver {
     return r;
   }
   const SolverConfig& config() const { return cfg_; }
+  // not in reference: the FP64 Jacobi-PCG iteration as one cooperative launch (1), three
+  // kernels (0) or, by default, one launch up to 65,536 unknowns (-1)
+  void setFusedIteration(int on) { check(frehg_cg_set_fused_iteration(cg_, on), "setFusedIteration"); }
 
  private:
   static StencilSystem& sys(SparseSystem& A) {

@@ -3,7 +3,9 @@
 // test_petsc_linear_solver.cpp:70-102, asks for L2 error < 1e-9), its error behaviour, and the
 // ReSolver interface on the closed heterogeneous box of tests/re/test_re_3d.cpp:210-227 (water
 // volume conserved to 1e-10 relative).  Prints one line per check; exit status 0 when all pass.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -95,6 +97,21 @@ static void seam(const char* precision, const char* pc = "jacobi") {
   const double rel = std::sqrt(e2 / n2);
   EXPECT(rel < 1e-9, "seam %s %s: manufactured Laplacian relative L2 error %.3e (%d iterations)",
          precision, pc, rel, ls->getIterationCount());
+  if (!std::strcmp(precision, "fp64") && !std::strcmp(pc, "jacobi")) {
+    // the same solve as three kernels per iteration instead of one cooperative launch
+    auto* gls = dynamic_cast<g::GpuLinearSolver*>(ls.get());
+    EXPECT(gls != nullptr, "makeLinearSolver(\"gb300\") gives a GpuLinearSolver");
+    const int its1 = ls->getIterationCount();
+    std::vector<double> x3;
+    gls->setFusedIteration(0);
+    ls->solve(*A, b, x3);
+    double dmax = 0.0;
+    for (size_t q = 0; q < x.size(); ++q) dmax = std::max(dmax, std::fabs(x3[q] - x[q]));
+    EXPECT(std::abs(ls->getIterationCount() - its1) <= 1 && dmax < 1e-10,
+           "seam: one-launch and three-kernel iterations agree (%d / %d iterations, %.1e)", its1,
+           ls->getIterationCount(), dmax);
+    gls->setFusedIteration(-1);
+  }
   // getSolution returns the last solve's x
   std::vector<double> x2;
   A->getSolution(x2);
