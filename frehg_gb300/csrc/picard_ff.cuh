@@ -178,6 +178,51 @@ __device__ __forceinline__ void ff_bottom_face(const ReArgs& a, const FfConst& K
   }
 }
 
+// The Picard update and the next iteration's constitutive relations in one pass:
+// h += s x~ with the limiter and |d|_inf exactly as k_pic_update<true>, then theta, K/Ks and C at
+// the new head exactly as k_constit_ff, into kr, th, cap (the caller's second set of arrays:
+// the current ones still hold the values at the previous head, which the final update of a
+// converged step uses).  Same bits as the two kernels; one read of the head instead of two.
+template <bool ALL_FF>
+__global__ void __launch_bounds__(256, 4) k_pic_update_constit_ff(
+    ReArgs a, const double* __restrict__ d, const double* __restrict__ s,
+    double* __restrict__ kr, double* __restrict__ th, double* __restrict__ cap) {
+  const long long kAbs = 0x7fffffffffffffffll;
+  long long m = 0;
+  const double lim = a.picard_dh_max;
+  const long long lim_bits = lim > 0.0 ? __double_as_longlong(lim) : kAbs;
+  const bool col_map = a.soil.cid && !a.soil.cid3d;
+  const bool small = a.n <= 0xffffffffull;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < a.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = !col_map ? 0
+                       : small  ? (size_t)((uint32_t)c % (uint32_t)a.ncol)
+                                : c % a.ncol;
+    const int id = a.soil.cid ? (int)a.soil.cid[a.soil.cid3d ? c : col] : 0;
+    double dc = d[c];
+    dc *= s[c];
+    const double hc = a.h_new[c] + pic_limited(dc, lim_bits, m);
+    a.h_new[c] = hc;
+    const SoilClass& k = a.soil.cls[id];
+    Constit r;
+    if (ALL_FF || (k.use_vg && !k.use_mvg)) {
+      const ff alpha = a.soil.alpha ? ff_from_double_nb(a.soil.alpha[c])
+                                    : ff_make(k.ff_alpha[0], k.ff_alpha[1]);
+      r = vg_constit_ff<true, true>(k, alpha, a.soil.continuous_theta ? 0.0 : k.aev, hc);
+    } else {
+      r = vg_constit<true, true>(soil_of(a.soil, c, col), hc);
+    }
+    kr[c] = r.kr;
+    th[c] = r.theta;
+    cap[c] = r.cap;
+  }
+  m = m > 0x7ff0000000000000ll ? 0x7ff0000000000000ll : m;  // NaN -> inf
+  double tot;
+  if (grid_max(__longlong_as_double(m), a.partials + 2 * kMaxRedBlocks, &a.sc->arrive[1], &tot) &&
+      flat_tid() == 0)
+    a.sc->dq_max = tot;
+}
+
 // The Picard residual's float-float part V Ss (wcn/ths) (h - h_old) - dt q, renormalised (the
 // storage difference and the final combination are FP64)
 __device__ __forceinline__ ff ff_residual_rest(ff V, ff dt, ff st, ff h, double h_old, ff q) {

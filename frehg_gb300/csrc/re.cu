@@ -41,6 +41,11 @@ struct frehg_re {
   double* kr = nullptr;
   double* wch = nullptr;
   double* cap = nullptr;
+  // second set for the float-float Picard update that also forms the next iteration's
+  // constitutive values (allocated on first use; swapped with the first set when taken)
+  double* kr2 = nullptr;
+  double* wch2 = nullptr;
+  double* cap2 = nullptr;
   double* qx = nullptr;
   double* qy = nullptr;
   double* qz = nullptr;
@@ -95,6 +100,9 @@ frehg_re::~frehg_re() {
   cudaFree(kr);
   cudaFree(wch);
   cudaFree(cap);
+  cudaFree(kr2);
+  cudaFree(wch2);
+  cudaFree(cap2);
   cudaFree(qx);
   cudaFree(qy);
   cudaFree(qz);
@@ -754,12 +762,15 @@ static int picard_step(frehg_re* re) {
               k_copy64<<<nb, 256, 0, st>>>(a.h_new, a.h_old, re->n));
     bool converged = false;
     int fail = FREHG_OK;
+    // the previous iteration's update formed this iteration's constitutive values
+    bool constit_ready = false;
     for (its = 0; its < re->p.picard_max_it; ++its) {
       if (!picard_ff(re))
         FG_LAUNCH(prof, st, "k_kr", (32.0 + sb) * n,
                   (k_constit<true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr, re->wch,
                                                              re->cap)));
-      else if (all_ff)
+      else if (constit_ready) {
+      } else if (all_ff)
         FG_LAUNCH(prof, st, "k_kr_ff", (32.0 + sb) * n,
                   (k_constit_ff<true, true, true><<<nb, 256, 0, st>>>(a, a.h_new, re->kr,
                                                                       re->wch, re->cap)));
@@ -815,9 +826,26 @@ static int picard_step(frehg_re* re) {
         fail = rc;
         break;
       }
+      // float-float kernels: the update also forms the constitutive values at the new head
+      // into the second set, which the next iteration takes (a converged step keeps the first
+      // set, at the head its final update needs)
+      const bool fused_update = !sor && picard_ff(re);
+      if (fused_update && !re->kr2) {
+        FG_CUDA(cudaMalloc(&re->kr2, re->n * sizeof(double)));
+        FG_CUDA(cudaMalloc(&re->wch2, re->n * sizeof(double)));
+        FG_CUDA(cudaMalloc(&re->cap2, re->n * sizeof(double)));
+      }
       if (sor)
         FG_LAUNCH(prof, st, "k_pic_update", 24.0 * n,
                   k_pic_update<false><<<nb, 256, 0, st>>>(a, re->scratch));
+      else if (fused_update && all_ff)
+        FG_LAUNCH(prof, st, "k_pic_update_kr_ff", (56.0 + sb) * n,
+                  k_pic_update_constit_ff<true><<<nb, 256, 0, st>>>(
+                      a, re->ksp.x, re->ksp.scale_vector(re->A), re->kr2, re->wch2, re->cap2));
+      else if (fused_update)
+        FG_LAUNCH(prof, st, "k_pic_update_kr_ff", (56.0 + sb) * n,
+                  k_pic_update_constit_ff<false><<<nb, 256, 0, st>>>(
+                      a, re->ksp.x, re->ksp.scale_vector(re->A), re->kr2, re->wch2, re->cap2));
       else
         FG_LAUNCH(prof, st, "k_pic_update", 32.0 * n,
                   k_pic_update<true><<<nb, 256, 0, st>>>(a, re->ksp.x,
@@ -837,6 +865,15 @@ static int picard_step(frehg_re* re) {
         converged = true;
         ++its;
         break;
+      }
+      if (fused_update) {
+        std::swap(re->kr, re->kr2);
+        std::swap(re->wch, re->wch2);
+        std::swap(re->cap, re->cap2);
+        a.kr = re->kr;
+        a.wch = re->wch;
+        a.cap = re->cap;
+        constit_ready = true;
       }
     }
     if (converged) break;
