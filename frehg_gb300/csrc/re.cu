@@ -55,6 +55,10 @@ struct frehg_re {
   uint8_t* flags = nullptr;
   double* scratch = nullptr;  // n doubles for exports / Picard increments
   bool staged = false;        // Picard assembly staged through TMA (frehg_re_set_assembly_staging)
+  // kr, wch, cap hold the values at the current head: set by a converged float-float Picard
+  // step (its last update formed them), taken by the next step's first iteration, and cleared
+  // by every call that changes the head, the soil, the parameters or the solver
+  bool constit_fresh = false;
   ReScalars* sc = nullptr;
   ReScalars* sc_host = nullptr;
   double* partials = nullptr;
@@ -574,6 +578,7 @@ static double soil_bytes(const frehg_re* re) {
 // PCA step (ReSolver::advanceStep, ReSolver.cpp:931-969)
 
 static int pca_step(frehg_re* re) {
+  re->constit_fresh = false;  // the step writes kr and cap at other heads
   cudaStream_t st = re->stream;
   ReArgs a = make_args(re);
   const int nb = nblocks(re->n);
@@ -755,6 +760,10 @@ static int picard_step(frehg_re* re) {
   const bool f32 = picard_ff(re) && mixed_solve(re);
   if (f32) FG_TRY(re->ksp.ensure32(re->n));
   int its = 0;
+  // the previous step's last update formed the constitutive values at this step's start
+  bool reuse = re->constit_fresh && picard_ff(re);
+  re->constit_fresh = false;
+  bool last_fused = false;
   for (;;) {
     FG_CUDA(cudaMemcpyAsync(&re->sc->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st));
     FG_LAUNCH(prof, st, "k_step_begin", 0.0, k_step_begin<<<1, 1, 0, st>>>(re->sc));
@@ -762,8 +771,11 @@ static int picard_step(frehg_re* re) {
               k_copy64<<<nb, 256, 0, st>>>(a.h_new, a.h_old, re->n));
     bool converged = false;
     int fail = FREHG_OK;
-    // the previous iteration's update formed this iteration's constitutive values
-    bool constit_ready = false;
+    // the previous iteration's update formed this iteration's constitutive values (or the
+    // previous step's, for the first attempt's first iteration)
+    bool constit_ready = reuse;
+    reuse = false;
+    last_fused = false;
     for (its = 0; its < re->p.picard_max_it; ++its) {
       if (!picard_ff(re))
         FG_LAUNCH(prof, st, "k_kr", (32.0 + sb) * n,
@@ -830,6 +842,7 @@ static int picard_step(frehg_re* re) {
       // into the second set, which the next iteration takes (a converged step keeps the first
       // set, at the head its final update needs)
       const bool fused_update = !sor && picard_ff(re);
+      last_fused = fused_update;
       if (fused_update && !re->kr2) {
         FG_CUDA(cudaMalloc(&re->kr2, re->n * sizeof(double)));
         FG_CUDA(cudaMalloc(&re->wch2, re->n * sizeof(double)));
@@ -903,6 +916,14 @@ static int picard_step(frehg_re* re) {
               (k_pic_assemble_ff<false, true, double><<<PL.grid, PL.block, 0, st>>>(
                   a, nullptr, nullptr, nullptr, nullptr, nullptr, PL.planes, PL.tiles)));
   FG_CUDA(cudaGetLastError());
+  if (last_fused) {
+    // the last update formed the values at the step's final head (the final update above,
+    // launched with the frozen set, leaves the head as it is): the next step starts with them
+    std::swap(re->kr, re->kr2);
+    std::swap(re->wch, re->wch2);
+    std::swap(re->cap, re->cap2);
+    re->constit_fresh = true;
+  }
   re->cnt.last_picard_iterations = its;
   if (re->p.picard_dt_adapt) {
     // Picard-count controller: grow after <= 3 iterations, shrink after >= 8, within
@@ -1039,6 +1060,7 @@ int frehg_re_destroy(frehg_re* re) {
 
 int frehg_re_set_params(frehg_re* re, const frehg_re_params* p) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && p, "null argument");
   FG_TRY(validate_params(p));
   const double old_dt = re->p.dt;
@@ -1063,6 +1085,7 @@ int frehg_re_get_params(const frehg_re* re, frehg_re_params* p) {
 int frehg_re_set_soil_map(frehg_re* re, const frehg_soil_params* classes, int nclass,
                           const int32_t* class_index, int is3d) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && classes && class_index, "null argument");
   FG_ARG(nclass >= 1 && nclass <= 256, "nclass must be in [1, 256]");
   const size_t cnt = is3d ? re->n : re->ncol;
@@ -1089,6 +1112,7 @@ int frehg_re_set_soil_map(frehg_re* re, const frehg_soil_params* classes, int nc
 
 int frehg_re_set_cell_fields(frehg_re* re, const double* Ks, const double* alpha) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re, "null handle");
   FG_CUDA(cudaStreamSynchronize(re->stream));
   cudaFree(re->fKs);
@@ -1107,6 +1131,7 @@ int frehg_re_set_cell_fields(frehg_re* re, const double* Ks, const double* alpha
 
 int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && cfg, "null argument");
   if (strcmp(cfg->ksp_type, "cg") != 0 && strcmp(cfg->ksp_type, "fcg") != 0) {
     set_error("ksp_type '%s' is not available (cg, fcg)", cfg->ksp_type);
@@ -1137,6 +1162,7 @@ int frehg_re_attach_solver(frehg_re* re, const frehg_solver_config* cfg) {
 
 int frehg_re_initialize_geometry(frehg_re* re) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re, "null handle");
   re->have_geometry = true;  // uniform dz per layer, every cell active (ReSolver.cpp:104-131)
   return FREHG_OK;
@@ -1144,6 +1170,7 @@ int frehg_re_initialize_geometry(frehg_re* re) {
 
 int frehg_re_set_initial_head(frehg_re* re, const double* h) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && h, "null argument");
   FG_TRY(wait_copies(re, -1, true));
   FG_CUDA(cudaStreamSynchronize(re->stream));
@@ -1158,6 +1185,7 @@ int frehg_re_set_initial_head(frehg_re* re, const double* h) {
 
 int frehg_re_set_initial_water_content(frehg_re* re, const double* wc) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && wc, "null argument");
   FG_TRY(wait_copies(re, -1, true));
   FG_CUDA(cudaStreamSynchronize(re->stream));
@@ -1172,6 +1200,7 @@ int frehg_re_set_initial_water_content(frehg_re* re, const double* wc) {
 
 int frehg_re_finalize_initial_state(frehg_re* re) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re, "null handle");
   FG_TRY(wait_copies(re, -1, true));
   if (!re->have_state) {
@@ -1201,6 +1230,7 @@ int frehg_re_finalize_initial_state(frehg_re* re) {
 
 int frehg_re_initialize_uniform_column(frehg_re* re, double init_wc) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re, "null handle");
   FG_TRY(frehg_re_initialize_geometry(re));
   std::vector<double> w(re->n, init_wc);
@@ -1278,6 +1308,7 @@ int frehg_re_surface_exchange(frehg_re* re, double* eta, const double* bottom, d
                               double visc, double min_depth, double* q_out, double* total,
                               int on_device) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && eta && bottom && q_out && total, "null argument");
   FG_TRY(wait_copies(re, -1, true));
   FG_ARG(dt > 0.0, "dt must be positive");
@@ -1347,6 +1378,7 @@ int frehg_re_checkpoint(frehg_re* re, double* h, double* wc, double* state) {
 
 int frehg_re_restart(frehg_re* re, const double* h, const double* wc, const double* state) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && h && wc && state, "null argument");
   FG_TRY(wait_copies(re, -1, true));
   FG_ARG(state[1] > 0.0 && state[2] > 0.0, "checkpoint state has no positive dt");
@@ -1674,6 +1706,7 @@ int frehg_re_get_counters(const frehg_re* re, frehg_re_counters* c) {
 
 int frehg_re_attach_unet(frehg_re* re, frehg_unet* net) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re, "null handle");
   FG_ARG(re->nx % 4 == 0 && re->ny % 4 == 0 && re->nz % 4 == 0,
          "the learned preconditioner needs nx, ny, nz divisible by 4");
@@ -1723,6 +1756,7 @@ int frehg_re_set_learned_policy(frehg_re* re, int probe_every, double max_ratio)
 int frehg_re_training_pairs(frehg_re* re, int npairs, const int* iters, int target,
                             float* r_out, float* e_out, float* lnk_out, float* cap_out) {
   clear_error();
+  if (re) re->constit_fresh = false;
   FG_ARG(re && iters && r_out && e_out && lnk_out && cap_out && npairs > 0, "bad argument");
   FG_ARG(target >= 0 && target <= 2, "target must be 0 (error), 1 (error - r) or 2 "
          "(error - line solve of r)");
