@@ -130,3 +130,25 @@ def test_record_missing_or_mismatched_fields(gpu_lib):
     bad = dict(rec, gw_h=rec["gw_h"][:-1])
     with pytest.raises(RuntimeError, match="size mismatch"):
         g.restart_from_record(bad)
+
+
+def test_constitutive_values_follow_a_soil_change(gpu_lib):
+    """A converged float-float Picard step hands its last update's constitutive values to the
+    next step; a change of the soil in between must discard them.  The step after the change
+    equals, bit for bit, that of a handle built with the new soil and restarted from the same
+    state."""
+    import dataclasses
+    w = W.config1("picard", nx=16, ny=12, nz=24, steps=3, precision=1)
+    w.solver.pc_type = b"line"
+    a = new(w)
+    a.advance_step()
+    a.advance_step()
+    cp = a.checkpoint()
+    alpha2 = w.alpha * 1.3
+    a.set_cell_fields(w.Ks, alpha2)
+    a.advance_step()
+    b = new(dataclasses.replace(w, alpha=alpha2))
+    b.restart(cp)
+    b.advance_step()
+    assert np.array_equal(a.interior("h"), b.interior("h"))
+    assert np.array_equal(a.interior("wc"), b.interior("wc"))
