@@ -43,34 +43,28 @@ __device__ __forceinline__ int converged_test(CgDevState* s, double rnorm) {
 // ------------------------------------------------------------------------------------------
 // geometry helpers
 
-// target: the blocks aimed at; total_cap: the most blocks in all
-static StencilLaunch stencil_launch_for(int n0, int n1, int n2, long target, long total_cap) {
+StencilLaunch stencil_launch(int n0, int n1, int n2) {
   StencilLaunch L;
   L.block = dim3(32, 8, 1);
   const int t0 = (n0 + 31) / 32, t1 = (n1 + 7) / 8;
   const long tiles = (long)t0 * t1;
+  // about two waves of 8 resident (32 x 8)-thread blocks per SM; the launch shape, and with
+  // it the summation tree of the reductions, depends on the grid sizes only
+  const long target = (long)kNumSMs * 8 * 2;
   long z = target / (tiles > 0 ? tiles : 1);
   if (z < 1) z = 1;
   if (z > n2) z = n2;
   int planes = (int)((n2 + z - 1) / z);
   z = (n2 + planes - 1) / planes;
-  // blocks stride over tiles when there are more tiles than the cap allows
+  // blocks stride over tiles when there are more tiles than reduction partial slots
   long gx = tiles;
-  const long cap = total_cap / z;
+  const long cap = kMaxRedBlocks / z;
   if (gx > cap) gx = cap;
-  if (gx < 1) gx = 1;
   L.planes = planes;
   L.tiles = (int)tiles;
   L.grid = dim3((unsigned)gx, (unsigned)z, 1);
   return L;
 }
-
-StencilLaunch stencil_launch(int n0, int n1, int n2) {
-  // about two waves of 8 resident (32 x 8)-thread blocks per SM; the launch shape, and with
-  // it the summation tree of the reductions, depends on the grid sizes only
-  return stencil_launch_for(n0, n1, n2, (long)kNumSMs * 8 * 2, kMaxRedBlocks);
-}
-
 
 namespace {
 __global__ void k_fetch_words(const unsigned* __restrict__ src, unsigned* __restrict__ dst,
