@@ -11,11 +11,12 @@
 //    is Jacobi-PCG on A (x~ = D^1/2 x, r~ = D^-1/2 r, beta = r.z = r~.r~, p'Ap = p~'A~p~,
 //    ||B r|| = ||s r~|| with s = D^-1/2), so the diagonal is never stored or multiplied and
 //    no divisions remain in the loop.
-//  * One cooperative launch per iteration (k_cg_iter: p-update, stencil SpMV + p.w, update +
-//    two norms, separated by two bounded grid barriers), or, where the device has no
-//    cooperative launch, the same three phases as three kernels; the last reduction ends in
-//    the last-arriving block, which also runs the scalar part of the algorithm (beta,
-//    stopping test) on the device.  Launches of a converged solve return at once, so
+//  * Three phases per iteration (p-update, stencil SpMV + p.w, update + two norms), as one
+//    cooperative launch (k_cg_iter, the phases separated by two bounded grid barriers; by
+//    default for systems of up to kFusedAutoCells unknowns) or as three kernels (larger
+//    systems, or devices without cooperative launch); the last reduction ends in the
+//    last-arriving block, which also runs the scalar part of the algorithm (beta, stopping
+//    test) on the device.  Launches of a converged solve return at once, so
 //    iterations are captured in a CUDA graph of `chunk` iterations and the host only reads
 //    the status between chunks.  Reductions are deterministic (fixed block partition, fixed
 //    summation tree).
