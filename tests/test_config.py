@@ -108,6 +108,11 @@ def test_parameter_mapping():
     # per-class overrides win over the groundwater-level keys (src/soil/SoilConfig.cpp:22-29)
     d["soil"]["types"][0]["specific_storage"] = 2e-5
     assert cf.soil_classes(d)[0].Ss == 2e-5
+    # Picard kernel precision: unset follows the solve (-1), true FP64 (1), false float-float
+    assert p.picard_fp64 == -1
+    for v, want in ((True, 1), (False, 0)):
+        d["groundwater"]["picard_fp64"] = v
+        assert cf.re_params(d, scheme).picard_fp64 == want
 
 
 def test_capability_gate():
